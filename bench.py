@@ -1,0 +1,338 @@
+"""Benchmark: point inversions/s on one GB300 (mixed precision vs plain FP64).
+
+Workload (default "large"): one bicubic rational B-spline surface, 64x64 control net, clamped
+non-uniform knots (interior gaps U[0.5,1.5]), z = 0.1 N(0,1) smoothed by a 5-point stencil,
+w ~ U[0.5,2]; 2^20 inversion queries P = S(u,v) + |N(0,1e-2)| n(u,v).  Seeded synthetic data.
+
+A step = one nurbs_invert launch over the whole query batch with the queries resident in HBM
+(`value`).  `e2e` repeats it through nurbs_invert_host with pinned host buffers: the
+host->device copy of the queries and the device->host copy of uv/status/residual are inside
+each timed step.  L2 is flushed (a 512 MB write) before every timed step.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload ...]
+
+Under torchrun (N > 1) every rank inverts its own batch of the same size (weak scaling, no
+data-path collective); rank 0 prints the JSON line with the max time over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import importlib.util
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG_DIR = os.path.join(ROOT, "gpu-nurbs_gb300")
+sys.path.insert(0, ROOT)
+
+METRIC = "point inversions/s at <=1e-9 param err, mixed vs plain FP64; serve p50/p99 ms"
+
+
+def load_pkg():
+    if "gpu_nurbs_gb300" in sys.modules:
+        return sys.modules["gpu_nurbs_gb300"]
+    spec = importlib.util.spec_from_file_location("gpu_nurbs_gb300", os.path.join(PKG_DIR, "__init__.py"),
+                                                  submodule_search_locations=[PKG_DIR])
+    mod = importlib.util.module_from_spec(spec)
+    sys.modules["gpu_nurbs_gb300"] = mod
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={gpu_index}", f"--query-gpu={self.FIELDS}",
+                                       "--format=csv,noheader,nounits", "-lms", "100"], stdout=self.f,
+                                      stderr=subprocess.DEVNULL)
+        except (FileNotFoundError, OSError):
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        self.f.flush()
+        rows = [l.split(",") for l in open(self.f.name).read().strip().splitlines() if l.strip()]
+        os.unlink(self.f.name)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+                for k, nm in enumerate(names):
+                    if r[5 + k].strip() == "Active":
+                        reasons.add(nm)
+            except (ValueError, IndexError):
+                continue
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_workload(gn, torch, name, n, seed):
+    from gpu_nurbs_gb300 import synth
+    if name == "large":
+        surf, kind = synth.surface_large(), "large"
+    elif name == "small":
+        surf, kind = synth.surface_small(), "small"
+    elif name == "quintic":
+        surf, kind = synth.surface_quintic(), "small"
+    else:
+        raise SystemExit(f"unknown workload {name}")
+    s = gn.Surface(surf)
+    uv, off = synth.query_params(n, seed, kind)
+    E = s.eval(torch.as_tensor(uv, device="cuda"), gn.S | gn.SU | gn.SV).cpu().numpy()
+    P = synth.form_queries(E[0:3].T, E[3:6].T, E[6:9].T, off)
+    return surf, s, uv, P
+
+
+def fp64_peak_tflops(torch):
+    """FP64 FMA throughput of this GPU, measured with the library-independent probe kernel
+    shipped in the package (independent FMA chains; 2 flops per FMA)."""
+    gn = load_pkg()
+    import ctypes as C
+    L = gn.lib()
+    if not hasattr(L, "nurbs_probe_fp_peak"):
+        return None, None
+    f = L.nurbs_probe_fp_peak
+    f.restype = C.c_int
+    f.argtypes = [C.c_int, C.POINTER(C.c_double), C.c_void_p]
+    out = C.c_double()
+    st = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    best64 = best32 = 0.0
+    for _ in range(3):
+        if f(64, C.byref(out), st) == 0:
+            best64 = max(best64, out.value)
+        if f(32, C.byref(out), st) == 0:
+            best32 = max(best32, out.value)
+    return best64 or None, best32 or None
+
+
+def run_ours(a):
+    import torch
+    import torch.distributed as dist
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl")
+    gn = load_pkg()
+    n = a.queries
+    surf, s, uv_true, P = make_workload(gn, torch, a.workload, n, 1000 + rank)
+    Pd = torch.as_tensor(P, device="cuda")
+    uv = torch.empty((n, 2), dtype=torch.float64, device="cuda")
+    st = torch.empty(n, dtype=torch.int32, device="cuda")
+    res = torch.empty(n, dtype=torch.float64, device="cuda")
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+
+    def timed(fn, steps):
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        for k in range(steps):
+            flush.fill_(float(k))
+            evs[k][0].record(stream)
+            fn()
+            evs[k][1].record(stream)
+        torch.cuda.synchronize()
+        return [e0.elapsed_time(e1) for e0, e1 in evs]
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+
+    inv_mixed = lambda: s.invert(Pd, gn.PREC_MIXED, out=(uv, st, res))
+    inv_fp64 = lambda: s.invert(Pd, gn.PREC_FP64, out=(uv, st, res))
+    # pinned host buffers for the end-to-end leg
+    Ph = torch.from_numpy(P).pin_memory().numpy()
+    huv = torch.empty((n, 2), dtype=torch.float64).pin_memory().numpy()
+    hst = torch.empty(n, dtype=torch.int32).pin_memory().numpy()
+    hres = torch.empty(n, dtype=torch.float64).pin_memory().numpy()
+    inv_host = lambda: s.invert_host(Ph, gn.PREC_MIXED, out=(huv, hst, hres))
+
+    for _ in range(a.warmup):
+        inv_mixed()
+        inv_fp64()
+    torch.cuda.synchronize()
+    # accuracy of this run's mixed results against the generating parameters
+    inv_mixed()
+    g_uv, g_st = uv.cpu().numpy(), st.cpu().numpy()
+    found = g_st == 0
+    err = np.abs(g_uv - uv_true).max(1)
+    acc = {"found_frac": float(found.mean()),
+           "uv_err_vs_truth_p50": float(np.median(err[found])) if found.any() else None,
+           "uv_err_vs_truth_p99": float(np.percentile(err[found], 99)) if found.any() else None,
+           "frac_found_within_1e9_of_truth": float((err[found] <= 1e-9).mean()) if found.any() else None}
+
+    clocks = Clocks(local)
+    barrier()
+    t_mixed = timed(inv_mixed, a.steps)
+    barrier()
+    clk = clocks.stop()
+    barrier()
+    t_fp64 = timed(inv_fp64, max(3, a.steps // 2))
+    barrier()
+    # e2e through the C-ABI with host buffers
+    for _ in range(2):
+        inv_host()
+    barrier()
+    t_e2e = []
+    for k in range(a.steps):
+        flush.fill_(float(k))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        inv_host()
+        t_e2e.append((time.perf_counter() - t0) * 1e3)
+    barrier()
+
+    def agg(ts):
+        tot = sum(ts)
+        if world > 1:
+            t = torch.tensor([tot], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            tot = float(t.item())
+        return tot / len(ts)
+
+    ms_mixed, ms_fp64, ms_e2e = agg(t_mixed), agg(t_fp64), agg(t_e2e)
+    if rank != 0:
+        if world > 1:
+            dist.destroy_process_group()
+        return
+    peak64, peak32 = fp64_peak_tflops(torch)
+    k1 = surf["p"] + 1
+    k2 = surf["q"] + 1
+    # nominal algorithmic work per query (p=q=3: ~2.6 kflop): (1+I) evaluations of S,Su,Sv
+    # plus I 2x2 solves, I = 6 iterations
+    I = 6
+    flop_q = (1 + I) * 2 * (4 * k1 * k2 * 2 + 4 * k1 * 3) + I * 30
+    qps = n * world / (ms_mixed / 1e3)
+    achieved = flop_q * n / (ms_mixed / 1e3) / 1e12
+    line = {
+        "metric": METRIC,
+        "value": qps,
+        "unit": "inversions/s",
+        "n_gpus": world,
+        "steps": a.steps,
+        "warmup": a.warmup,
+        "ms_per_step": ms_mixed,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "fp32+fp64 (mixed)",
+        "data": "synthetic (seeded)",
+        "config": {"workload": f"{a.workload}: bicubic 64x64 net, 2^{int(np.log2(n))} queries, offsets |N(0,1e-2)|"
+                   if a.workload == "large" else a.workload,
+                   "queries_per_step": n, "precision": "mixed", "l2": "flushed (512 MB write) before each step",
+                   "parallelism": f"replicas x{world}"},
+        "fp64_value": n * world / (ms_fp64 / 1e3),
+        "fp64_ms_per_step": ms_fp64,
+        "mixed_vs_fp64": ms_fp64 / ms_mixed,
+        "accuracy": acc,
+        "e2e": {"value": n * world / (ms_e2e / 1e3), "unit": "inversions/s", "h2d_bytes_per_step": n * 24,
+                "d2h_bytes_per_step": n * (16 + 4 + 8), "ms_per_step": ms_e2e},
+        "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak64, "unit": "TFLOP/s",
+                     "frac": (achieved / peak64) if peak64 else None, "traffic": None,
+                     "peak_source": "FP64 FMA probe kernel run in this process",
+                     "fp32_peak": peak32, "flop_per_query_nominal": flop_q},
+        "clocks": clk,
+        "gpu_launches": a.steps,
+    }
+    if not a.no_cpu:
+        line["cpu_baseline"] = cpu_baseline(surf, P, a.cpu_sample)
+    print(json.dumps(line))
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def cpu_baseline(surf, P, sample):
+    """The oracle (C restatement of the reference FP64 path) on all host cores, bounded sample."""
+    import oracle as O
+    cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
+    o = O.OracleSurface(surf)
+    o.tree()
+    Ps = P[:sample]
+    t0 = time.perf_counter()
+    o.invert(Ps, threads=cores)
+    dt = time.perf_counter() - t0
+    return {"value": len(Ps) / dt, "unit": "inversions/s", "cores": cores, "kind": "port",
+            "sample": f"{len(Ps)} queries of the same workload, converged-GN oracle, {dt:.2f} s wall"}
+
+
+def run_reference(a):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    load_pkg()
+    from gpu_nurbs_gb300 import synth
+    import oracle as O
+    surf = synth.surface_large() if a.workload == "large" else synth.surface_small()
+    o = O.OracleSurface(surf)
+    uv, off = synth.query_params(a.cpu_sample, 1000, "large" if a.workload == "large" else "small")
+    E = o.eval(uv, 7)
+    P = synth.form_queries(E[0:3].T, E[3:6].T, E[6:9].T, off)
+    o.tree()
+    cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
+    for _ in range(min(a.warmup, 1)):
+        o.invert(P[:1024], threads=cores)
+    ts = []
+    for _ in range(a.steps):
+        t0 = time.perf_counter()
+        o.invert(P, threads=cores)
+        ts.append(time.perf_counter() - t0)
+    dt = sum(ts) / len(ts)
+    v = len(P) / dt
+    kind = "reference" if O.ref_lib() is not None else "port"
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "inversions/s", "n_gpus": world,
+        "steps": a.steps, "warmup": a.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "fp64", "data": "synthetic (seeded)",
+        "config": {"workload": a.workload, "queries_per_step": len(P)},
+        "cpu_baseline": {"value": v, "unit": "inversions/s", "cores": cores, "kind": "port",
+                         "sample": f"{len(P)} queries per step (bounded sample of the workload), all host cores"},
+        "e2e": {"value": v, "unit": "inversions/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="large", choices=["large", "small", "quintic"])
+    ap.add_argument("--queries", type=int, default=1 << 20)
+    ap.add_argument("--cpu-sample", type=int, default=1 << 14)
+    ap.add_argument("--no-cpu", action="store_true")
+    a = ap.parse_args()
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_ours(a)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,294 @@
+"""gpu_nurbs_gb300 — Python host binding of the GB300 NURBS engine.
+
+Thin ctypes layer over ``libgpunurbs.so`` (the C-ABI of ``include/gpu_nurbs.h``).  It mirrors
+the reference's calls (Qiang-Zou/GPU-NURBS): ``read_nu`` for ``readNu`` (src/main.cu:45-113),
+``Surface`` for the GetMatrixN upload (src/NURBS/Evaluate.cu:3-88), ``Surface.eval`` for
+MatrixSurfacePoint / MatrixSurfaceDerivative* (Evaluate.cu:159-930), ``Surface.tree`` and
+``Surface.candidates`` for the subdivision tree and the NewInverse scan (src/kernel/kernel.cu),
+and ``Surface.invert`` for NewInverse + GaussNewton.
+
+Device buffers are torch CUDA tensors (torch is used for device memory and streams only);
+all computation happens in the library's CUDA kernels.  There is no CPU fallback: if the
+library is missing, importing this module raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Optional
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libgpunurbs.so")
+
+OK = 0
+E_INVALID, E_CUDA, E_NOMEM, E_IO, E_PARSE, E_UNSUPPORTED, E_BUDGET, E_TIMEOUT, E_STATE = range(-1, -10, -1)
+S, SU, SV, SUU, SUV, SVV = 1, 2, 4, 8, 16, 32
+PREC_FP64, PREC_MIXED, PREC_FP32 = 0, 1, 2
+INV_FOUND, INV_AMBIGUOUS, INV_NO_CANDIDATE, INV_NOT_CONVERGED = 0, 1, 2, 3
+PTR_HOST, PTR_DEVICE = 0, 1
+TREE_NODES = 65
+
+
+class NurbsError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{msg} (status {code})")
+        self.code = code
+
+
+class NuDesc(C.Structure):
+    _fields_ = [("degree_u", C.c_int), ("degree_v", C.c_int), ("cp_u", C.c_int), ("cp_v", C.c_int),
+                ("knots_u", C.POINTER(C.c_double)), ("knots_v", C.POINTER(C.c_double)),
+                ("cps", C.POINTER(C.c_double)), ("weights", C.POINTER(C.c_double))]
+
+
+class SurfaceInfo(C.Structure):
+    _fields_ = [("degree_u", C.c_int), ("degree_v", C.c_int), ("cp_u", C.c_int), ("cp_v", C.c_int),
+                ("spans_u", C.c_int), ("spans_v", C.c_int), ("device_bytes", C.c_int64), ("tree_built", C.c_int)]
+
+
+_vp = C.c_void_p
+_i64 = C.c_int64
+
+# name -> (restype, argtypes); the list is the C-ABI of include/gpu_nurbs.h
+SIGNATURES = {
+    "nurbs_status_string": (C.c_char_p, [C.c_int]),
+    "nurbs_last_error": (C.c_char_p, []),
+    "nurbs_version": (C.c_char_p, []),
+    "nurbs_nu_read": (C.c_int, [C.c_char_p, C.POINTER(NuDesc)]),
+    "nurbs_nu_parse": (C.c_int, [C.c_char_p, _i64, C.POINTER(NuDesc)]),
+    "nurbs_nu_write": (C.c_int, [C.c_char_p, C.POINTER(NuDesc)]),
+    "nurbs_nu_free": (None, [C.POINTER(NuDesc)]),
+    "nurbs_surface_create": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, _vp, _vp, _vp, _vp, C.c_int, _vp,
+                                       C.POINTER(_vp)]),
+    "nurbs_surface_destroy": (C.c_int, [_vp]),
+    "nurbs_surface_info": (C.c_int, [_vp, C.POINTER(SurfaceInfo)]),
+    "nurbs_matrix_n_size": (_i64, [C.c_int, C.c_int, C.c_int, C.c_int]),
+    "nurbs_matrix_n_position": (_i64, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]),
+    "nurbs_get_matrix_n": (C.c_int, [_vp, _vp, _vp]),
+    "nurbs_get_matrix_n_raw": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int, _vp, _vp, _vp, _vp, _vp]),
+    "nurbs_eval": (C.c_int, [_vp, _vp, _i64, C.c_uint, _vp, C.c_int, _vp]),
+    "nurbs_eval_f32": (C.c_int, [_vp, _vp, _i64, C.c_uint, _vp, _vp]),
+    "nurbs_evaluate_random": (C.c_int, [_vp, _vp, _i64, _vp, C.c_int, C.c_int, C.c_int, C.c_int, _vp, _vp, _vp]),
+    "nurbs_build_tree": (C.c_int, [_vp, C.c_int, _vp]),
+    "nurbs_tree_export": (C.c_int, [_vp, _vp, _vp, _vp]),
+    "nurbs_candidates": (C.c_int, [_vp, _vp, _i64, _vp, _vp, _vp]),
+    "nurbs_invert": (C.c_int, [_vp, _vp, _i64, _vp, _vp, _vp, C.c_int, _vp]),
+    "nurbs_invert_host": (C.c_int, [_vp, _vp, _i64, _vp, _vp, _vp, C.c_int, _vp]),
+    "nurbs_probe_fp_peak": (C.c_int, [C.c_int, C.POINTER(C.c_double), _vp]),
+}
+
+_lib = None
+
+
+def lib():
+    """The loaded C-ABI library (raises if it was not built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"libgpunurbs.so not built at {LIB_PATH}; run __graft_entry__.build()")
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def check(rc: int, what: str = ""):
+    if rc != OK:
+        msg = lib().nurbs_last_error().decode(errors="replace")
+        raise NurbsError(rc, f"{what}: {msg or lib().nurbs_status_string(rc).decode()}")
+
+
+# ------------------------------------------------------------------------ .nu files
+def _desc_to_dict(d: NuDesc) -> dict:
+    p, q, nu, nv = d.degree_u, d.degree_v, d.cp_u, d.cp_v
+    return dict(p=p, q=q, nu=nu, nv=nv,
+                knots_u=np.ctypeslib.as_array(d.knots_u, (p + nu + 1,)).copy(),
+                knots_v=np.ctypeslib.as_array(d.knots_v, (q + nv + 1,)).copy(),
+                cps=np.ctypeslib.as_array(d.cps, (nu * nv * 3,)).copy().reshape(nu * nv, 3),
+                weights=np.ctypeslib.as_array(d.weights, (nu * nv,)).copy())
+
+
+def read_nu(path: str) -> dict:
+    """Reads a .nu file with the library's reader (readNu grammar)."""
+    d = NuDesc()
+    rc = lib().nurbs_nu_read(path.encode(), C.byref(d))
+    if rc != OK:
+        raise NurbsError(rc, f"nurbs_nu_read({path})")
+    try:
+        return _desc_to_dict(d)
+    finally:
+        lib().nurbs_nu_free(C.byref(d))
+
+
+def parse_nu(text: str) -> dict:
+    b = text.encode()
+    d = NuDesc()
+    rc = lib().nurbs_nu_parse(b, len(b), C.byref(d))
+    if rc != OK:
+        raise NurbsError(rc, "nurbs_nu_parse")
+    try:
+        return _desc_to_dict(d)
+    finally:
+        lib().nurbs_nu_free(C.byref(d))
+
+
+def write_nu(path: str, surf: dict):
+    ku = np.ascontiguousarray(surf["knots_u"], np.float64)
+    kv = np.ascontiguousarray(surf["knots_v"], np.float64)
+    cps = np.ascontiguousarray(surf["cps"], np.float64).reshape(-1)
+    w = np.ascontiguousarray(surf["weights"], np.float64)
+    dp = C.POINTER(C.c_double)
+    d = NuDesc(int(surf["p"]), int(surf["q"]), int(surf["nu"]), int(surf["nv"]), ku.ctypes.data_as(dp),
+               kv.ctypes.data_as(dp), cps.ctypes.data_as(dp), w.ctypes.data_as(dp))
+    check(lib().nurbs_nu_write(path.encode(), C.byref(d)), "nurbs_nu_write")
+
+
+# -------------------------------------------------------------------------- helpers
+def _torch():
+    import torch
+    return torch
+
+
+def _stream(stream=None):
+    if stream is not None:
+        return stream
+    torch = _torch()
+    return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def _ptr(t) -> int:
+    return t.data_ptr()
+
+
+# -------------------------------------------------------------------------- surface
+class Surface:
+    """A surface resident on the GPU in matrix form, with its subdivision tree."""
+
+    def __init__(self, surf: dict, stream=None):
+        self.p, self.q = int(surf["p"]), int(surf["q"])
+        self.nu, self.nv = int(surf["nu"]), int(surf["nv"])
+        ku = np.ascontiguousarray(surf["knots_u"], np.float64)
+        kv = np.ascontiguousarray(surf["knots_v"], np.float64)
+        cps = np.ascontiguousarray(surf["cps"], np.float64).reshape(-1)
+        w = np.ascontiguousarray(surf["weights"], np.float64).reshape(-1)
+        h = C.c_void_p()
+        rc = lib().nurbs_surface_create(self.p, self.q, self.nu, self.nv, ku.ctypes.data, kv.ctypes.data,
+                                        cps.ctypes.data, w.ctypes.data, PTR_HOST, _stream(stream), C.byref(h))
+        check(rc, "nurbs_surface_create")
+        self.h = h
+        self.knots_u, self.knots_v = ku, kv
+
+    def close(self):
+        if getattr(self, "h", None) and self.h.value:
+            lib().nurbs_surface_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def info(self) -> SurfaceInfo:
+        i = SurfaceInfo()
+        check(lib().nurbs_surface_info(self.h, C.byref(i)), "nurbs_surface_info")
+        return i
+
+    def matrix_n(self, stream=None):
+        """The span matrices in the reference MatrixN layout (empty spans zero)."""
+        torch = _torch()
+        n = lib().nurbs_matrix_n_size(self.p, self.q, self.nu, self.nv)
+        out = torch.zeros(n, dtype=torch.float64, device="cuda")
+        check(lib().nurbs_get_matrix_n(self.h, _ptr(out), _stream(stream)), "nurbs_get_matrix_n")
+        return out
+
+    def eval(self, uv, mask: int = S, stream=None):
+        """uv: (n,2) float64 CUDA tensor -> (3*nblocks, n) float64 SoA tensor."""
+        torch = _torch()
+        uv = uv.contiguous()
+        n = uv.shape[0]
+        nb = bin(mask & 63).count("1")
+        out = torch.empty((3 * nb, n), dtype=torch.float64, device=uv.device)
+        check(lib().nurbs_eval(self.h, _ptr(uv), n, mask, _ptr(out), PREC_FP64, _stream(stream)), "nurbs_eval")
+        return out
+
+    def eval_f32(self, uv, mask: int = S, stream=None):
+        torch = _torch()
+        uv = uv.contiguous()
+        n = uv.shape[0]
+        nb = bin(mask & 63).count("1")
+        out = torch.empty((3 * nb, n), dtype=torch.float32, device=uv.device)
+        check(lib().nurbs_eval_f32(self.h, _ptr(uv), n, mask, _ptr(out), _stream(stream)), "nurbs_eval_f32")
+        return out
+
+    def tree(self):
+        nodes = np.zeros((TREE_NODES, 10), np.float64)
+        div = np.zeros(TREE_NODES, np.uint8)
+        built = np.zeros(TREE_NODES, np.uint8)
+        check(lib().nurbs_tree_export(self.h, nodes.ctypes.data, div.ctypes.data, built.ctypes.data),
+              "nurbs_tree_export")
+        return nodes, div, built
+
+    def candidates(self, P, stream=None):
+        torch = _torch()
+        P = P.contiguous()
+        n = P.shape[0]
+        lst = torch.empty((n, TREE_NODES), dtype=torch.int32, device=P.device)
+        cnt = torch.empty(n, dtype=torch.int32, device=P.device)
+        check(lib().nurbs_candidates(self.h, _ptr(P), n, _ptr(lst), _ptr(cnt), _stream(stream)), "nurbs_candidates")
+        return lst, cnt
+
+    def invert(self, P, precision: int = PREC_MIXED, stream=None, out=None):
+        """P: (n,3) float64 CUDA tensor -> (uv (n,2), status (n,), residual (n,))."""
+        torch = _torch()
+        P = P.contiguous()
+        n = P.shape[0]
+        if out is None:
+            uv = torch.empty((n, 2), dtype=torch.float64, device=P.device)
+            st = torch.empty(n, dtype=torch.int32, device=P.device)
+            res = torch.empty(n, dtype=torch.float64, device=P.device)
+        else:
+            uv, st, res = out
+        check(lib().nurbs_invert(self.h, _ptr(P), n, _ptr(uv), _ptr(st), _ptr(res), precision, _stream(stream)),
+              "nurbs_invert")
+        return uv, st, res
+
+    def invert_host(self, P: np.ndarray, precision: int = PREC_MIXED, stream=None, out=None):
+        """Host buffers in and out (copies inside the call)."""
+        P = np.ascontiguousarray(P, np.float64).reshape(-1, 3)
+        n = P.shape[0]
+        if out is None:
+            uv = np.empty((n, 2), np.float64)
+            st = np.empty(n, np.int32)
+            res = np.empty(n, np.float64)
+        else:
+            uv, st, res = out
+        rc = lib().nurbs_invert_host(self.h, P.ctypes.data, n, uv.ctypes.data, st.ctypes.data, res.ctypes.data,
+                                     precision, _stream(stream))
+        check(rc, "nurbs_invert_host")
+        return uv, st, res
+
+
+def get_matrix_n_raw(p, q, nu, nv, knots_u, knots_v, cps, weights, stream=None):
+    """Legacy GetMatrixN with device tensors; returns the MatrixN tensor."""
+    torch = _torch()
+    n = lib().nurbs_matrix_n_size(p, q, nu, nv)
+    out = torch.zeros(n, dtype=torch.float64, device="cuda")
+    check(lib().nurbs_get_matrix_n_raw(_ptr(out), p, q, nu, nv, _ptr(knots_u), _ptr(knots_v), _ptr(cps),
+                                       _ptr(weights), _stream(stream)), "nurbs_get_matrix_n_raw")
+    return out
+
+
+def evaluate_random(uv, matrix_n, p, q, nu, nv, knots_u, knots_v, stream=None):
+    """Legacy EvaluateRandom with device tensors; returns (n,3) points."""
+    torch = _torch()
+    n = uv.shape[0]
+    out = torch.empty((n, 3), dtype=torch.float64, device=uv.device)
+    check(lib().nurbs_evaluate_random(_ptr(uv), _ptr(out), n, _ptr(matrix_n), p, q, nu, nv, _ptr(knots_u),
+                                      _ptr(knots_v), _stream(stream)), "nurbs_evaluate_random")
+    return out

@@ -1,0 +1,434 @@
+// C-ABI of the GB300 NURBS engine (declared in include/gpu_nurbs.h).
+//
+// Host-side duties: argument validation, the per-surface device arena, breakpoint tables,
+// launches on the caller's stream, and status codes.  Nothing here calls exit().
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "gpu_nurbs.h"
+#include "nurbs_internal.h"
+
+using namespace gnurbs;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+  return fail(NURBS_E_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define CUDA_TRY(expr, what)                         \
+  do {                                               \
+    cudaError_t e_ = (expr);                         \
+    if (e_ != cudaSuccess) return cuda_fail(e_, what); \
+  } while (0)
+
+size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+// Distinct breakpoints of the domain [k[p], k[n]] and the knot index of each non-empty span.
+// Spans are the m in [p, cp-1] with k[m] < k[m+1]: exactly those findSpan can return for a
+// parameter in the domain (src/NURBS/Evaluate.cu:504-533).
+void breakpoints(const double* k, int p, int cp, std::vector<double>& b, std::vector<int>& idx) {
+  b.clear();
+  idx.clear();
+  for (int m = p; m < cp; ++m) {
+    if (k[m] < k[m + 1]) {
+      if (b.empty()) b.push_back(k[m]);
+      idx.push_back(m);
+      b.push_back(k[m + 1]);
+    }
+  }
+}
+
+int validate_knots(const double* k, int p, int cp, const char* name) {
+  int nk = p + cp + 1;
+  for (int i = 0; i < nk; ++i)
+    if (!std::isfinite(k[i])) return fail(NURBS_E_INVALID, "%s[%d] is not finite", name, i);
+  for (int i = 0; i + 1 < nk; ++i)
+    if (k[i] > k[i + 1]) return fail(NURBS_E_INVALID, "%s is not non-decreasing at %d", name, i);
+  if (!(k[p] < k[cp])) return fail(NURBS_E_INVALID, "%s: empty parameter domain [k[%d], k[%d]]", name, p, cp);
+  return NURBS_OK;
+}
+
+int validate_dims(int p, int q, int nu, int nv) {
+  if (p < 1 || q < 1 || p > NURBS_MAX_DEGREE || q > NURBS_MAX_DEGREE)
+    return fail(NURBS_E_INVALID, "degrees (%d,%d) outside 1..%d", p, q, NURBS_MAX_DEGREE);
+  if (nu < p + 1 || nv < q + 1) return fail(NURBS_E_INVALID, "control net %dx%d too small for degree (%d,%d)", nu, nv, p, q);
+  if ((int64_t)nu * nv > (int64_t)1 << 28) return fail(NURBS_E_UNSUPPORTED, "control net %dx%d too large", nu, nv);
+  return NURBS_OK;
+}
+
+// Host copy of a buffer given as host or device pointer.
+int fetch(const double* src, size_t n, int kind, std::vector<double>& dst, cudaStream_t st) {
+  dst.resize(n);
+  if (kind == NURBS_PTR_HOST) {
+    std::memcpy(dst.data(), src, n * sizeof(double));
+    return NURBS_OK;
+  }
+  CUDA_TRY(cudaMemcpyAsync(dst.data(), src, n * sizeof(double), cudaMemcpyDeviceToHost, st), "copy to host");
+  CUDA_TRY(cudaStreamSynchronize(st), "stream sync");
+  return NURBS_OK;
+}
+
+}  // namespace
+
+struct nurbs_surface_s {
+  SurfDev dev{};
+  void* arena = nullptr;
+  size_t arena_bytes = 0;
+  double* basis_u = nullptr;
+  double* basis_v = nullptr;
+  int device = 0;
+  bool tree_built = false;
+};
+
+extern "C" {
+
+const char* nurbs_status_string(int status) {
+  switch (status) {
+    case NURBS_OK: return "ok";
+    case NURBS_E_INVALID: return "invalid argument";
+    case NURBS_E_CUDA: return "CUDA error";
+    case NURBS_E_NOMEM: return "out of memory";
+    case NURBS_E_IO: return "I/O error";
+    case NURBS_E_PARSE: return "parse error";
+    case NURBS_E_UNSUPPORTED: return "unsupported";
+    case NURBS_E_BUDGET: return "memory budget exceeded";
+    case NURBS_E_TIMEOUT: return "timeout";
+    case NURBS_E_STATE: return "invalid state";
+    default: return "unknown status";
+  }
+}
+
+const char* nurbs_last_error(void) { return g_last_error.c_str(); }
+const char* nurbs_version(void) { return "gpu-nurbs-gb300 0.1 (sm_103a)"; }
+
+int64_t nurbs_matrix_n_size(int p, int q, int nu, int nv) {
+  return (int64_t)(p + nu) * (q + nv) * 4 * (p + 1) * (q + 1);
+}
+
+int64_t nurbs_matrix_n_position(int i, int j, int p, int q, int nu, int nv, int c) {
+  (void)nu;
+  return (((int64_t)i * (q + nv) + j) * 4 + c) * (int64_t)(p + 1) * (q + 1);
+}
+
+int nurbs_surface_create(int p, int q, int nu, int nv, const double* knots_u, const double* knots_v,
+                         const double* cps, const double* weights, int ptr_kind, void* stream,
+                         nurbs_surface_t* out) {
+  if (!out) return fail(NURBS_E_INVALID, "out is NULL");
+  *out = nullptr;
+  if (!knots_u || !knots_v || !cps || !weights) return fail(NURBS_E_INVALID, "NULL surface array");
+  if (ptr_kind != NURBS_PTR_HOST && ptr_kind != NURBS_PTR_DEVICE) return fail(NURBS_E_INVALID, "bad ptr_kind");
+  int rc = validate_dims(p, q, nu, nv);
+  if (rc) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  std::vector<double> ku, kv, hc, hw;
+  if ((rc = fetch(knots_u, p + nu + 1, ptr_kind, ku, st))) return rc;
+  if ((rc = fetch(knots_v, q + nv + 1, ptr_kind, kv, st))) return rc;
+  if ((rc = validate_knots(ku.data(), p, nu, "knots_u"))) return rc;
+  if ((rc = validate_knots(kv.data(), q, nv, "knots_v"))) return rc;
+  const size_t ncp = (size_t)nu * nv;
+  if (ptr_kind == NURBS_PTR_HOST) {
+    for (size_t i = 0; i < ncp; ++i) {
+      if (!(weights[i] > 0) || !std::isfinite(weights[i]))
+        return fail(NURBS_E_INVALID, "weight %zu is not a finite positive number", i);
+      for (int c = 0; c < 3; ++c)
+        if (!std::isfinite(cps[3 * i + c])) return fail(NURBS_E_INVALID, "control point %zu is not finite", i);
+    }
+  }
+  std::vector<double> bu, bv;
+  std::vector<int> iu, iv;
+  breakpoints(ku.data(), p, nu, bu, iu);
+  breakpoints(kv.data(), q, nv, bv, iv);
+  const int nsu = (int)iu.size(), nsv = (int)iv.size();
+  const int k1 = p + 1, k2 = q + 1, k12 = k1 * k2;
+  const size_t nspan = (size_t)nsu * nsv;
+
+  // arena layout
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    size_t o = off;
+    off = align256(off + bytes);
+    return o;
+  };
+  size_t o_bu = take((nsu + 1) * 8), o_bv = take((nsv + 1) * 8);
+  size_t o_idu = take(nsu * 8), o_idv = take(nsv * 8);
+  size_t o_bu32 = take((nsu + 1) * 4), o_bv32 = take((nsv + 1) * 4);
+  size_t o_idu32 = take(nsu * 4), o_idv32 = take(nsv * 4);
+  size_t o_iu = take(nsu * 4), o_iv = take(nsv * 4);
+  size_t o_ku = take(ku.size() * 8), o_kv = take(kv.size() * 8);
+  size_t o_cps = take(ncp * 3 * 8), o_w = take(ncp * 8);
+  size_t o_m64 = take(nspan * k12 * 4 * 8), o_m32 = take(nspan * k12 * 4 * 4);
+  size_t o_bas_u = take((size_t)nsu * k1 * k1 * 8), o_bas_v = take((size_t)nsv * k2 * k2 * 8);
+  size_t o_tree = take(kTreeNodes * sizeof(TreeNodeDev));
+  size_t o_div = take(kTreeNodes), o_built = take(kTreeNodes);
+  const size_t total = off;
+
+  nurbs_surface_s* s = new (std::nothrow) nurbs_surface_s();
+  if (!s) return fail(NURBS_E_NOMEM, "host allocation failed");
+  cudaGetDevice(&s->device);
+  cudaError_t e = cudaMalloc(&s->arena, total);
+  if (e != cudaSuccess) {
+    delete s;
+    cudaGetLastError();
+    return fail(NURBS_E_NOMEM, "device allocation of %zu bytes failed: %s", total, cudaGetErrorString(e));
+  }
+  s->arena_bytes = total;
+  char* A = (char*)s->arena;
+  std::vector<double> idu(nsu), idv(nsv);
+  std::vector<float> bu32(bu.begin(), bu.end()), bv32(bv.begin(), bv.end()), idu32(nsu), idv32(nsv);
+  for (int i = 0; i < nsu; ++i) idu[i] = 1.0 / (bu[i + 1] - bu[i]), idu32[i] = (float)idu[i];
+  for (int i = 0; i < nsv; ++i) idv[i] = 1.0 / (bv[i + 1] - bv[i]), idv32[i] = (float)idv[i];
+
+  SurfDev& d = s->dev;
+  d.p = p; d.q = q; d.nu = nu; d.nv = nv; d.ns_u = nsu; d.ns_v = nsv;
+  d.range_u = ku[p + nu] - ku[0];  // kernel.cu:167
+  d.range_v = kv[q + nv] - kv[0];
+  d.range_u32 = (float)d.range_u;
+  d.range_v32 = (float)d.range_v;
+  d.dom_u0 = ku[p]; d.dom_u1 = ku[nu]; d.dom_v0 = kv[q]; d.dom_v1 = kv[nv];
+  d.bu = (const double*)(A + o_bu); d.bv = (const double*)(A + o_bv);
+  d.inv_du = (const double*)(A + o_idu); d.inv_dv = (const double*)(A + o_idv);
+  d.bu32 = (const float*)(A + o_bu32); d.bv32 = (const float*)(A + o_bv32);
+  d.inv_du32 = (const float*)(A + o_idu32); d.inv_dv32 = (const float*)(A + o_idv32);
+  d.knot_u = (const int*)(A + o_iu); d.knot_v = (const int*)(A + o_iv);
+  d.knots_u = (const double*)(A + o_ku); d.knots_v = (const double*)(A + o_kv);
+  d.cps = (const double*)(A + o_cps); d.weights = (const double*)(A + o_w);
+  d.m64 = (const double*)(A + o_m64); d.m32 = (const float*)(A + o_m32);
+  d.tree = (TreeNodeDev*)(A + o_tree);
+  d.divided = (unsigned char*)(A + o_div);
+  d.built = (unsigned char*)(A + o_built);
+  s->basis_u = (double*)(A + o_bas_u);
+  s->basis_v = (double*)(A + o_bas_v);
+
+  auto up = [&](size_t o, const void* src, size_t bytes) {
+    return cudaMemcpyAsync(A + o, src, bytes, cudaMemcpyHostToDevice, st);
+  };
+  cudaMemcpyKind ck = ptr_kind == NURBS_PTR_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
+  cudaError_t errs[16];
+  int ne = 0;
+  errs[ne++] = up(o_bu, bu.data(), bu.size() * 8);
+  errs[ne++] = up(o_bv, bv.data(), bv.size() * 8);
+  errs[ne++] = up(o_idu, idu.data(), nsu * 8);
+  errs[ne++] = up(o_idv, idv.data(), nsv * 8);
+  errs[ne++] = up(o_bu32, bu32.data(), bu32.size() * 4);
+  errs[ne++] = up(o_bv32, bv32.data(), bv32.size() * 4);
+  errs[ne++] = up(o_idu32, idu32.data(), nsu * 4);
+  errs[ne++] = up(o_idv32, idv32.data(), nsv * 4);
+  errs[ne++] = up(o_iu, iu.data(), nsu * 4);
+  errs[ne++] = up(o_iv, iv.data(), nsv * 4);
+  errs[ne++] = up(o_ku, ku.data(), ku.size() * 8);
+  errs[ne++] = up(o_kv, kv.data(), kv.size() * 8);
+  errs[ne++] = cudaMemcpyAsync(A + o_cps, cps, ncp * 3 * 8, ck, st);
+  errs[ne++] = cudaMemcpyAsync(A + o_w, weights, ncp * 8, ck, st);
+  errs[ne++] = cudaMemsetAsync(A + o_tree, 0, o_built + kTreeNodes - o_tree, st);
+  for (int i = 0; i < ne; ++i)
+    if (errs[i] != cudaSuccess) {
+      cudaFree(s->arena);
+      delete s;
+      return cuda_fail(errs[i], "surface upload");
+    }
+  cudaError_t le = launch_basis(d.knots_u, p, d.knot_u, nsu, s->basis_u, st);
+  if (le == cudaSuccess) le = launch_basis(d.knots_v, q, d.knot_v, nsv, s->basis_v, st);
+  if (le == cudaSuccess) le = launch_span_matrices(d, s->basis_u, s->basis_v, (double*)d.m64, (float*)d.m32, st);
+  if (le == cudaSuccess) le = launch_tree(d, st);
+  if (le == cudaSuccess) le = cudaStreamSynchronize(st);
+  if (le != cudaSuccess) {
+    cudaFree(s->arena);
+    delete s;
+    return cuda_fail(le, "matrix-form conversion");
+  }
+  s->tree_built = true;
+  *out = s;
+  return NURBS_OK;
+}
+
+int nurbs_surface_destroy(nurbs_surface_t s) {
+  if (!s) return NURBS_OK;
+  cudaError_t e = cudaFree(s->arena);
+  delete s;
+  if (e != cudaSuccess) return cuda_fail(e, "cudaFree");
+  return NURBS_OK;
+}
+
+int nurbs_surface_info(nurbs_surface_t s, nurbs_surface_info_t* info) {
+  if (!s || !info) return fail(NURBS_E_INVALID, "NULL argument");
+  info->degree_u = s->dev.p;
+  info->degree_v = s->dev.q;
+  info->cp_u = s->dev.nu;
+  info->cp_v = s->dev.nv;
+  info->spans_u = s->dev.ns_u;
+  info->spans_v = s->dev.ns_v;
+  info->device_bytes = (int64_t)s->arena_bytes;
+  info->tree_built = s->tree_built ? 1 : 0;
+  return NURBS_OK;
+}
+
+int nurbs_get_matrix_n(nurbs_surface_t s, double* matrix_n_dev, void* stream) {
+  if (!s || !matrix_n_dev) return fail(NURBS_E_INVALID, "NULL argument");
+  CUDA_TRY(launch_export_ref_layout(s->dev, matrix_n_dev, (cudaStream_t)stream), "export MatrixN");
+  return NURBS_OK;
+}
+
+int nurbs_get_matrix_n_raw(double* matrix_n_dev, int p, int q, int nu, int nv, const double* knots_u_dev,
+                           const double* knots_v_dev, const double* control_points_dev, const double* weights_dev,
+                           void* stream) {
+  if (!matrix_n_dev || !knots_u_dev || !knots_v_dev || !control_points_dev || !weights_dev)
+    return fail(NURBS_E_INVALID, "NULL argument");
+  int rc = validate_dims(p, q, nu, nv);
+  if (rc) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  std::vector<double> ku, kv;
+  if ((rc = fetch(knots_u_dev, p + nu + 1, NURBS_PTR_DEVICE, ku, st))) return rc;
+  if ((rc = fetch(knots_v_dev, q + nv + 1, NURBS_PTR_DEVICE, kv, st))) return rc;
+  if ((rc = validate_knots(ku.data(), p, nu, "knots_u"))) return rc;
+  if ((rc = validate_knots(kv.data(), q, nv, "knots_v"))) return rc;
+  std::vector<double> bu, bv;
+  std::vector<int> iu, iv;
+  breakpoints(ku.data(), p, nu, bu, iu);
+  breakpoints(kv.data(), q, nv, bv, iv);
+  const int nsu = (int)iu.size(), nsv = (int)iv.size(), k1 = p + 1, k2 = q + 1;
+  size_t o_iu = 0, o_iv = align256(nsu * 4), o_bu = o_iv + align256(nsv * 4);
+  size_t o_bv = o_bu + align256((size_t)nsu * k1 * k1 * 8);
+  size_t total = o_bv + align256((size_t)nsv * k2 * k2 * 8);
+  char* tmp = nullptr;
+  CUDA_TRY(cudaMallocAsync((void**)&tmp, total, st), "temporary allocation");
+  SurfDev d{};
+  d.p = p; d.q = q; d.nu = nu; d.nv = nv; d.ns_u = nsu; d.ns_v = nsv;
+  d.knot_u = (const int*)(tmp + o_iu);
+  d.knot_v = (const int*)(tmp + o_iv);
+  d.cps = control_points_dev;
+  d.weights = weights_dev;
+  cudaError_t e = cudaMemcpyAsync(tmp + o_iu, iu.data(), nsu * 4, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(tmp + o_iv, iv.data(), nsv * 4, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = launch_basis(knots_u_dev, p, d.knot_u, nsu, (double*)(tmp + o_bu), st);
+  if (e == cudaSuccess) e = launch_basis(knots_v_dev, q, d.knot_v, nsv, (double*)(tmp + o_bv), st);
+  if (e == cudaSuccess)
+    e = launch_span_matrices(d, (double*)(tmp + o_bu), (double*)(tmp + o_bv), matrix_n_dev, nullptr, st);
+  // the host vectors above must outlive the async copies
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  cudaFreeAsync(tmp, st);
+  if (e != cudaSuccess) return cuda_fail(e, "GetMatrixN");
+  return NURBS_OK;
+}
+
+int nurbs_eval(nurbs_surface_t s, const double* uv_dev, int64_t n, unsigned mask, double* out_dev, int precision,
+               void* stream) {
+  if (!s) return fail(NURBS_E_INVALID, "NULL surface");
+  if (n < 0) return fail(NURBS_E_INVALID, "negative count");
+  if (mask == 0 || mask > 63u) return fail(NURBS_E_INVALID, "mask 0x%x outside 1..63", mask);
+  if (precision != NURBS_PREC_FP64) return fail(NURBS_E_INVALID, "nurbs_eval computes in FP64; use nurbs_eval_f32");
+  if (n == 0) return NURBS_OK;
+  if (!uv_dev || !out_dev) return fail(NURBS_E_INVALID, "NULL buffer");
+  CUDA_TRY(launch_eval_f64(s->dev, uv_dev, n, mask, out_dev, (cudaStream_t)stream), "eval launch");
+  return NURBS_OK;
+}
+
+int nurbs_eval_f32(nurbs_surface_t s, const float* uv_dev, int64_t n, unsigned mask, float* out_dev, void* stream) {
+  if (!s) return fail(NURBS_E_INVALID, "NULL surface");
+  if (n < 0) return fail(NURBS_E_INVALID, "negative count");
+  if (mask == 0 || mask > 63u) return fail(NURBS_E_INVALID, "mask 0x%x outside 1..63", mask);
+  if (n == 0) return NURBS_OK;
+  if (!uv_dev || !out_dev) return fail(NURBS_E_INVALID, "NULL buffer");
+  CUDA_TRY(launch_eval_f32(s->dev, uv_dev, n, mask, out_dev, (cudaStream_t)stream), "eval launch");
+  return NURBS_OK;
+}
+
+int nurbs_evaluate_random(const double* uv_dev, double* xyz_dev, int64_t n, const double* matrix_n_dev, int p, int q,
+                          int nu, int nv, const double* knots_u_dev, const double* knots_v_dev, void* stream) {
+  int rc = validate_dims(p, q, nu, nv);
+  if (rc) return rc;
+  if (n < 0) return fail(NURBS_E_INVALID, "negative count");
+  if (n == 0) return NURBS_OK;
+  if (!uv_dev || !xyz_dev || !matrix_n_dev || !knots_u_dev || !knots_v_dev) return fail(NURBS_E_INVALID, "NULL buffer");
+  CUDA_TRY(launch_evaluate_random(uv_dev, xyz_dev, n, matrix_n_dev, p, q, nu, nv, knots_u_dev, knots_v_dev,
+                                  (cudaStream_t)stream),
+           "EvaluateRandom launch");
+  return NURBS_OK;
+}
+
+int nurbs_build_tree(nurbs_surface_t s, int levels, void* stream) {
+  if (!s) return fail(NURBS_E_INVALID, "NULL surface");
+  if (levels != 2) return fail(NURBS_E_UNSUPPORTED, "only the 2-level tree is supported (got %d)", levels);
+  cudaStream_t st = (cudaStream_t)stream;
+  CUDA_TRY(launch_tree(s->dev, st), "tree launch");
+  CUDA_TRY(cudaStreamSynchronize(st), "tree sync");
+  s->tree_built = true;
+  return NURBS_OK;
+}
+
+int nurbs_tree_export(nurbs_surface_t s, double* nodes_host, unsigned char* divided_host, unsigned char* built_host) {
+  if (!s || !nodes_host || !divided_host || !built_host) return fail(NURBS_E_INVALID, "NULL argument");
+  static_assert(sizeof(TreeNodeDev) == 80, "TreeNodeDev layout");
+  CUDA_TRY(cudaMemcpy(nodes_host, s->dev.tree, kTreeNodes * sizeof(TreeNodeDev), cudaMemcpyDeviceToHost), "tree copy");
+  CUDA_TRY(cudaMemcpy(divided_host, s->dev.divided, kTreeNodes, cudaMemcpyDeviceToHost), "divided copy");
+  CUDA_TRY(cudaMemcpy(built_host, s->dev.built, kTreeNodes, cudaMemcpyDeviceToHost), "built copy");
+  return NURBS_OK;
+}
+
+int nurbs_candidates(nurbs_surface_t s, const double* P_dev, int64_t n, int* list_dev, int* counts_dev, void* stream) {
+  if (!s) return fail(NURBS_E_INVALID, "NULL surface");
+  if (n < 0) return fail(NURBS_E_INVALID, "negative count");
+  if (n == 0) return NURBS_OK;
+  if (!P_dev || !list_dev || !counts_dev) return fail(NURBS_E_INVALID, "NULL buffer");
+  CUDA_TRY(launch_candidates(s->dev, P_dev, n, list_dev, counts_dev, (cudaStream_t)stream), "candidates launch");
+  return NURBS_OK;
+}
+
+int nurbs_invert(nurbs_surface_t s, const double* P_dev, int64_t n, double* uv_dev, int* status_dev,
+                 double* residual_dev, int precision, void* stream) {
+  if (!s) return fail(NURBS_E_INVALID, "NULL surface");
+  if (n < 0) return fail(NURBS_E_INVALID, "negative count");
+  if (precision != NURBS_PREC_FP64 && precision != NURBS_PREC_MIXED)
+    return fail(NURBS_E_INVALID, "precision %d is not FP64 or MIXED", precision);
+  if (n == 0) return NURBS_OK;
+  if (!P_dev || !uv_dev || !status_dev || !residual_dev) return fail(NURBS_E_INVALID, "NULL buffer");
+  CUDA_TRY(launch_invert(s->dev, P_dev, n, uv_dev, status_dev, residual_dev, precision, (cudaStream_t)stream),
+           "invert launch");
+  return NURBS_OK;
+}
+
+int nurbs_invert_host(nurbs_surface_t s, const double* P_host, int64_t n, double* uv_host, int* status_host,
+                      double* residual_host, int precision, void* stream) {
+  if (!s) return fail(NURBS_E_INVALID, "NULL surface");
+  if (n < 0) return fail(NURBS_E_INVALID, "negative count");
+  if (n == 0) return NURBS_OK;
+  if (!P_host || !uv_host || !status_host || !residual_host) return fail(NURBS_E_INVALID, "NULL buffer");
+  cudaStream_t st = (cudaStream_t)stream;
+  size_t bP = (size_t)n * 24, bUV = (size_t)n * 16, bS = (size_t)n * 4, bR = (size_t)n * 8;
+  size_t oUV = align256(bP), oS = oUV + align256(bUV), oR = oS + align256(bS), total = oR + align256(bR);
+  char* buf = nullptr;
+  CUDA_TRY(cudaMallocAsync((void**)&buf, total, st), "device buffers");
+  cudaError_t e = cudaMemcpyAsync(buf, P_host, bP, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess)
+    e = launch_invert(s->dev, (const double*)buf, n, (double*)(buf + oUV), (int*)(buf + oS), (double*)(buf + oR),
+                      precision, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(uv_host, buf + oUV, bUV, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(status_host, buf + oS, bS, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(residual_host, buf + oR, bR, cudaMemcpyDeviceToHost, st);
+  cudaFreeAsync(buf, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_fail(e, "invert (host buffers)");
+  return NURBS_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,152 @@
+// Stage c: 2-level subdivision tree of AABBs and candidate selection (K3 tree_build).
+//
+// Replaces, per level, the reference's chain GetPoints -> 3x GetSecondDerivatives ->
+// 3x Max_Sequential_Addressing_Shared -> TightBoundingBox (src/kernel/kernel.cu:375-431,
+// 544-621, 707-733; driven by src/main.cu:280-309) with one fused kernel: one CTA per node,
+// one thread per lattice sample (9x9), samples and second-derivative maxima kept in shared
+// memory, box inflation K = (M1 + 2 M2 + M3) sqrt(3) / (8 (8g)^2), clip to the parent box,
+// flatness test NeedDivide (kernel.cu:859-878).
+// Compiled with --fmad=false and evaluated with the reference-order functions of
+// gnurbs::exact, so boxes and Divided flags are bit-identical to the reference's FP64 math.
+#include "nurbs_internal.h"
+#include "nurbs_math.cuh"
+
+namespace gnurbs {
+
+__device__ __forceinline__ bool need_divide(const TreeNodeDev& n) {  // kernel.cu:859-878
+  double dx = n.rt[0] - n.lb[0], dy = n.rt[1] - n.lb[1], dz = n.rt[2] - n.lb[2], t;
+  if (dx > dy) { t = dx; dx = dy; dy = t; }
+  if (dx > dz) { t = dx; dx = dz; dz = t; }
+  if ((dx < 0.5 * dy) && (dx < 0.5 * dz)) return false;
+  return true;
+}
+
+__global__ void __launch_bounds__(96) k_tree_level(SurfDev s, int level) {
+  const unsigned g = level == 0 ? 1u : (unsigned)kGap;
+  const unsigned blk = blockIdx.x;
+  const unsigned bx = blk / g, by = blk % g;
+  const int tree_index = level == 0 ? 0 : 1 + (int)blk;
+  if (level == 1 && !s.divided[0]) {  // parent not divided: node not built
+    if (threadIdx.x == 0) s.built[tree_index] = 0;
+    return;
+  }
+  __shared__ double sM[3][kPts * kPts];
+  __shared__ double sS[3][kPts * kPts];
+  const int t = threadIdx.x;
+  const int p = s.p, q = s.q, k2 = q + 1, k12 = (p + 1) * (q + 1);
+  if (t < kPts * kPts) {
+    const int tx = t / kPts, ty = t % kPts;
+    // GetPoints / GetSecondDerivatives sample (kernel.cu:383-388, 412-417)
+    double base_unit = 1.0 / g;
+    double unit = base_unit / kGap;
+    double base_u = base_unit * bx, base_v = base_unit * by;
+    double p1 = base_u + tx * unit, p2 = base_v + ty * unit;
+    int su = exact::find_seg(s.bu, s.ns_u, p1);
+    int sv = exact::find_seg(s.bv, s.ns_v, p2);
+    double du = s.bu[su + 1] - s.bu[su], dv = s.bv[sv + 1] - s.bv[sv];
+    double u = (p1 - s.bu[su]) / du;
+    double v = (p2 - s.bv[sv]) / dv;
+    double spanU = s.range_u / du;
+    double spanV = s.range_v / dv;
+    exact::DenseSpan M{s.m64 + (size_t)(su * s.ns_v + sv) * k12 * 4, k2};
+    v4<double> R = exact::point_r(M, p, q, u, v);
+    v3<double> a = exact::der_uu(M, p, q, u, v, R, spanU);
+    v3<double> b = exact::der_uv(M, p, q, u, v, R, spanU, spanV);
+    v3<double> c = exact::der_vv(M, p, q, u, v, R, spanV);
+    sM[0][t] = fmax(fabs(a.x), fmax(fabs(a.y), fabs(a.z)));  // kernel.cu:399
+    sM[1][t] = fmax(fabs(b.x), fmax(fabs(b.y), fabs(b.z)));
+    sM[2][t] = fmax(fabs(c.x), fmax(fabs(c.y), fabs(c.z)));
+    v3<double> S = exact::cart(R);
+    sS[0][t] = S.x;
+    sS[1][t] = S.y;
+    sS[2][t] = S.z;
+  }
+  __syncthreads();
+  if (t < 9) {
+    // t in 0..2: max of M_t; 3..5: max of S_(t-3); 6..8: min of S_(t-6).  Exact, so the
+    // order (sequential here, a strided tree in the reference) does not change the value.
+    const double* src = t < 3 ? sM[t] : sS[t < 6 ? t - 3 : t - 6];
+    double acc = src[0];
+    if (t < 6) {
+      for (int k = 1; k < kPts * kPts; ++k) acc = acc < src[k] ? src[k] : acc;  // kernel.cu:725
+    } else {
+      for (int k = 1; k < kPts * kPts; ++k) acc = acc > src[k] ? src[k] : acc;  // kernel.cu:593-595
+    }
+    __syncwarp(0x1ffu);
+    // reuse slot 0 of each array for the reduced value
+    __shared__ double red[9];
+    red[t] = acc;
+    __syncwarp(0x1ffu);
+    if (t == 0) {
+      unsigned den = 8u * kGap * g * kGap * g;
+      double K = (red[0] + 2 * red[1] + red[2]) * 1.7320508075688772 / den;  // sqrt(3), kernel.cu:574
+      TreeNodeDev n;
+      n.rt[0] = red[3] + K;
+      n.rt[1] = red[4] + K;
+      n.rt[2] = red[5] + K;
+      n.lb[0] = red[6] - K;
+      n.lb[1] = red[7] - K;
+      n.lb[2] = red[8] - K;
+      double uunit = 1.0 / g;  // kernel.cu:604-605
+      n.uv_lb[0] = bx * uunit;
+      n.uv_lb[1] = by * uunit;
+      n.uv_rt[0] = (bx + 1) * uunit;
+      n.uv_rt[1] = (by + 1) * uunit;
+      if (level == 1) {  // min/max(TreeNode) against the parent (kernel.cu:606-611, 885-901)
+        const TreeNodeDev& P = s.tree[0];
+        for (int k = 0; k < 3; ++k) {
+          n.rt[k] = fmin(n.rt[k], P.rt[k]);
+          n.lb[k] = fmax(n.lb[k], P.lb[k]);
+        }
+      }
+      s.tree[tree_index] = n;
+      s.divided[tree_index] = need_divide(n) ? 1 : 0;
+      s.built[tree_index] = 1;
+    }
+  }
+}
+
+// NewInverse's scan (kernel.cu:456-457) over built nodes, NewBoundingBoxCheck (:466-469).
+__global__ void k_candidates(SurfDev s, const double* __restrict__ P, int64_t n, int* __restrict__ list,
+                             int* __restrict__ counts) {
+  __shared__ double box[kTreeNodes][6];
+  __shared__ unsigned char built[kTreeNodes];
+  for (int k = threadIdx.x; k < kTreeNodes; k += blockDim.x) {
+    built[k] = s.built[k];
+    for (int c = 0; c < 3; ++c) {
+      box[k][c] = s.tree[k].lb[c];
+      box[k][3 + c] = s.tree[k].rt[c];
+    }
+  }
+  __syncthreads();
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    double x = P[3 * i], y = P[3 * i + 1], z = P[3 * i + 2];
+    int cnt = 0;
+    for (int k = 0; k < kTreeNodes; ++k) {
+      if (!built[k]) continue;
+      if ((x >= box[k][0]) && (y >= box[k][1]) && (z >= box[k][2]) && (x <= box[k][3]) && (y <= box[k][4]) &&
+          (z <= box[k][5]))
+        list[i * kTreeNodes + cnt++] = k;
+    }
+    counts[i] = cnt;
+  }
+}
+
+cudaError_t launch_tree(const SurfDev& s, cudaStream_t st) {
+  k_tree_level<<<1, 96, 0, st>>>(s, 0);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  k_tree_level<<<kGap * kGap, 96, 0, st>>>(s, 1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_candidates(const SurfDev& s, const double* P, int64_t n, int* list, int* counts,
+                              cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  int64_t blocks = (n + 255) / 256;
+  if (blocks > 152 * 32) blocks = 152 * 32;
+  k_candidates<<<(unsigned)blocks, 256, 0, st>>>(s, P, n, list, counts);
+  return cudaGetLastError();
+}
+
+}  // namespace gnurbs

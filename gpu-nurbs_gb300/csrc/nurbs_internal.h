@@ -1,0 +1,80 @@
+// Internal host/device declarations of the GB300 NURBS engine (not part of the C-ABI).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace gnurbs {
+
+constexpr int kMaxDegree = 7;     // p, q <= 7 (reference MAX_DEGREE 8 = p+1)
+constexpr int kTreeNodes = 65;    // root + 8x8 children
+constexpr int kGap = 8;           // GapPerEdge (src/kernel/kernel.cuh:17)
+constexpr int kPts = kGap + 1;    // PointsPerEdge
+
+// Device view of one surface.  All pointers are device pointers into the surface's arena.
+//
+// HBM layout (one arena per surface, 256-byte aligned sub-buffers):
+//   bu[ns_u+1], bv[ns_v+1]           breakpoints = distinct knots of the domain, ascending
+//   inv_du[ns_u], inv_dv[ns_v]       1/(bu[s+1]-bu[s])
+//   bu32/bv32, inv_du32/inv_dv32     the same in FP32 (mixed-precision seeding)
+//   knot_u[ns_u], knot_v[ns_v]       knot index m of span s (k[m] = bu[s]) for the reference layout
+//   m64[ns_u*ns_v][k1][k2][4]        span matrices, homogeneous components (xw, yw, zw, w)
+//                                    innermost, so one (a,b) coefficient is one 32-byte vector
+//   m32                              the same rounded to FP32 (16 bytes per coefficient)
+//   tree[65]                         TreeNodeDev; divided[65], built[65]
+struct SurfDev {
+  int p, q, nu, nv;
+  int ns_u, ns_v;
+  double range_u, range_v;   // k[last]-k[0] (derivative scale numerator, kernel.cu:167-168)
+  float range_u32, range_v32;
+  double dom_u0, dom_u1, dom_v0, dom_v1;  // knot domain [k[p], k[nu]] x [k[q], k[nv]]
+  const double* bu;
+  const double* bv;
+  const double* inv_du;
+  const double* inv_dv;
+  const float* bu32;
+  const float* bv32;
+  const float* inv_du32;
+  const float* inv_dv32;
+  const int* knot_u;
+  const int* knot_v;
+  const double* m64;
+  const float* m32;
+  const double* cps;      // 3*nu*nv  (xyz interleaved)
+  const double* weights;  // nu*nv
+  const double* knots_u;  // p+nu+1
+  const double* knots_v;  // q+nv+1
+  struct TreeNodeDev* tree;
+  unsigned char* divided;
+  unsigned char* built;
+};
+
+// Tree node in the reference TreeNode order (src/kernel/kernel.cuh:30-39), 80 bytes.
+struct TreeNodeDev {
+  double uv_lb[2], uv_rt[2];
+  double lb[3], rt[3];
+};
+
+// ---- launchers (each returns a cudaError_t from the launch) ----
+// stage a
+cudaError_t launch_basis(const double* knots, int degree, const int* knot_idx, int nspans,
+                         double* basis_out, cudaStream_t st);
+cudaError_t launch_span_matrices(const SurfDev& s, const double* basis_u, const double* basis_v,
+                                 double* m64, float* m32, cudaStream_t st);
+cudaError_t launch_export_ref_layout(const SurfDev& s, double* matrix_n, cudaStream_t st);
+// stage b
+cudaError_t launch_eval_f64(const SurfDev& s, const double* uv, int64_t n, unsigned mask, double* out,
+                            cudaStream_t st);
+cudaError_t launch_eval_f32(const SurfDev& s, const float* uv, int64_t n, unsigned mask, float* out,
+                            cudaStream_t st);
+cudaError_t launch_evaluate_random(const double* uv, double* xyz, int64_t n, const double* matrix_n, int p,
+                                   int q, int nu, int nv, const double* knots_u, const double* knots_v,
+                                   cudaStream_t st);
+// stage c
+cudaError_t launch_tree(const SurfDev& s, cudaStream_t st);
+cudaError_t launch_candidates(const SurfDev& s, const double* P, int64_t n, int* list, int* counts,
+                              cudaStream_t st);
+// stage d
+cudaError_t launch_invert(const SurfDev& s, const double* P, int64_t n, double* uv, int* status,
+                          double* residual, int precision, cudaStream_t st);
+
+}  // namespace gnurbs

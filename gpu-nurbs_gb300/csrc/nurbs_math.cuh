@@ -1,0 +1,416 @@
+// Device math of the GB300 NURBS engine.
+//
+// Two families:
+//  * gnurbs::exact — the reference's FP64 expressions term by term (power vectors by running
+//    product, matrix_mult sums from 0 in ascending order, the old-style quotient-rule
+//    derivatives of src/NURBS/Evaluate.cu:535-930).  Used where results must be bit-identical
+//    to the reference (span conversion, subdivision tree); the translation units that use
+//    them are compiled with --fmad=false so that no product is fused into a sum.
+//  * gnurbs::fast — Horner contractions of the same span matrices for batched evaluation and
+//    Gauss-Newton: one pass over the (p+1)(q+1) coefficient vectors yields R and its
+//    derivatives up to second order for all four homogeneous components at once.
+#pragma once
+#include <cuda_runtime.h>
+#include <math.h>
+#include "nurbs_internal.h"
+
+#define GN_HD __host__ __device__ __forceinline__
+
+namespace gnurbs {
+
+template <typename T>
+struct v4 {
+  T x, y, z, w;
+};
+template <typename T>
+struct v3 {
+  T x, y, z;
+};
+
+// ------------------------------------------------------------------ exact (reference order)
+namespace exact {
+
+// Once-rounded x^3 from an error-free product expansion (TwoProduct via fma).  Equals a
+// correctly rounded pow(x, 3) (the reference writes pow(h, 3), Evaluate.cu:737, 844, 926).
+GN_HD double cube(double x) {
+  double a = x * x;
+  double b = fma(x, x, -a);
+  double c = a * x;
+  double d = fma(a, x, -c);
+  double e = b * x;
+  return c + (d + e);
+}
+GN_HD double sq(double x) { return x * x; }  // pow(x, 2): the square rounded once
+
+// Coefficient accessor over the dense span layout [a][b][c].
+struct DenseSpan {
+  const double* m;
+  int k2;
+  GN_HD double operator()(int c, int a, int b) const { return m[((a * k2) + b) * 4 + c]; }
+};
+// Coefficient accessor over the reference MatrixN layout (4 planes of k1 x k2 row-major).
+struct RefSpan {
+  const double* m;
+  int k1, k2;
+  GN_HD double operator()(int c, int a, int b) const { return m[(c * k1 + a) * k2 + b]; }
+};
+
+GN_HD void power_vec(double t, int k, double* out) {  // Evaluate.cu:172-181
+  double now = 1;
+  for (int i = 0; i < k; i++) {
+    out[i] = now;
+    now *= t;
+  }
+}
+GN_HD void dpower_vec(double t, int k, double* out) {  // Evaluate.cu:540-545
+  double now = 1;
+  out[0] = 0;
+  for (int i = 0; i < k - 1; i++) {
+    out[i + 1] = (i + 1) * now;
+    now *= t;
+  }
+}
+GN_HD void ddpower_vec(double t, int k, double* out) {  // Evaluate.cu:680-685
+  double now = 1;
+  out[0] = 0;
+  if (k > 1) out[1] = 0;
+  for (int i = 0; i < k - 2; i++) {
+    out[i + 2] = (i + 2) * (i + 1) * now;
+    now *= t;
+  }
+}
+
+// temp_c[a] = sum_b M_c[a][b] * vec[b]  (matrix_mult(middle_c, vec, temp_c, k1, k2, 1))
+template <class Acc>
+GN_HD void mv(const Acc& M, int k1, int k2, const double* vec, double (*tmp)[kMaxDegree + 1]) {
+  for (int c = 0; c < 4; ++c)
+    for (int a = 0; a < k1; ++a) {
+      double acc = 0;
+      for (int b = 0; b < k2; ++b) acc += M(c, a, b) * vec[b];
+      tmp[c][a] = acc;
+    }
+}
+// temp_c[b] = sum_a vec[a] * M_c[a][b]  (matrix_mult(vectorUT, middle_c, temp_c, 1, k1, k2))
+template <class Acc>
+GN_HD void vm(const Acc& M, int k1, int k2, const double* vec, double (*tmp)[kMaxDegree + 1]) {
+  for (int c = 0; c < 4; ++c)
+    for (int b = 0; b < k2; ++b) {
+      double acc = 0;
+      for (int a = 0; a < k1; ++a) acc += vec[a] * M(c, a, b);
+      tmp[c][b] = acc;
+    }
+}
+GN_HD double dotk(const double* a, const double* b, int k) {
+  double acc = 0;
+  for (int l = 0; l < k; ++l) acc += a[l] * b[l];
+  return acc;
+}
+GN_HD v4<double> dot4(const double* vec, double (*tmp)[kMaxDegree + 1], int k) {
+  return {dotk(vec, tmp[0], k), dotk(vec, tmp[1], k), dotk(vec, tmp[2], k), dotk(vec, tmp[3], k)};
+}
+
+// MatrixSurfacePoint (Evaluate.cu:159-227)
+template <class Acc>
+GN_HD v4<double> point_r(const Acc& M, int p, int q, double u, double v) {
+  double U[kMaxDegree + 1], V[kMaxDegree + 1], tmp[4][kMaxDegree + 1];
+  power_vec(u, p + 1, U);
+  power_vec(v, q + 1, V);
+  mv(M, p + 1, q + 1, V, tmp);
+  return dot4(U, tmp, p + 1);
+}
+GN_HD v3<double> cart(v4<double> R) { return {R.x / R.w, R.y / R.w, R.z / R.w}; }  // ExtraMath.cu:3-5
+
+// old MatrixSurfaceDerivativeU (Evaluate.cu:535-598)
+template <class Acc>
+GN_HD v3<double> der_u(const Acc& M, int p, int q, double u, double v, v4<double> R, double spanU) {
+  double dU[kMaxDegree + 1], V[kMaxDegree + 1], tmp[4][kMaxDegree + 1];
+  dpower_vec(u, p + 1, dU);
+  power_vec(v, q + 1, V);
+  mv(M, p + 1, q + 1, V, tmp);
+  v4<double> RdU = dot4(dU, tmp, p + 1);
+  double h = R.w, hdU = RdU.w, s = -hdU / sq(h);
+  return {(R.x * s + RdU.x / h) * spanU, (R.y * s + RdU.y / h) * spanU, (R.z * s + RdU.z / h) * spanU};
+}
+// old MatrixSurfaceDerivativeV (Evaluate.cu:600-665)
+template <class Acc>
+GN_HD v3<double> der_v(const Acc& M, int p, int q, double u, double v, v4<double> R, double spanV) {
+  double U[kMaxDegree + 1], dV[kMaxDegree + 1], tmp[4][kMaxDegree + 1];
+  power_vec(u, p + 1, U);
+  dpower_vec(v, q + 1, dV);
+  mv(M, p + 1, q + 1, dV, tmp);
+  v4<double> RdV = dot4(U, tmp, p + 1);
+  double h = R.w, hdV = RdV.w, s = -hdV / sq(h);
+  return {(R.x * s + RdV.x / h) * spanV, (R.y * s + RdV.y / h) * spanV, (R.z * s + RdV.z / h) * spanV};
+}
+// old MatrixSurfaceDerivativeUU (Evaluate.cu:667-741)
+template <class Acc>
+GN_HD v3<double> der_uu(const Acc& M, int p, int q, double u, double v, v4<double> R, double spanU) {
+  double dU[kMaxDegree + 1], ddU[kMaxDegree + 1], V[kMaxDegree + 1], tmp[4][kMaxDegree + 1];
+  dpower_vec(u, p + 1, dU);
+  ddpower_vec(u, p + 1, ddU);
+  power_vec(v, q + 1, V);
+  mv(M, p + 1, q + 1, V, tmp);
+  v4<double> RdU = dot4(dU, tmp, p + 1);
+  v4<double> RdUU = dot4(ddU, tmp, p + 1);
+  double h = R.w, hdU = RdU.w, hdUU = RdUU.w;
+  double s1 = (2 * sq(hdU) / cube(h)) - (hdUU / sq(h));
+  double s2 = -hdU / sq(h);
+  return {((R.x * s1 + (2 * RdU.x) * s2) + RdUU.x / h) * spanU * spanU,
+          ((R.y * s1 + (2 * RdU.y) * s2) + RdUU.y / h) * spanU * spanU,
+          ((R.z * s1 + (2 * RdU.z) * s2) + RdUU.z / h) * spanU * spanU};
+}
+// old MatrixSurfaceDerivativeUV (Evaluate.cu:743-847) — the correct-sign mixed derivative
+template <class Acc>
+GN_HD v3<double> der_uv(const Acc& M, int p, int q, double u, double v, v4<double> R, double spanU,
+                        double spanV) {
+  double U[kMaxDegree + 1], dU[kMaxDegree + 1], V[kMaxDegree + 1], dV[kMaxDegree + 1];
+  double tmp[4][kMaxDegree + 1];
+  power_vec(u, p + 1, U);
+  dpower_vec(u, p + 1, dU);
+  power_vec(v, q + 1, V);
+  dpower_vec(v, q + 1, dV);
+  mv(M, p + 1, q + 1, V, tmp);
+  v4<double> RdU = dot4(dU, tmp, p + 1);
+  mv(M, p + 1, q + 1, dV, tmp);
+  v4<double> RdV = dot4(U, tmp, p + 1);
+  v4<double> RdUV = dot4(dU, tmp, p + 1);
+  double h = R.w, hdU = RdU.w, hdV = RdV.w, hdUV = RdUV.w;
+  double h2 = sq(h), h3 = cube(h);
+  return {((((RdUV.x * h - hdV * RdU.x) - RdV.x * hdU) - R.x * hdUV) / h2 + ((2 * R.x) * hdU * hdV) / h3) * spanU * spanV,
+          ((((RdUV.y * h - hdV * RdU.y) - RdV.y * hdU) - R.y * hdUV) / h2 + ((2 * R.y) * hdU * hdV) / h3) * spanU * spanV,
+          ((((RdUV.z * h - hdV * RdU.z) - RdV.z * hdU) - R.z * hdUV) / h2 + ((2 * R.z) * hdU * hdV) / h3) * spanU * spanV};
+}
+// old MatrixSurfaceDerivativeVV (Evaluate.cu:849-930): contracts U first
+template <class Acc>
+GN_HD v3<double> der_vv(const Acc& M, int p, int q, double u, double v, v4<double> R, double spanV) {
+  double U[kMaxDegree + 1], dV[kMaxDegree + 1], ddV[kMaxDegree + 1], tmp[4][kMaxDegree + 1];
+  power_vec(u, p + 1, U);
+  dpower_vec(v, q + 1, dV);
+  ddpower_vec(v, q + 1, ddV);
+  vm(M, p + 1, q + 1, U, tmp);
+  v4<double> RdV = dot4(dV, tmp, q + 1);
+  v4<double> RdVV = dot4(ddV, tmp, q + 1);
+  double h = R.w, hdV = RdV.w, hdVV = RdVV.w;
+  double s1 = (2 * sq(hdV) / cube(h)) - (hdVV / sq(h));
+  double s2 = -hdV / sq(h);
+  return {((R.x * s1 + (2 * RdV.x) * s2) + RdVV.x / h) * spanV * spanV,
+          ((R.y * s1 + (2 * RdV.y) * s2) + RdVV.y / h) * spanV * spanV,
+          ((R.z * s1 + (2 * RdV.z) * s2) + RdVV.z / h) * spanV * spanV};
+}
+
+// findSpan semantics over the breakpoints of the domain: the largest s in [0, ns-1] with
+// b[s] <= x (x below the domain -> 0, at or above its end -> ns-1), i.e. the knot span m with
+// k[m] <= x < k[m+1] that findSpan (Evaluate.cu:504-533) returns.  Bounded; NaN -> 0.
+GN_HD int find_seg(const double* b, int ns, double x) {
+  int lo = 0;
+  int step = 1;
+  while ((step << 1) <= ns) step <<= 1;
+  for (; step > 0; step >>= 1) {
+    int t = lo + step;
+    if (t < ns && b[t] <= x) lo = t;
+  }
+  return lo;
+}
+
+}  // namespace exact
+
+// ------------------------------------------------------------------------ fast (Horner)
+namespace fast {
+
+GN_HD double mad(double a, double b, double c) { return fma(a, b, c); }
+GN_HD float mad(float a, float b, float c) { return fmaf(a, b, c); }
+
+template <typename T>
+GN_HD v4<T> vmad(const v4<T>& a, T s, const v4<T>& c) {
+  return {mad(a.x, s, c.x), mad(a.y, s, c.y), mad(a.z, s, c.z), mad(a.w, s, c.w)};
+}
+
+__device__ __forceinline__ v4<double> load_coef(const double* m, int idx) {
+  const double2* p = reinterpret_cast<const double2*>(m + 4 * idx);
+  double2 lo = __ldg(p), hi = __ldg(p + 1);
+  return {lo.x, lo.y, hi.x, hi.y};
+}
+__device__ __forceinline__ v4<float> load_coef(const float* m, int idx) {
+  float4 f = __ldg(reinterpret_cast<const float4*>(m + 4 * idx));
+  return {f.x, f.y, f.z, f.w};
+}
+
+// Horner accumulator tracking value and D derivatives (D <= 2).  Coefficients are pushed from
+// the highest power down; after all pushes p = f(x), dp = f'(x), ddp = f''(x)/2.  The first
+// two pushes are peeled so no FMA is spent on zero accumulators.
+template <typename T, int D>
+struct Horner {
+  v4<T> p, dp, ddp;
+  int k;
+  GN_HD Horner() : k(0) {}
+  GN_HD void push(const v4<T>& c, T x) {
+    if (k == 0) {
+      p = c;
+    } else {
+      if (D >= 2) {
+        if (k == 2) ddp = dp;
+        else if (k > 2) ddp = vmad(ddp, x, dp);
+      }
+      if (D >= 1) {
+        if (k == 1) dp = p;
+        else dp = vmad(dp, x, p);
+      }
+      p = vmad(p, x, c);
+    }
+    ++k;
+  }
+};
+
+template <typename T>
+GN_HD v4<T> zero4() {
+  return {T(0), T(0), T(0), T(0)};
+}
+
+// Homogeneous R and its local derivatives at local (u,v) in one span.
+//   ORDER 0: R; ORDER 1: + Ru, Rv; ORDER 2: + Ruu, Ruv, Rvv.
+// P, Q > 0 fix the degrees at compile time; P = Q = 0 reads p, q at run time.
+template <typename T>
+struct RDer {
+  v4<T> R, Ru, Rv, Ruu, Ruv, Rvv;
+};
+
+template <typename T, int P, int Q, int ORDER>
+__device__ __forceinline__ RDer<T> span_contract(const T* __restrict__ m, int p_rt, int q_rt, T u, T v) {
+  const int pp = P > 0 ? P : p_rt;
+  const int qq = Q > 0 ? Q : q_rt;
+  const int k2 = qq + 1;
+  constexpr int DR = ORDER;                  // derivatives of the u-Horner over t_a
+  constexpr int DV = ORDER >= 1 ? ORDER - 1 : 0;
+  Horner<T, DR> colR;
+  Horner<T, DV> colV;
+  Horner<T, 0> colVV;
+#pragma unroll
+  for (int a = (P > 0 ? P : kMaxDegree); a >= 0; --a) {
+    if (P == 0 && a > pp) continue;
+    Horner<T, ORDER> row;
+#pragma unroll
+    for (int b = (Q > 0 ? Q : kMaxDegree); b >= 0; --b) {
+      if (Q == 0 && b > qq) continue;
+      row.push(load_coef(m, a * k2 + b), v);
+    }
+    colR.push(row.p, u);
+    if (ORDER >= 1) colV.push(row.dp, u);
+    if (ORDER >= 2) colVV.push(row.ddp, u);
+  }
+  RDer<T> o;
+  o.R = colR.p;
+  if (ORDER >= 1) {
+    o.Ru = colR.dp;
+    o.Rv = colV.p;
+  }
+  if (ORDER >= 2) {
+    o.Ruu = {T(2) * colR.ddp.x, T(2) * colR.ddp.y, T(2) * colR.ddp.z, T(2) * colR.ddp.w};
+    o.Ruv = colV.dp;
+    o.Rvv = {T(2) * colVV.p.x, T(2) * colVV.p.y, T(2) * colVV.p.z, T(2) * colVV.p.w};
+  }
+  return o;
+}
+
+// Cartesian point and derivatives with respect to the global parameters.
+template <typename T>
+struct SDer {
+  v3<T> S, Su, Sv, Suu, Suv, Svv;
+};
+
+template <typename T>
+GN_HD v3<T> xyz(const v4<T>& a) {
+  return {a.x, a.y, a.z};
+}
+// (a - s*b) * f, componentwise, s scalar
+template <typename T>
+GN_HD v3<T> sub_scaled(const v3<T>& a, T s, const v3<T>& b, T f) {
+  return {(a.x - s * b.x) * f, (a.y - s * b.y) * f, (a.z - s * b.z) * f};
+}
+
+// Quotient rule S = R.xyz / h and its derivatives (h = R.w), mapped to global parameters
+// by su = d(local u)/du and sv.
+template <typename T, int ORDER>
+GN_HD SDer<T> quotient(const RDer<T>& d, T su, T sv) {
+  SDer<T> o;
+  T ih = T(1) / d.R.w;
+  o.S = {d.R.x * ih, d.R.y * ih, d.R.z * ih};
+  if (ORDER >= 1) {
+    v3<T> Au = sub_scaled(xyz(d.Ru), d.Ru.w, o.S, ih);  // local dS/du
+    v3<T> Av = sub_scaled(xyz(d.Rv), d.Rv.w, o.S, ih);
+    if (ORDER >= 2) {
+      T hu = d.Ru.w, hv = d.Rv.w;
+      v3<T> Auu = {(d.Ruu.x - T(2) * hu * Au.x - d.Ruu.w * o.S.x) * ih,
+                   (d.Ruu.y - T(2) * hu * Au.y - d.Ruu.w * o.S.y) * ih,
+                   (d.Ruu.z - T(2) * hu * Au.z - d.Ruu.w * o.S.z) * ih};
+      v3<T> Auv = {(d.Ruv.x - hu * Av.x - hv * Au.x - d.Ruv.w * o.S.x) * ih,
+                   (d.Ruv.y - hu * Av.y - hv * Au.y - d.Ruv.w * o.S.y) * ih,
+                   (d.Ruv.z - hu * Av.z - hv * Au.z - d.Ruv.w * o.S.z) * ih};
+      v3<T> Avv = {(d.Rvv.x - T(2) * hv * Av.x - d.Rvv.w * o.S.x) * ih,
+                   (d.Rvv.y - T(2) * hv * Av.y - d.Rvv.w * o.S.y) * ih,
+                   (d.Rvv.z - T(2) * hv * Av.z - d.Rvv.w * o.S.z) * ih};
+      T suu = su * su, suv = su * sv, svv = sv * sv;
+      o.Suu = {Auu.x * suu, Auu.y * suu, Auu.z * suu};
+      o.Suv = {Auv.x * suv, Auv.y * suv, Auv.z * suv};
+      o.Svv = {Avv.x * svv, Avv.y * svv, Avv.z * svv};
+    }
+    o.Su = {Au.x * su, Au.y * su, Au.z * su};
+    o.Sv = {Av.x * sv, Av.y * sv, Av.z * sv};
+  }
+  return o;
+}
+
+// Breakpoint search with __ldg (see exact::find_seg for the semantics).
+template <typename T>
+__device__ __forceinline__ int find_seg(const T* __restrict__ b, int ns, T x) {
+  int lo = 0;
+  int step = 1 << (31 - __clz(ns));
+  for (; step > 0; step >>= 1) {
+    int t = lo + step;
+    if (t < ns && __ldg(b + t) <= x) lo = t;
+  }
+  return lo;
+}
+
+// Locates (u,v) and evaluates S and derivatives up to ORDER in precision T.
+template <typename T, int P, int Q, int ORDER>
+__device__ __forceinline__ SDer<T> eval_point(const SurfDev& s, T u, T v) {
+  const T* bu;
+  const T* bv;
+  const T* iu;
+  const T* iv;
+  const T* m;
+  if constexpr (sizeof(T) == 8) {
+    bu = reinterpret_cast<const T*>(s.bu);
+    bv = reinterpret_cast<const T*>(s.bv);
+    iu = reinterpret_cast<const T*>(s.inv_du);
+    iv = reinterpret_cast<const T*>(s.inv_dv);
+    m = reinterpret_cast<const T*>(s.m64);
+  } else {
+    bu = reinterpret_cast<const T*>(s.bu32);
+    bv = reinterpret_cast<const T*>(s.bv32);
+    iu = reinterpret_cast<const T*>(s.inv_du32);
+    iv = reinterpret_cast<const T*>(s.inv_dv32);
+    m = reinterpret_cast<const T*>(s.m32);
+  }
+  int su = find_seg(bu, s.ns_u, u);
+  int sv = find_seg(bv, s.ns_v, v);
+  T idu = __ldg(iu + su), idv = __ldg(iv + sv);
+  T lu = (u - __ldg(bu + su)) * idu;
+  T lv = (v - __ldg(bv + sv)) * idv;
+  const int k12 = (s.p + 1) * (s.q + 1);
+  const T* span = m + (size_t)(su * s.ns_v + sv) * k12 * 4;
+  RDer<T> d = span_contract<T, P, Q, ORDER>(span, s.p, s.q, lu, lv);
+  T ru, rv;
+  if constexpr (sizeof(T) == 8) {
+    ru = s.range_u;
+    rv = s.range_v;
+  } else {
+    ru = s.range_u32;
+    rv = s.range_v32;
+  }
+  T scu = ru * idu, scv = rv * idv;
+  return quotient<T, ORDER>(d, scu, scv);
+}
+
+}  // namespace fast
+}  // namespace gnurbs

@@ -1,0 +1,176 @@
+/*
+ * gpu_nurbs.h — C-ABI of the GB300 NURBS evaluation / inverse-evaluation engine.
+ *
+ * Drop-in boundary for the reference Qiang-Zou/GPU-NURBS, whose "API" is its .nu reader,
+ * its kernels and its __device__ functions (src/main.cu, src/NURBS/Evaluate.cu,
+ * src/kernel/kernel.cu).  Each entry point below names the reference interface it replaces.
+ *
+ * Conventions
+ *   - Every call returns an int status: NURBS_OK (0) or a negative NURBS_E_* code; nothing
+ *     calls exit().  nurbs_last_error() gives a message for the calling thread.
+ *   - Pointers named *_dev are device pointers owned by the caller; *_host are host pointers.
+ *     Entry points that take a `stream` enqueue work on it and return without waiting, unless
+ *     their comment says otherwise.  `stream` is a cudaStream_t passed as void* (NULL = the
+ *     legacy default stream).
+ *   - Layouts: (u,v) pairs and points are interleaved arrays of doubles (double2 / double3 in
+ *     the reference).  Control points are row-major over (u-index i, v-index j): i*cp_v + j.
+ *   - A surface handle may be used from several host threads; calls on one handle are
+ *     serialised by the caller's stream order.
+ */
+#ifndef GPU_NURBS_H
+#define GPU_NURBS_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ status codes */
+#define NURBS_OK              0
+#define NURBS_E_INVALID      -1   /* bad argument (degree, size, null pointer, knot order) */
+#define NURBS_E_CUDA         -2   /* a CUDA runtime call failed */
+#define NURBS_E_NOMEM        -3   /* device or host allocation failed */
+#define NURBS_E_IO           -4   /* file could not be opened / written */
+#define NURBS_E_PARSE        -5   /* malformed .nu text */
+#define NURBS_E_UNSUPPORTED  -6   /* valid input outside what this build handles */
+#define NURBS_E_BUDGET       -7   /* admission refused by a device-memory budget */
+#define NURBS_E_TIMEOUT      -8   /* a bounded wait ran out */
+#define NURBS_E_STATE        -9   /* call not valid in the object's current state */
+
+#define NURBS_MAX_DEGREE 7        /* MAX_DEGREE 8 = p+1, src/NURBS/Evaluate.cuh:15 */
+#define NURBS_TREE_NODES 65       /* root + 8x8 children (src/main.cu:283, kernel.cuh:23-25) */
+
+/* evaluation output blocks (bit set => 3 planes x[n],y[n],z[n] in the output, in this order) */
+#define NURBS_S    1u
+#define NURBS_SU   2u
+#define NURBS_SV   4u
+#define NURBS_SUU  8u
+#define NURBS_SUV 16u
+#define NURBS_SVV 32u
+
+/* precision schedules */
+#define NURBS_PREC_FP64   0   /* every iteration and contraction in FP64 */
+#define NURBS_PREC_MIXED  1   /* FP32 seeding/early iterations, FP64 final 2 steps + residual */
+#define NURBS_PREC_FP32   2   /* evaluation only: FP32 contraction of the FP32 span matrices */
+
+/* inversion status per query */
+#define NURBS_INV_FOUND        0   /* converged, in-domain, best candidate unique */
+#define NURBS_INV_AMBIGUOUS    1   /* converged; another distinct minimum is as close */
+#define NURBS_INV_NO_CANDIDATE 2   /* P lies in no tree box (NewInverse leaves flag unset) */
+#define NURBS_INV_NOT_CONVERGED 3  /* no candidate converged inside the knot domain */
+
+const char* nurbs_status_string(int status);
+const char* nurbs_last_error(void);
+const char* nurbs_version(void);
+
+/* ------------------------------------------------------------------- .nu files */
+/* Replaces readNu (src/main.cu:45-113): same tags NU, CP, KNu, KNv, DP.  Allocates host
+ * arrays owned by the descriptor; release with nurbs_nu_free.  Unlike the reference, a
+ * missing tag or short line returns NURBS_E_PARSE instead of looping forever. */
+typedef struct {
+    int degree_u, degree_v, cp_u, cp_v;
+    double* knots_u;   /* degree_u + cp_u + 1 */
+    double* knots_v;   /* degree_v + cp_v + 1 */
+    double* cps;       /* 3 * cp_u * cp_v, xyz interleaved, row-major i*cp_v + j */
+    double* weights;   /* cp_u * cp_v */
+} nurbs_nu_desc;
+
+int nurbs_nu_read(const char* path, nurbs_nu_desc* out);
+int nurbs_nu_parse(const char* text, int64_t len, nurbs_nu_desc* out);
+int nurbs_nu_write(const char* path, const nurbs_nu_desc* desc);
+void nurbs_nu_free(nurbs_nu_desc* desc);
+
+/* --------------------------------------------------------------- surface handle */
+typedef struct nurbs_surface_s* nurbs_surface_t;
+
+#define NURBS_PTR_HOST   0   /* knots/cps/weights are host pointers */
+#define NURBS_PTR_DEVICE 1   /* knots/cps/weights are device pointers */
+
+/* Uploads a surface and converts it to matrix form (stage a; replaces the GetMatrixN launch
+ * of src/main.cu:252): dense FP64 and FP32 span matrices over the non-empty spans.  Also
+ * builds the 2-level subdivision tree (stage c).  Synchronous: returns when done. */
+int nurbs_surface_create(int degree_u, int degree_v, int cp_u, int cp_v,
+                         const double* knots_u, const double* knots_v,
+                         const double* cps, const double* weights,
+                         int ptr_kind, void* stream, nurbs_surface_t* out);
+int nurbs_surface_destroy(nurbs_surface_t s);
+
+typedef struct {
+    int degree_u, degree_v, cp_u, cp_v;
+    int spans_u, spans_v;          /* non-empty spans per direction */
+    int64_t device_bytes;          /* device memory held by the handle */
+    int tree_built;                /* 1 once the tree exists */
+} nurbs_surface_info_t;
+int nurbs_surface_info(nurbs_surface_t s, nurbs_surface_info_t* info);
+
+/* ------------------------------------------------------------ stage a: matrix form */
+/* Size in doubles of the reference's MatrixN buffer (src/main.cu:182). */
+int64_t nurbs_matrix_n_size(int degree_u, int degree_v, int cp_u, int cp_v);
+/* Offset of component c of knot span (i,j) in MatrixN: MatrixNPosition
+ * (src/NURBS/Evaluate.cu:110-112). */
+int64_t nurbs_matrix_n_position(int i, int j, int degree_u, int degree_v, int cp_u, int cp_v, int c);
+/* Writes the handle's span matrices into a caller buffer in the reference's MatrixN layout
+ * (slots of empty spans are left untouched, as GetMatrixN leaves them). */
+int nurbs_get_matrix_n(nurbs_surface_t s, double* matrix_n_dev, void* stream);
+/* Legacy GetMatrixN (src/NURBS/Evaluate.cu:3-88) with the reference's argument list; all
+ * pointers are device pointers and control_points is double3[cp_u*cp_v].  No device heap and
+ * no dynamic parallelism; values are bit-identical to the reference's FP64 arithmetic. */
+int nurbs_get_matrix_n_raw(double* matrix_n_dev, int degree_u, int degree_v, int cp_u, int cp_v,
+                           const double* knots_u_dev, const double* knots_v_dev,
+                           const double* control_points_dev, const double* weights_dev, void* stream);
+
+/* -------------------------------------------------------------- stage b: evaluation */
+/* Batched evaluation at n parameter pairs uv_dev[2n] (global parameters).  out_dev is SoA:
+ * for each set bit of mask, in the order S,Su,Sv,Suu,Suv,Svv, three planes of n doubles.
+ * Replaces MatrixSurfacePoint + MatrixSurfaceDerivative{U,V,UU,UV,VV}
+ * (src/NURBS/Evaluate.cu:159-227, 535-930) driven per point as EvaluateRandom does
+ * (:1023-1038).  precision NURBS_PREC_FP64 only (see nurbs_eval_f32). */
+int nurbs_eval(nurbs_surface_t s, const double* uv_dev, int64_t n, unsigned mask,
+               double* out_dev, int precision, void* stream);
+/* FP32 variant: float (u,v) in, float SoA out, contraction of the FP32 span matrices. */
+int nurbs_eval_f32(nurbs_surface_t s, const float* uv_dev, int64_t n, unsigned mask,
+                   float* out_dev, void* stream);
+/* Legacy EvaluateRandom (src/NURBS/Evaluate.cu:1023-1038): S at n points straight from a
+ * reference-layout MatrixN; xyz_dev is double3[n].  Guards index < n (the reference does not). */
+int nurbs_evaluate_random(const double* uv_dev, double* xyz_dev, int64_t n, const double* matrix_n_dev,
+                          int degree_u, int degree_v, int cp_u, int cp_v,
+                          const double* knots_u_dev, const double* knots_v_dev, void* stream);
+
+/* ------------------------------------------------ stage c: subdivision tree / culling */
+/* (Re)builds the tree: GetPoints + GetSecondDerivatives + Max_Sequential_Addressing_Shared
+ * + TightBoundingBox for levels 0..levels-1 (src/main.cu:280-309).  Only levels == 2 (the
+ * reference's setting) is supported. */
+int nurbs_build_tree(nurbs_surface_t s, int levels, void* stream);
+/* Copies the tree to host memory in the reference TreeNode order (kernel.cuh:30-39):
+ * per node 10 doubles {uv.lb.x, uv.lb.y, uv.rt.x, uv.rt.y, lb.x, lb.y, lb.z, rt.x, rt.y, rt.z},
+ * plus Divided[] and built[] (1 where the node was computed).  Synchronous. */
+int nurbs_tree_export(nurbs_surface_t s, double* nodes_host, unsigned char* divided_host,
+                      unsigned char* built_host);
+/* Candidate lists (the NewInverse scan, src/kernel/kernel.cu:456-457, over built nodes):
+ * for query k, counts_dev[k] ascending node indices in list_dev[k*65 ...]. */
+int nurbs_candidates(nurbs_surface_t s, const double* P_dev, int64_t n, int* list_dev, int* counts_dev,
+                     void* stream);
+
+/* ----------------------------------------------------------- stage d: inversion */
+/* Point inversion of n points P_dev[3n]: candidates from the tree, Gauss-Newton from each
+ * candidate's uv-centre (GaussNewton, src/kernel/kernel.cu:151-249), converged and kept when
+ * inside the knot domain; the closest wins.  Outputs uv_dev[2n], status_dev[n] (NURBS_INV_*),
+ * residual_dev[n] = |S(uv) - P| in FP64.  precision: NURBS_PREC_FP64 or NURBS_PREC_MIXED. */
+int nurbs_invert(nurbs_surface_t s, const double* P_dev, int64_t n, double* uv_dev, int* status_dev,
+                 double* residual_dev, int precision, void* stream);
+/* Same with host buffers: copies P in, runs, copies results out, waits.  Pinned host memory
+ * gives the fastest copies. */
+int nurbs_invert_host(nurbs_surface_t s, const double* P_host, int64_t n, double* uv_host, int* status_host,
+                      double* residual_host, int precision, void* stream);
+
+/* ------------------------------------------------------------------ diagnostics */
+/* Measured FMA throughput of the current GPU in TFLOP/s (bits = 64 or 32): independent FMA
+ * chains over 8 CTAs per SM, timed with CUDA events.  No reference counterpart; used as the
+ * roofline denominator for the FP64/FP32 pipes.  Synchronous. */
+int nurbs_probe_fp_peak(int bits, double* tflops, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

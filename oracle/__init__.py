@@ -1,0 +1,228 @@
+"""CPU oracle — test infrastructure only.
+
+ctypes bindings for ``liboracle.so`` (the plain-C restatement of the reference's FP64
+path, ``nurbs_oracle.c``) and, where it was built, ``_ref/libnurbs_ref.so`` (the
+reference's own functions compiled for the host; see ``ref_shim.cu``).  Only the tests,
+``__graft_entry__.smoke()`` and the CPU-baseline leg of ``bench.py`` import this module.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+TREE_NODES = 65
+
+S, SU, SV, SUU, SUV, SVV = 1, 2, 4, 8, 16, 32
+FOUND_UNIQUE, FOUND_AMBIGUOUS, NO_CANDIDATE, NOT_CONVERGED = 0, 1, 2, 3
+
+_dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+_ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+_bp = np.ctypeslib.ndpointer(dtype=np.uint8, flags="C_CONTIGUOUS")
+
+
+class _Surf(C.Structure):
+    _fields_ = [("degree_u", C.c_int), ("degree_v", C.c_int), ("cp_u", C.c_int), ("cp_v", C.c_int),
+                ("knots_u", C.c_void_p), ("knots_v", C.c_void_p), ("cps", C.c_void_p), ("weights", C.c_void_p)]
+
+
+def build(force: bool = False) -> str:
+    """Compile liboracle.so in place (gcc, no GPU needed)."""
+    so = os.path.join(HERE, "liboracle.so")
+    if force or not os.path.exists(so) or os.path.getmtime(so) < max(
+            os.path.getmtime(os.path.join(HERE, f)) for f in ("nurbs_oracle.c", "nurbs_oracle.h")):
+        subprocess.run(["make", "-s", "-C", HERE, "liboracle.so"], check=True)
+    return so
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        _lib = C.CDLL(build())
+        L = _lib
+        L.orc_matrix_n_size.restype = C.c_int64
+        L.orc_matrix_n_size.argtypes = [C.POINTER(_Surf)]
+        L.orc_matrix_n.restype = C.c_int
+        L.orc_matrix_n.argtypes = [C.POINTER(_Surf), _dp]
+        L.orc_eval.restype = None
+        L.orc_eval.argtypes = [C.POINTER(_Surf), _dp, _dp, C.c_int64, C.c_uint, _dp, C.c_int]
+        L.orc_build_tree.restype = None
+        L.orc_build_tree.argtypes = [C.POINTER(_Surf), _dp, _dp, _bp, _bp]
+        L.orc_candidates.restype = C.c_int
+        L.orc_candidates.argtypes = [_dp, _bp, _dp, _ip]
+        L.orc_invert.restype = None
+        L.orc_invert.argtypes = [C.POINTER(_Surf), _dp, _dp, _bp, _dp, C.c_int64, C.c_int, _dp, _ip, _dp,
+                                 C.c_void_p, C.c_int]
+        L.orc_gauss_newton_shipped.restype = C.c_int
+        L.orc_gauss_newton_shipped.argtypes = [C.POINTER(_Surf), _dp, _dp, _dp, C.c_double, _dp]
+        L.orc_find_span.restype = C.c_int
+        L.orc_find_span.argtypes = [C.c_int, C.c_int, _dp, C.c_double]
+        L.orc_cube.restype = C.c_double
+        L.orc_cube.argtypes = [C.c_double]
+        L.orc_point_r.restype = None
+        L.orc_point_r.argtypes = [_dp, C.c_int, C.c_int, C.c_double, C.c_double, _dp]
+    return _lib
+
+
+class OracleSurface:
+    """Holds contiguous arrays for one surface and the oracle's span matrices / tree."""
+
+    def __init__(self, surf):
+        self.p, self.q = int(surf["p"]), int(surf["q"])
+        self.nu, self.nv = int(surf["nu"]), int(surf["nv"])
+        self.ku = np.ascontiguousarray(surf["knots_u"], dtype=np.float64)
+        self.kv = np.ascontiguousarray(surf["knots_v"], dtype=np.float64)
+        self.cps = np.ascontiguousarray(surf["cps"], dtype=np.float64).reshape(-1, 3)
+        self.w = np.ascontiguousarray(surf["weights"], dtype=np.float64).reshape(-1)
+        self._s = _Surf(self.p, self.q, self.nu, self.nv, self.ku.ctypes.data, self.kv.ctypes.data,
+                        self.cps.ctypes.data, self.w.ctypes.data)
+        self._M = None
+        self._tree = None
+
+    @property
+    def matrix_n(self) -> np.ndarray:
+        if self._M is None:
+            n = lib().orc_matrix_n_size(C.byref(self._s))
+            M = np.zeros(n, dtype=np.float64)
+            rc = lib().orc_matrix_n(C.byref(self._s), M)
+            if rc < 0:
+                raise ValueError("oracle: unsupported surface")
+            self._M = M
+        return self._M
+
+    def eval(self, uv: np.ndarray, mask: int, threads: int = 0) -> np.ndarray:
+        uv = np.ascontiguousarray(uv, dtype=np.float64).reshape(-1, 2)
+        n = uv.shape[0]
+        nb = bin(mask & 63).count("1")
+        out = np.empty(3 * nb * n, dtype=np.float64)
+        lib().orc_eval(C.byref(self._s), self.matrix_n, uv, n, mask, out, threads)
+        return out.reshape(3 * nb, n)
+
+    def tree(self):
+        if self._tree is None:
+            t = np.zeros(TREE_NODES * 10, dtype=np.float64)
+            d = np.zeros(TREE_NODES, dtype=np.uint8)
+            b = np.zeros(TREE_NODES, dtype=np.uint8)
+            lib().orc_build_tree(C.byref(self._s), self.matrix_n, t, d, b)
+            self._tree = (t.reshape(TREE_NODES, 10), d, b)
+        return self._tree
+
+    def candidates(self, P: np.ndarray):
+        t, _, b = self.tree()
+        tf = np.ascontiguousarray(t.reshape(-1))
+        P = np.ascontiguousarray(P, dtype=np.float64).reshape(-1, 3)
+        out = []
+        lst = np.zeros(TREE_NODES, dtype=np.int32)
+        for k in range(P.shape[0]):
+            n = lib().orc_candidates(tf, b, np.ascontiguousarray(P[k]), lst)
+            out.append(lst[:n].copy())
+        return out
+
+    def invert(self, P: np.ndarray, max_iter: int = 200, threads: int = 0):
+        t, _, b = self.tree()
+        P = np.ascontiguousarray(P, dtype=np.float64).reshape(-1, 3)
+        n = P.shape[0]
+        uv = np.empty(2 * n, dtype=np.float64)
+        st = np.empty(n, dtype=np.int32)
+        res = np.empty(n, dtype=np.float64)
+        it = np.empty(n, dtype=np.int32)
+        lib().orc_invert(C.byref(self._s), self.matrix_n, np.ascontiguousarray(t.reshape(-1)), b, P, n, max_iter,
+                         uv, st, res, it.ctypes.data, threads)
+        return uv.reshape(n, 2), st, res, it
+
+    def gauss_newton_shipped(self, seed, P, max_edge):
+        uv = np.zeros(2)
+        ok = lib().orc_gauss_newton_shipped(C.byref(self._s), self.matrix_n, np.asarray(seed, np.float64),
+                                            np.asarray(P, np.float64), max_edge, uv)
+        return bool(ok), uv
+
+
+# ------------------------------------------------------------------ reference shim
+_ref = None
+
+
+def ref_lib():
+    """The reference's own functions compiled for the host (only where oracle/_ref was built)."""
+    global _ref
+    if _ref is None:
+        so = os.path.join(HERE, "_ref", "libnurbs_ref.so")
+        if not os.path.exists(so):
+            return None
+        R = C.CDLL(so)
+        R.ref_matrix_n.restype = C.c_int
+        R.ref_matrix_n.argtypes = [C.c_int] * 4 + [_dp, _dp, _dp, _dp, _dp]
+        R.ref_eval.restype = None
+        R.ref_eval.argtypes = [C.c_int] * 4 + [_dp, _dp, _dp, _dp, C.c_longlong, C.c_uint, _dp]
+        R.ref_build_tree.restype = None
+        R.ref_build_tree.argtypes = [C.c_int] * 4 + [_dp, _dp, _dp, _dp, _bp, _bp]
+        R.ref_box_check.restype = C.c_int
+        R.ref_box_check.argtypes = [_dp, _dp]
+        R.ref_gauss_newton.restype = C.c_int
+        R.ref_gauss_newton.argtypes = [C.c_int] * 4 + [_dp, _dp, _dp, _dp, _dp, C.c_double, _dp]
+        R.ref_find_span.restype = C.c_int
+        R.ref_find_span.argtypes = [C.c_int, C.c_int, _dp, C.c_double]
+        _ref = R
+    return _ref
+
+
+class RefSurface:
+    """Same interface as OracleSurface, backed by the reference's own compiled functions."""
+
+    def __init__(self, surf):
+        self.o = OracleSurface(surf)
+        self.R = ref_lib()
+        if self.R is None:
+            raise RuntimeError("oracle/_ref not built")
+        self._M = None
+        self._tree = None
+
+    def _dims(self):
+        o = self.o
+        return (o.p, o.q, o.nu, o.nv)
+
+    @property
+    def matrix_n(self):
+        if self._M is None:
+            o = self.o
+            M = np.zeros(lib().orc_matrix_n_size(C.byref(o._s)), dtype=np.float64)
+            self.R.ref_matrix_n(*self._dims(), o.ku, o.kv, np.ascontiguousarray(o.cps.reshape(-1)), o.w, M)
+            self._M = M
+        return self._M
+
+    def eval(self, uv, mask):
+        uv = np.ascontiguousarray(uv, dtype=np.float64).reshape(-1, 2)
+        n = uv.shape[0]
+        nb = bin(mask & 63).count("1")
+        out = np.empty(3 * nb * n, dtype=np.float64)
+        self.R.ref_eval(*self._dims(), self.o.ku, self.o.kv, self.matrix_n, uv, n, mask, out)
+        return out.reshape(3 * nb, n)
+
+    def tree(self):
+        if self._tree is None:
+            t = np.zeros(TREE_NODES * 10, dtype=np.float64)
+            d = np.zeros(TREE_NODES, dtype=np.uint8)
+            b = np.zeros(TREE_NODES, dtype=np.uint8)
+            self.R.ref_build_tree(*self._dims(), self.o.ku, self.o.kv, self.matrix_n, t, d, b)
+            self._tree = (t.reshape(TREE_NODES, 10), d, b)
+        return self._tree
+
+    def candidates(self, P):
+        t, _, b = self.tree()
+        P = np.ascontiguousarray(P, dtype=np.float64).reshape(-1, 3)
+        out = []
+        for k in range(P.shape[0]):
+            pk = np.ascontiguousarray(P[k])
+            out.append(np.array([i for i in range(TREE_NODES)
+                                 if b[i] and self.R.ref_box_check(np.ascontiguousarray(t[i]), pk)], dtype=np.int32))
+        return out
+
+    def gauss_newton_shipped(self, node_uv4, P, max_edge):
+        uv = np.zeros(2)
+        ok = self.R.ref_gauss_newton(*self._dims(), self.o.ku, self.o.kv, self.matrix_n,
+                                     np.asarray(node_uv4, np.float64), np.asarray(P, np.float64), max_edge, uv)
+        return bool(ok), uv

@@ -1,0 +1,595 @@
+/*
+ * CPU ORACLE — test infrastructure only (see nurbs_oracle.h).
+ *
+ * Plain-C restatement of the reference FP64 path.  Arithmetic follows the reference's
+ * expression order term by term (and is compiled without FMA contraction) so that the
+ * values match the reference's own functions bit for bit where the reference is
+ * deterministic.  Two documented substitutions:
+ *   - pow(h,2) is h*h (IEEE-exact rounding of the square) and pow(h,3) is orc_cube(h),
+ *     the once-rounded cube; both equal a correctly rounded pow.
+ *   - the tree's block max/min reductions are done sequentially; max/min are exact, so
+ *     only the sign of a zero could differ from the reference's shared-memory tree.
+ */
+#include "nurbs_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+/* ---------------------------------------------------------------- small helpers */
+
+double orc_cube(double x) {
+    /* x^2 = a + b exactly (Dekker/Ogita-Rump-Oishi TwoProduct via fma). */
+    double a = x * x;
+    double b = fma(x, x, -a);
+    /* a*x = c + d exactly; b*x is ~2^-53 of the result, so its own rounding is ~2^-106. */
+    double c = a * x;
+    double d = fma(a, x, -c);
+    double e = b * x;
+    return c + (d + e);
+}
+
+static double sq(double x) { return x * x; }
+
+int64_t orc_matrix_n_position(int i, int j, int degree_u, int degree_v, int cp_u, int cp_v, int c) {
+    /* MatrixNPosition, src/NURBS/Evaluate.cu:110-112 */
+    (void)cp_u;
+    int64_t k12 = (int64_t)(degree_u + 1) * (degree_v + 1);
+    return (((int64_t)i * (degree_v + cp_v) + j) * 4 + c) * k12;
+}
+
+int64_t orc_matrix_n_size(const orc_surface* s) {
+    /* cudaMalloc size of MatrixN, src/main.cu:182 */
+    return (int64_t)(s->degree_u + s->cp_u) * (s->degree_v + s->cp_v) * 4 *
+           (s->degree_u + 1) * (s->degree_v + 1);
+}
+
+int orc_find_span(int degree, int cp, const double* knots, double u) {
+    /* findSpan, src/NURBS/Evaluate.cu:504-533 */
+    int n = cp - 1;
+    if (u >= knots[n + 1]) return n;
+    if (u <= knots[degree]) return degree;
+    int low = degree, high = n + 1;
+    int mid = (int)((low + high) / 2.0);
+    while (u < knots[mid] || u >= knots[mid + 1]) {
+        if (u < knots[mid]) high = mid; else low = mid;
+        mid = (int)((low + high) / 2.0);
+    }
+    return mid;
+}
+
+/* ------------------------------------------------- stage a: span matrices (GetMatrixN) */
+
+/* Nabla(knot, d, i, k) = knot[i+d-1+k] - knot[i+d-1]   (Evaluate.cu:105-108) */
+static double nabla(const double* knot, int d, int i, int k) {
+    int index = i + d - 1;
+    return knot[index + k] - knot[index];
+}
+
+/* Basis-to-power matrix of one span: N[r][c] = Nrc(knot, d, r+1, c+1, I, I, d) with
+ * I = span - (d-1) (Evaluate.cu:16-20).  Nrc (Evaluate.cu:90-103) is a pure function of
+ * (m, r, c, j); it is tabulated bottom-up over m so each state is computed once, with the
+ * reference's expression for every state, which gives the same values as the recursion. */
+static void span_basis_matrix(const double* knot, int d, int span, double* N /* (d+1)^2 */) {
+    const int I = span - (d - 1);
+    const int R0 = 1 - d, RN = 2 * d + 1;     /* r in [1-d, d+1] */
+    const int J0 = I - d, JN = d + 1;         /* j in [I-d, I]   */
+    double prev[(2 * ORC_MAX_DEGREE + 1) * (ORC_MAX_DEGREE + 1)];
+    double cur[(2 * ORC_MAX_DEGREE + 1) * (ORC_MAX_DEGREE + 1)];
+    for (int c = 1; c <= d + 1; ++c) {
+        /* m = 0 (Evaluate.cu:91-95) */
+        for (int ri = 0; ri < RN; ++ri)
+            for (int ji = 0; ji < JN; ++ji) {
+                int r = R0 + ri, j = J0 + ji;
+                prev[ri * JN + ji] = (((I + c - 1) == (j + d)) && (r == 1)) ? 1.0 : 0.0;
+            }
+        for (int m = 1; m <= d; ++m) {
+            /* states reachable at depth m: j in [I-(d-m), I], r in [1-(d-m), d+1] */
+            for (int ri = 0; ri < RN; ++ri)
+                for (int ji = 0; ji < JN; ++ji) cur[ri * JN + ji] = 0.0;
+            for (int r = 1 - (d - m); r <= d + 1; ++r) {
+                int ri = r - R0;
+                for (int j = I - (d - m); j <= I; ++j) {
+                    int ji = j - J0;
+                    /* ri-1 >= 0 and ji-1 >= 0 hold on the reachable set */
+                    double n1 = prev[(ri - 1) * JN + ji];       /* Nrc(m-1, r-1, c, j)   */
+                    double n2 = prev[ri * JN + ji];             /* Nrc(m-1, r,   c, j)   */
+                    double n3 = prev[ri * JN + (ji - 1)];       /* Nrc(m-1, r,   c, j-1) */
+                    double n4 = prev[(ri - 1) * JN + (ji - 1)]; /* Nrc(m-1, r-1, c, j-1) */
+                    double A = nabla(knot, d, I, 1);
+                    double B = nabla(knot, d, j, d - m + 1);
+                    double C = nabla(knot, d, j, I - j);
+                    cur[ri * JN + ji] = A / B * n1 + C / B * n2 + (1 - C / B) * n3 + (-A / B) * n4;
+                }
+            }
+            memcpy(prev, cur, sizeof(double) * RN * JN);
+        }
+        for (int r = 1; r <= d + 1; ++r) N[(r - 1) * (d + 1) + (c - 1)] = prev[(r - R0) * JN + (I - J0)];
+    }
+}
+
+/* matrix_mult (src/util/Matrix.cu:43-52): c[i][j] = sum over l ascending, from 0. */
+static void mat_mult(const double* a, const double* b, double* c, int m, int n, int k) {
+    for (int i = 0; i < m; i++)
+        for (int j = 0; j < k; j++) {
+            double acc = 0;
+            for (int l = 0; l < n; l++) acc += a[i * n + l] * b[l * k + j];
+            c[i * k + j] = acc;
+        }
+}
+
+int orc_matrix_n(const orc_surface* s, double* matrix_n) {
+    const int p = s->degree_u, q = s->degree_v, k1 = p + 1, k2 = q + 1;
+    const int nu = s->cp_u, nv = s->cp_v;
+    if (p < 1 || q < 1 || p > ORC_MAX_DEGREE || q > ORC_MAX_DEGREE || nu < p + 1 || nv < q + 1) return -1;
+    double* Nu = (double*)malloc(sizeof(double) * k1 * k1 * (nu));
+    double* Nv = (double*)malloc(sizeof(double) * k2 * k2 * (nv));
+    /* Nu depends on i only and Nv on j only: compute each once (the reference recomputes
+     * them per (i,j) thread, with identical results). */
+    for (int i = p; i < nu; ++i)
+        if (s->knots_u[i] != s->knots_u[i + 1]) span_basis_matrix(s->knots_u, p, i, Nu + (size_t)i * k1 * k1);
+    for (int j = q; j < nv; ++j)
+        if (s->knots_v[j] != s->knots_v[j + 1]) span_basis_matrix(s->knots_v, q, j, Nv + (size_t)j * k2 * k2);
+    int written = 0;
+    double mid[4][(ORC_MAX_DEGREE + 1) * (ORC_MAX_DEGREE + 1)];
+    double tmp[(ORC_MAX_DEGREE + 1) * (ORC_MAX_DEGREE + 1)];
+    double nvt[(ORC_MAX_DEGREE + 1) * (ORC_MAX_DEGREE + 1)];
+    for (int i = p; i < nu; ++i) {
+        if (s->knots_u[i] == s->knots_u[i + 1]) continue;   /* Evaluate.cu:10-11 */
+        for (int j = q; j < nv; ++j) {
+            if (s->knots_v[j] == s->knots_v[j + 1]) continue;
+            const double* nvm = Nv + (size_t)j * k2 * k2;
+            for (int m = 0; m < k2; ++m)          /* NvT[n][m] = Nv[m][n]  (Evaluate.cu:24-28) */
+                for (int n = 0; n < k2; ++n) nvt[n * k2 + m] = nvm[m * k2 + n];
+            for (int a = 0; a <= p; ++a)          /* Middle_c = P_c * w  (Evaluate.cu:35-43) */
+                for (int b = 0; b <= q; ++b) {
+                    size_t idx = (size_t)(a + i - p) * nv + (b + j - q);
+                    double w = s->weights[idx];
+                    mid[0][a * k2 + b] = s->cps[3 * idx + 0] * w;
+                    mid[1][a * k2 + b] = s->cps[3 * idx + 1] * w;
+                    mid[2][a * k2 + b] = s->cps[3 * idx + 2] * w;
+                    mid[3][a * k2 + b] = w;
+                }
+            for (int c = 0; c < 4; ++c) {         /* temp = Middle*NvT ; out = Nu*temp  (:58-66) */
+                mat_mult(mid[c], nvt, tmp, k1, k2, k2);
+                mat_mult(Nu + (size_t)i * k1 * k1, tmp,
+                         matrix_n + orc_matrix_n_position(i, j, p, q, nu, nv, c), k1, k1, k2);
+            }
+            ++written;
+        }
+    }
+    free(Nu);
+    free(Nv);
+    return written;
+}
+
+/* ------------------------------------------------------------- stage b: evaluation */
+
+typedef struct { double x, y, z, w; } d4;
+typedef struct { double x, y, z; } d3;
+
+static void power_vec(double t, int k, double* out) {      /* [1, t, t^2, ...] running product */
+    double now = 1;
+    for (int i = 0; i < k; i++) { out[i] = now; now *= t; }
+}
+static void dpower_vec(double t, int k, double* out) {     /* Evaluate.cu:540-545 */
+    double now = 1;
+    out[0] = 0;
+    for (int i = 0; i < k - 1; i++) { out[i + 1] = (i + 1) * now; now *= t; }
+}
+static void ddpower_vec(double t, int k, double* out) {    /* Evaluate.cu:680-685 */
+    double now = 1;
+    out[0] = 0;
+    if (k > 1) out[1] = 0;
+    for (int i = 0; i < k - 2; i++) { out[i + 2] = (i + 2) * (i + 1) * now; now *= t; }
+}
+
+/* temp_c = M_c * vec (k1 rows), then r.c = uvec . temp_c  (matrix_mult order) */
+static void mv4(const double* middle, int k1, int k2, const double* vec, double tmp[4][8]) {
+    for (int c = 0; c < 4; ++c) mat_mult(middle + c * k1 * k2, vec, tmp[c], k1, k2, 1);
+}
+static d4 dot4(const double* uvec, int k1, double tmp[4][8]) {
+    d4 r;
+    mat_mult(uvec, tmp[0], &r.x, 1, k1, 1);
+    mat_mult(uvec, tmp[1], &r.y, 1, k1, 1);
+    mat_mult(uvec, tmp[2], &r.z, 1, k1, 1);
+    mat_mult(uvec, tmp[3], &r.w, 1, k1, 1);
+    return r;
+}
+
+void orc_point_r(const double* middle, int p, int q, double u, double v, double R[4]) {
+    /* MatrixSurfacePoint, Evaluate.cu:159-227 */
+    int k1 = p + 1, k2 = q + 1;
+    double U[8], V[8], tmp[4][8];
+    power_vec(u, k1, U);
+    power_vec(v, k2, V);
+    mv4(middle, k1, k2, V, tmp);
+    d4 r = dot4(U, k1, tmp);
+    R[0] = r.x; R[1] = r.y; R[2] = r.z; R[3] = r.w;
+}
+
+static d4 R_of(const double* middle, int p, int q, double u, double v) {
+    double R[4];
+    orc_point_r(middle, p, q, u, v, R);
+    d4 r = {R[0], R[1], R[2], R[3]};
+    return r;
+}
+
+/* old MatrixSurfaceDerivativeU, Evaluate.cu:535-598 */
+static d3 der_u(const double* middle, int p, int q, double u, double v, d4 R, double spanU) {
+    int k1 = p + 1, k2 = q + 1;
+    double dU[8], V[8], tmp[4][8];
+    dpower_vec(u, k1, dU);
+    power_vec(v, k2, V);
+    mv4(middle, k1, k2, V, tmp);
+    d4 RdU = dot4(dU, k1, tmp);
+    double h = R.w, hdU = RdU.w;
+    double s = -hdU / sq(h);
+    d3 o;
+    o.x = (R.x * s + RdU.x / h) * spanU;
+    o.y = (R.y * s + RdU.y / h) * spanU;
+    o.z = (R.z * s + RdU.z / h) * spanU;
+    return o;
+}
+
+/* old MatrixSurfaceDerivativeV, Evaluate.cu:600-665 */
+static d3 der_v(const double* middle, int p, int q, double u, double v, d4 R, double spanV) {
+    int k1 = p + 1, k2 = q + 1;
+    double U[8], dV[8], tmp[4][8];
+    power_vec(u, k1, U);
+    dpower_vec(v, k2, dV);
+    mv4(middle, k1, k2, dV, tmp);
+    d4 RdV = dot4(U, k1, tmp);
+    double h = R.w, hdV = RdV.w;
+    double s = -hdV / sq(h);
+    d3 o;
+    o.x = (R.x * s + RdV.x / h) * spanV;
+    o.y = (R.y * s + RdV.y / h) * spanV;
+    o.z = (R.z * s + RdV.z / h) * spanV;
+    return o;
+}
+
+/* old MatrixSurfaceDerivativeUU, Evaluate.cu:667-741 */
+static d3 der_uu(const double* middle, int p, int q, double u, double v, d4 R, double spanU) {
+    int k1 = p + 1, k2 = q + 1;
+    double dU[8], ddU[8], V[8], tmp[4][8];
+    dpower_vec(u, k1, dU);
+    ddpower_vec(u, k1, ddU);
+    power_vec(v, k2, V);
+    mv4(middle, k1, k2, V, tmp);
+    d4 RdU = dot4(dU, k1, tmp);
+    d4 RdUU = dot4(ddU, k1, tmp);
+    double h = R.w, hdU = RdU.w, hdUU = RdUU.w;
+    double s1 = (2 * sq(hdU) / orc_cube(h)) - (hdUU / sq(h));
+    double s2 = -hdU / sq(h);
+    d3 o;
+    o.x = ((R.x * s1 + (2 * RdU.x) * s2) + RdUU.x / h) * spanU * spanU;
+    o.y = ((R.y * s1 + (2 * RdU.y) * s2) + RdUU.y / h) * spanU * spanU;
+    o.z = ((R.z * s1 + (2 * RdU.z) * s2) + RdUU.z / h) * spanU * spanU;
+    return o;
+}
+
+/* old MatrixSurfaceDerivativeUV, Evaluate.cu:743-847 */
+static d3 der_uv(const double* middle, int p, int q, double u, double v, d4 R, double spanU, double spanV) {
+    int k1 = p + 1, k2 = q + 1;
+    double U[8], dU[8], V[8], dV[8], tmp[4][8];
+    power_vec(u, k1, U);
+    dpower_vec(u, k1, dU);
+    power_vec(v, k2, V);
+    dpower_vec(v, k2, dV);
+    mv4(middle, k1, k2, V, tmp);
+    d4 RdU = dot4(dU, k1, tmp);
+    mv4(middle, k1, k2, dV, tmp);
+    d4 RdV = dot4(U, k1, tmp);
+    d4 RdUV = dot4(dU, k1, tmp);
+    double h = R.w, hdU = RdU.w, hdV = RdV.w, hdUV = RdUV.w;
+    double h2 = sq(h), h3 = orc_cube(h);
+    d3 o;
+    o.x = ((((RdUV.x * h - hdV * RdU.x) - RdV.x * hdU) - R.x * hdUV) / h2 + ((2 * R.x) * hdU * hdV) / h3) * spanU * spanV;
+    o.y = ((((RdUV.y * h - hdV * RdU.y) - RdV.y * hdU) - R.y * hdUV) / h2 + ((2 * R.y) * hdU * hdV) / h3) * spanU * spanV;
+    o.z = ((((RdUV.z * h - hdV * RdU.z) - RdV.z * hdU) - R.z * hdUV) / h2 + ((2 * R.z) * hdU * hdV) / h3) * spanU * spanV;
+    return o;
+}
+
+/* old MatrixSurfaceDerivativeVV, Evaluate.cu:849-930 (contracts U first: temp = U^T M) */
+static d3 der_vv(const double* middle, int p, int q, double u, double v, d4 R, double spanV) {
+    int k1 = p + 1, k2 = q + 1;
+    double U[8], dV[8], ddV[8], tmp[4][8];
+    power_vec(u, k1, U);
+    dpower_vec(v, k2, dV);
+    ddpower_vec(v, k2, ddV);
+    for (int c = 0; c < 4; ++c) mat_mult(U, middle + c * k1 * k2, tmp[c], 1, k1, k2);
+    d4 RdV, RdVV;
+    mat_mult(tmp[0], dV, &RdV.x, 1, k2, 1);
+    mat_mult(tmp[1], dV, &RdV.y, 1, k2, 1);
+    mat_mult(tmp[2], dV, &RdV.z, 1, k2, 1);
+    mat_mult(tmp[3], dV, &RdV.w, 1, k2, 1);
+    mat_mult(tmp[0], ddV, &RdVV.x, 1, k2, 1);
+    mat_mult(tmp[1], ddV, &RdVV.y, 1, k2, 1);
+    mat_mult(tmp[2], ddV, &RdVV.z, 1, k2, 1);
+    mat_mult(tmp[3], ddV, &RdVV.w, 1, k2, 1);
+    double h = R.w, hdV = RdV.w, hdVV = RdVV.w;
+    double s1 = (2 * sq(hdV) / orc_cube(h)) - (hdVV / sq(h));
+    double s2 = -hdV / sq(h);
+    d3 o;
+    o.x = ((R.x * s1 + (2 * RdV.x) * s2) + RdVV.x / h) * spanV * spanV;
+    o.y = ((R.y * s1 + (2 * RdV.y) * s2) + RdVV.y / h) * spanV * spanV;
+    o.z = ((R.z * s1 + (2 * RdV.z) * s2) + RdVV.z / h) * spanV * spanV;
+    return o;
+}
+
+typedef struct {
+    const double* middle;
+    double u, v;           /* local parameters in [0,1] of the span */
+    double spanU, spanV;   /* derivative scale (kernel.cu:167-168) */
+} span_loc;
+
+/* findSpan + local parameter + MatrixNPosition as in EvaluateRandom (Evaluate.cu:1029-1034)
+ * and GaussNewton (kernel.cu:161-169). */
+static span_loc locate(const orc_surface* s, const double* M, double uu, double vv) {
+    const int p = s->degree_u, q = s->degree_v;
+    const double* ku = s->knots_u;
+    const double* kv = s->knots_v;
+    int m = orc_find_span(p, s->cp_u, ku, uu);
+    int n = orc_find_span(q, s->cp_v, kv, vv);
+    span_loc L;
+    L.u = (uu - ku[m]) / (ku[m + 1] - ku[m]);
+    L.v = (vv - kv[n]) / (kv[n + 1] - kv[n]);
+    L.spanU = (ku[p + s->cp_u] - ku[0]) / (ku[m + 1] - ku[m]);
+    L.spanV = (kv[q + s->cp_v] - kv[0]) / (kv[n + 1] - kv[n]);
+    L.middle = M + orc_matrix_n_position(m, n, p, q, s->cp_u, s->cp_v, 0);
+    return L;
+}
+
+static d3 cart(d4 R) {     /* homogenousToCartesian, src/util/ExtraMath.cu:3-5 */
+    d3 o = {R.x / R.w, R.y / R.w, R.z / R.w};
+    return o;
+}
+
+void orc_eval(const orc_surface* s, const double* M, const double* uv, int64_t n, unsigned mask,
+              double* out, int threads) {
+    const int p = s->degree_u, q = s->degree_v;
+    int nblk = 0;
+    for (int b = 0; b < 6; ++b) nblk += (mask >> b) & 1u;
+    (void)nblk;
+#ifdef _OPENMP
+    if (threads <= 0) threads = omp_get_max_threads();
+#pragma omp parallel for schedule(static) num_threads(threads)
+#endif
+    for (int64_t k = 0; k < n; ++k) {
+        span_loc L = locate(s, M, uv[2 * k], uv[2 * k + 1]);
+        d4 R = R_of(L.middle, p, q, L.u, L.v);
+        d3 blk[6];
+        if (mask & ORC_S) blk[0] = cart(R);
+        if (mask & ORC_SU) blk[1] = der_u(L.middle, p, q, L.u, L.v, R, L.spanU);
+        if (mask & ORC_SV) blk[2] = der_v(L.middle, p, q, L.u, L.v, R, L.spanV);
+        if (mask & ORC_SUU) blk[3] = der_uu(L.middle, p, q, L.u, L.v, R, L.spanU);
+        if (mask & ORC_SUV) blk[4] = der_uv(L.middle, p, q, L.u, L.v, R, L.spanU, L.spanV);
+        if (mask & ORC_SVV) blk[5] = der_vv(L.middle, p, q, L.u, L.v, R, L.spanV);
+        int o = 0;
+        for (int b = 0; b < 6; ++b) {
+            if (!((mask >> b) & 1u)) continue;
+            out[(3 * o + 0) * n + k] = blk[b].x;
+            out[(3 * o + 1) * n + k] = blk[b].y;
+            out[(3 * o + 2) * n + k] = blk[b].z;
+            ++o;
+        }
+    }
+}
+
+/* ---------------------------------------------------------------- stage c: the tree */
+
+#define GAP 8               /* GapPerEdge, src/kernel/kernel.cuh:17 */
+#define PTS (GAP + 1)       /* PointsPerEdge */
+
+static double max_abs3(d3 d) {   /* GetSecondDerivatives, kernel.cu:399 */
+    return fmax(fabs(d.x), fmax(fabs(d.y), fabs(d.z)));
+}
+
+static int need_divide(const orc_tree_node* n) {   /* NeedDivide, kernel.cu:859-878 */
+    double dx = n->rt[0] - n->lb[0], dy = n->rt[1] - n->lb[1], dz = n->rt[2] - n->lb[2], t;
+    if (dx > dy) { t = dx; dx = dy; dy = t; }
+    if (dx > dz) { t = dx; dx = dz; dz = t; }
+    if ((dx < 0.5 * dy) && (dx < 0.5 * dz)) return 0;
+    return 1;
+}
+
+/* One node of level grid g at block (bx,by): GetPoints (kernel.cu:404-431),
+ * GetSecondDerivatives (:375-402), the three block maxima (:707-733) and
+ * TightBoundingBox (:544-621). */
+static void build_node(const orc_surface* s, const double* M, unsigned g, unsigned bx, unsigned by,
+                       orc_tree_node* node, const orc_tree_node* parent) {
+    const int p = s->degree_u, q = s->degree_v;
+    double base_unit = 1.0 / g;
+    double unit = base_unit / GAP;
+    double base_u = base_unit * bx, base_v = base_unit * by;
+    double M1 = 0, M2 = 0, M3 = 0;
+    d3 mx = {0, 0, 0}, mn = {0, 0, 0};
+    for (int tx = 0; tx < PTS; ++tx)
+        for (int ty = 0; ty < PTS; ++ty) {
+            double p1 = base_u + tx * unit, p2 = base_v + ty * unit;
+            span_loc L = locate(s, M, p1, p2);
+            d4 R = R_of(L.middle, p, q, L.u, L.v);
+            double a = max_abs3(der_uu(L.middle, p, q, L.u, L.v, R, L.spanU));
+            double b = max_abs3(der_uv(L.middle, p, q, L.u, L.v, R, L.spanU, L.spanV));
+            double c = max_abs3(der_vv(L.middle, p, q, L.u, L.v, R, L.spanV));
+            d3 S = cart(R);
+            if (tx == 0 && ty == 0) {
+                M1 = a; M2 = b; M3 = c; mx = S; mn = S;
+            } else {
+                /* lhs < rhs ? rhs : lhs  (kernel.cu:725, 562-564) */
+                M1 = M1 < a ? a : M1;
+                M2 = M2 < b ? b : M2;
+                M3 = M3 < c ? c : M3;
+                mx.x = mx.x < S.x ? S.x : mx.x;
+                mx.y = mx.y < S.y ? S.y : mx.y;
+                mx.z = mx.z < S.z ? S.z : mx.z;
+                mn.x = mn.x > S.x ? S.x : mn.x;
+                mn.y = mn.y > S.y ? S.y : mn.y;
+                mn.z = mn.z > S.z ? S.z : mn.z;
+            }
+        }
+    /* K = (M1 + 2 M2 + M3) * sqrt(3) / (8 * GAP*g * GAP*g)   (kernel.cu:574, 601) */
+    unsigned den = 8u * GAP * g * GAP * g;
+    double K = (M1 + 2 * M2 + M3) * sqrt(3.0) / den;
+    node->rt[0] = mx.x + K; node->rt[1] = mx.y + K; node->rt[2] = mx.z + K;
+    node->lb[0] = mn.x - K; node->lb[1] = mn.y - K; node->lb[2] = mn.z - K;
+    double uunit = 1.0 / g;
+    node->uv_lb[0] = bx * uunit; node->uv_lb[1] = by * uunit;
+    node->uv_rt[0] = (bx + 1) * uunit; node->uv_rt[1] = (by + 1) * uunit;
+    if (parent) {   /* min/max(TreeNode) clip, kernel.cu:609-611, 885-901 */
+        for (int c = 0; c < 3; ++c) {
+            node->rt[c] = fmin(node->rt[c], parent->rt[c]);
+            node->lb[c] = fmax(node->lb[c], parent->lb[c]);
+        }
+    }
+}
+
+void orc_build_tree(const orc_surface* s, const double* M, orc_tree_node* tree, unsigned char* divided,
+                    unsigned char* built) {
+    memset(tree, 0, sizeof(orc_tree_node) * ORC_TREE_NODES);
+    memset(divided, 0, ORC_TREE_NODES);
+    memset(built, 0, ORC_TREE_NODES);
+    /* level 0: the root; its parent index (0-1)/64 truncates to 0 itself, so the clip is a
+     * no-op (kernel.cu:606-611) */
+    build_node(s, M, 1, 0, 0, &tree[0], NULL);
+    built[0] = 1;
+    divided[0] = (unsigned char)need_divide(&tree[0]);
+    if (!divided[0]) return;
+    /* level 1: 8x8 children, tree index 1 + bx*8 + by (kernel.cu:545-548) */
+    for (unsigned bx = 0; bx < GAP; ++bx)
+        for (unsigned by = 0; by < GAP; ++by) {
+            int t = 1 + (int)(bx * GAP + by);
+            build_node(s, M, GAP, bx, by, &tree[t], &tree[0]);
+            built[t] = 1;
+            divided[t] = (unsigned char)need_divide(&tree[t]);
+        }
+}
+
+int orc_candidates(const orc_tree_node* tree, const unsigned char* built, const double P[3], int* list) {
+    int n = 0;
+    for (int i = 0; i < ORC_TREE_NODES; ++i) {
+        if (!built[i]) continue;
+        const orc_tree_node* T = &tree[i];
+        if ((P[0] >= T->lb[0]) && (P[1] >= T->lb[1]) && (P[2] >= T->lb[2]) && (P[0] <= T->rt[0]) &&
+            (P[1] <= T->rt[1]) && (P[2] <= T->rt[2]))
+            list[n++] = i;
+    }
+    return n;
+}
+
+/* --------------------------------------------------------- stage d: Gauss-Newton */
+
+/* One reference GN update (kernel.cu:161-243).  Returns S at C in *Sout; writes step. */
+static void gn_step(const orc_surface* s, const double* M, const double C[2], const double P[3], d3* Sout,
+                    double step[2]) {
+    const int p = s->degree_u, q = s->degree_v;
+    span_loc L = locate(s, M, C[0], C[1]);
+    d4 R = R_of(L.middle, p, q, L.u, L.v);
+    d3 S = cart(R);
+    *Sout = S;
+    d3 du = der_u(L.middle, p, q, L.u, L.v, R, L.spanU);
+    d3 dv = der_v(L.middle, p, q, L.u, L.v, R, L.spanV);
+    double J[6] = {du.x, dv.x, du.y, dv.y, du.z, dv.z};
+    double JT[6];
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 2; j++) JT[j * 3 + i] = J[i * 2 + j];
+    double t[4];
+    mat_mult(JT, J, t, 2, 3, 2);
+    double det = t[0] * t[3] - t[1] * t[2];
+    double inv[4] = {t[3] / det, -t[1] / det, -t[2] / det, t[0] / det};
+    double IJ[6];
+    mat_mult(inv, JT, IJ, 2, 2, 3);
+    double dif[3] = {S.x - P[0], S.y - P[1], S.z - P[2]};
+    mat_mult(IJ, dif, step, 2, 3, 1);
+}
+
+static double dist3(d3 S, const double P[3]) {   /* norm(S-P), src/util/Matrix.cu:39-41 */
+    double x = S.x - P[0], y = S.y - P[1], z = S.z - P[2];
+    return sqrt(x * x + y * y + z * z);
+}
+
+static d3 surface_point(const orc_surface* s, const double* M, const double C[2]) {
+    span_loc L = locate(s, M, C[0], C[1]);
+    return cart(R_of(L.middle, s->degree_u, s->degree_v, L.u, L.v));
+}
+
+int orc_gauss_newton_shipped(const orc_surface* s, const double* M, const double seed[2], const double P[3],
+                             double max_edge, double uv[2]) {
+    double C[2] = {seed[0], seed[1]};
+    for (int i = 0; i < 10; i++) {
+        d3 S;
+        double step[2];
+        gn_step(s, M, C, P, &S, step);
+        if (dist3(S, P) < max_edge) {   /* kernel.cu:178 — tested before the step */
+            uv[0] = C[0];
+            uv[1] = C[1];
+            return 1;
+        }
+        C[0] = C[0] - step[0];
+        C[1] = C[1] - step[1];
+    }
+    return 0;
+}
+
+void orc_invert(const orc_surface* s, const double* M, const orc_tree_node* tree, const unsigned char* built,
+                const double* P, int64_t n, int max_iter, double* uv, int* status, double* residual, int* iters,
+                int threads) {
+    const double u0 = s->knots_u[s->degree_u], u1 = s->knots_u[s->cp_u];
+    const double v0 = s->knots_v[s->degree_v], v1 = s->knots_v[s->cp_v];
+#ifdef _OPENMP
+    if (threads <= 0) threads = omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 64) num_threads(threads)
+#endif
+    for (int64_t k = 0; k < n; ++k) {
+        const double* Pk = P + 3 * k;
+        int list[ORC_TREE_NODES];
+        int nc = orc_candidates(tree, built, Pk, list);
+        double best_uv[2] = {NAN, NAN}, best_r = INFINITY;
+        double sol_uv[ORC_TREE_NODES][2], sol_r[ORC_TREE_NODES];
+        int nsol = 0, total = 0;
+        for (int c = 0; c < nc; ++c) {
+            const orc_tree_node* T = &tree[list[c]];
+            /* seed = uv-centre of the node (kernel.cu:154) */
+            double C[2] = {(T->uv_lb[0] + T->uv_rt[0]) / 2, (T->uv_lb[1] + T->uv_rt[1]) / 2};
+            int converged = 0;
+            for (int it = 0; it < max_iter; ++it) {
+                d3 S;
+                double step[2];
+                gn_step(s, M, C, Pk, &S, step);
+                ++total;
+                if (!(isfinite(step[0]) && isfinite(step[1]))) break;
+                C[0] = C[0] - step[0];
+                C[1] = C[1] - step[1];
+                if (fabs(step[0]) < 1e-15 && fabs(step[1]) < 1e-15) { converged = 1; break; }
+                if (it == max_iter - 1 && fabs(step[0]) <= 1e-12 && fabs(step[1]) <= 1e-12) converged = 1;
+            }
+            if (!converged) continue;
+            if (!(C[0] >= u0 && C[0] <= u1 && C[1] >= v0 && C[1] <= v1)) continue;
+            double r = dist3(surface_point(s, M, C), Pk);
+            sol_uv[nsol][0] = C[0];
+            sol_uv[nsol][1] = C[1];
+            sol_r[nsol] = r;
+            ++nsol;
+            if (r < best_r) { best_r = r; best_uv[0] = C[0]; best_uv[1] = C[1]; }
+        }
+        int st;
+        if (nc == 0) st = ORC_NO_CANDIDATE;
+        else if (nsol == 0) st = ORC_NOT_CONVERGED;
+        else {
+            st = ORC_FOUND_UNIQUE;
+            for (int t = 0; t < nsol; ++t) {
+                int same = fabs(sol_uv[t][0] - best_uv[0]) <= 1e-7 && fabs(sol_uv[t][1] - best_uv[1]) <= 1e-7;
+                if (!same && sol_r[t] <= best_r * (1 + 1e-6) + 1e-12) st = ORC_FOUND_AMBIGUOUS;
+            }
+        }
+        uv[2 * k] = best_uv[0];
+        uv[2 * k + 1] = best_uv[1];
+        status[k] = st;
+        residual[k] = nsol ? best_r : NAN;
+        if (iters) iters[k] = total;
+    }
+}

@@ -1,0 +1,112 @@
+/*
+ * CPU ORACLE — test infrastructure only.
+ *
+ * A plain-C restatement of the reference's FP64 NURBS path (Qiang-Zou/GPU-NURBS):
+ * span-matrix conversion, point/derivative evaluation, the 2-level subdivision tree,
+ * candidate selection and Gauss-Newton inversion.  Each function cites the reference
+ * file:line it follows.  It is the checker for the CUDA library and the CPU baseline of
+ * the benchmark; it is never linked into, or called by, the product library.
+ *
+ * Parity of this restatement is pinned against the reference's own sources compiled for
+ * the host (oracle/_ref, built by oracle/Makefile from the reference tree) and against the
+ * reference's known-answer points; the fixtures produced that way live in tests/golden/.
+ *
+ * Build: gcc -O2 -ffp-contract=off (no FMA contraction, so rounding follows the source
+ * expression order exactly as the reference's unfused code does).
+ */
+#ifndef NURBS_ORACLE_H
+#define NURBS_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* A rational B-spline surface as the reference's .nu reader leaves it
+ * (src/main.cu:45-113): control points row-major over (u-index i, v-index j),
+ * index i*cp_v + j, xyz interleaved; weights not pre-multiplied. */
+typedef struct {
+    int degree_u, degree_v, cp_u, cp_v;
+    const double* knots_u;   /* degree_u + cp_u + 1 */
+    const double* knots_v;   /* degree_v + cp_v + 1 */
+    const double* cps;       /* 3 * cp_u * cp_v */
+    const double* weights;   /* cp_u * cp_v */
+} orc_surface;
+
+/* Tree node in the reference layout (src/kernel/kernel.cuh:30-39). */
+typedef struct {
+    double uv_lb[2], uv_rt[2];
+    double lb[3], rt[3];
+} orc_tree_node;
+
+#define ORC_TREE_NODES 65     /* root + 8x8 children: the reference's 2-level build */
+#define ORC_MAX_DEGREE 7      /* MAX_DEGREE 8 = k, so p <= 7 (src/NURBS/Evaluate.cuh:15) */
+
+/* Size in doubles of the reference MatrixN buffer (src/main.cu:182). */
+int64_t orc_matrix_n_size(const orc_surface* s);
+/* Offset of component c of span (i,j) in MatrixN (src/NURBS/Evaluate.cu:110-112). */
+int64_t orc_matrix_n_position(int i, int j, int degree_u, int degree_v, int cp_u, int cp_v, int c);
+/* findSpan (src/NURBS/Evaluate.cu:504-533). */
+int orc_find_span(int degree, int cp, const double* knots, double u);
+/* GetMatrixN (src/NURBS/Evaluate.cu:3-88) with the Nrc recursion (:90-108) memoised.
+ * Writes every non-empty span with i in [degree_u, cp_u-1], j in [degree_v, cp_v-1];
+ * other slots are left untouched.  Returns the number of spans written. */
+int orc_matrix_n(const orc_surface* s, double* matrix_n);
+
+/* Evaluation mask bits (output blocks, each 3 doubles per point). */
+#define ORC_S   1u
+#define ORC_SU  2u
+#define ORC_SV  4u
+#define ORC_SUU 8u
+#define ORC_SUV 16u
+#define ORC_SVV 32u
+/* Evaluates the blocks in mask at n (u,v) pairs (interleaved).  out is SoA:
+ * for each set bit b in ascending order, 3 planes x[n], y[n], z[n].
+ * Follows EvaluateRandom (src/NURBS/Evaluate.cu:1023-1038) for S and the old-style
+ * MatrixSurfaceDerivative{U,V,UU,UV,VV} (src/NURBS/Evaluate.cu:535-930) for derivatives. */
+void orc_eval(const orc_surface* s, const double* matrix_n, const double* uv, int64_t n,
+              unsigned mask, double* out, int threads);
+
+/* Homogeneous point R at local (u,v) in a span (MatrixSurfacePoint, Evaluate.cu:159-227). */
+void orc_point_r(const double* middle, int degree_u, int degree_v, double u, double v, double R[4]);
+
+/* The 2-level tree of the reference's inversion test (src/main.cu:280-309; kernels
+ * GetPoints, GetSecondDerivatives, Max_Sequential_Addressing_Shared, TightBoundingBox in
+ * src/kernel/kernel.cu).  divided[k] is meaningful for built nodes only; built[k] is 1
+ * for the root and, if divided[0], for nodes 1..64. */
+void orc_build_tree(const orc_surface* s, const double* matrix_n, orc_tree_node* tree,
+                    unsigned char* divided, unsigned char* built);
+
+/* Candidate list of query P: ascending built node indices whose closed AABB contains P
+ * (NewInverse loop, src/kernel/kernel.cu:456-457; NewBoundingBoxCheck :466-469).
+ * Returns the count; list must hold ORC_TREE_NODES ints. */
+int orc_candidates(const orc_tree_node* tree, const unsigned char* built, const double P[3], int* list);
+
+/* Inversion status codes (shared with the CUDA library). */
+#define ORC_FOUND_UNIQUE    0
+#define ORC_FOUND_AMBIGUOUS 1
+#define ORC_NO_CANDIDATE    2
+#define ORC_NOT_CONVERGED   3
+
+/* Converged Gauss-Newton inversion: the reference GN update (kernel.cu:151-249) run from
+ * the uv-centre of every candidate node until the step is below 1e-15 or max_iter
+ * iterations; results inside the knot domain are kept and the one of least distance is
+ * returned.  uv[2n], status[n], residual[n], iters[n] (total GN steps; may be NULL). */
+void orc_invert(const orc_surface* s, const double* matrix_n, const orc_tree_node* tree,
+                const unsigned char* built, const double* P, int64_t n, int max_iter,
+                double* uv, int* status, double* residual, int* iters, int threads);
+
+/* The reference's GaussNewton exactly as shipped (kernel.cu:151-249): <= 10 steps,
+ * success when |S-P| < max_edge before a step.  Returns 1 on success and writes uv. */
+int orc_gauss_newton_shipped(const orc_surface* s, const double* matrix_n, const double seed[2],
+                             const double P[3], double max_edge, double uv[2]);
+
+/* x*x*x rounded once (pow(x,3) of a correctly rounded libm), from an error-free
+ * product expansion.  Exposed for the tests that compare it with libm pow. */
+double orc_cube(double x);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,112 @@
+"""CPU tests: the C oracle against the golden fixtures made by the reference's own code.
+
+The fixtures (tests/golden/*.npz) were produced by the reference's FP64 functions compiled for
+the host (oracle/_ref, see tests/golden/make_golden.py).  These tests pin the oracle: span
+matrices, evaluation, tree and candidate lists must agree bit for bit.
+"""
+import math
+import os
+from fractions import Fraction
+
+import numpy as np
+import pytest
+
+import oracle as O
+from conftest import golden_files, load_golden, GOLDEN
+
+MODEL_FILES = [f for f in golden_files() if os.path.basename(f).startswith(("model_", "synth_"))]
+
+
+def surf_of(g):
+    return dict(p=g["p"], q=g["q"], nu=g["nu"], nv=g["nv"], knots_u=g["knots_u"], knots_v=g["knots_v"],
+                cps=g["cps"], weights=g["weights"])
+
+
+@pytest.mark.parametrize("path", MODEL_FILES, ids=lambda p: os.path.basename(p)[:-4])
+def test_matrix_n_bit_exact(path):
+    g = load_golden(path)
+    o = O.OracleSurface(surf_of(g))
+    assert np.array_equal(o.matrix_n.view(np.int64), g["matrix_n"].view(np.int64))
+
+
+@pytest.mark.parametrize("path", MODEL_FILES, ids=lambda p: os.path.basename(p)[:-4])
+def test_eval_bit_exact(path):
+    g = load_golden(path)
+    o = O.OracleSurface(surf_of(g))
+    ev = o.eval(g["uv"], 63)
+    assert np.array_equal(ev, g["eval"], equal_nan=True)
+
+
+@pytest.mark.parametrize("path", MODEL_FILES, ids=lambda p: os.path.basename(p)[:-4])
+def test_tree_and_candidates_exact(path):
+    g = load_golden(path)
+    o = O.OracleSurface(surf_of(g))
+    tree, div, built = o.tree()
+    assert np.array_equal(built, g["built"])
+    b = built == 1
+    assert np.array_equal(tree[b], g["tree"][b], equal_nan=True)
+    assert np.array_equal(div[b], g["divided"][b])
+    cands = o.candidates(g["P"])
+    counts = np.array([len(c) for c in cands], np.int32)
+    assert np.array_equal(counts, g["cand_counts"])
+    flat = np.concatenate(cands) if len(cands) else np.zeros(0, np.int32)
+    assert np.array_equal(flat, g["cand_flat"])
+
+
+@pytest.mark.parametrize("path", MODEL_FILES, ids=lambda p: os.path.basename(p)[:-4])
+def test_shipped_gauss_newton_exact(path):
+    g = load_golden(path)
+    o = O.OracleSurface(surf_of(g))
+    tree, _, built = o.tree()
+    for k, me, ok, u, v in g["gn_shipped"]:
+        node = tree[0] if built[0] else np.array([0, 0, 1, 1.0])
+        seed = np.array([(node[0] + node[2]) / 2, (node[1] + node[3]) / 2])
+        got_ok, uv = o.gauss_newton_shipped(seed, g["P"][int(k)], me)
+        assert got_ok == bool(ok)
+        if got_ok:
+            assert uv[0] == u and uv[1] == v
+
+
+def test_known_answer_points():
+    """S(0.25,0.25) of center_bk / test_face2 as hard-coded in src/kernel/kernel.cu:452-454."""
+    kat = np.load(os.path.join(GOLDEN, "kat.npz"))
+    for name in ("center_bk", "test_face2"):
+        g = load_golden(os.path.join(GOLDEN, f"model_{name}.npz"))
+        S = O.OracleSurface(surf_of(g)).eval(np.array([[0.25, 0.25]]), 1).ravel()
+        assert np.array_equal(S, kat[name])
+        # the reference prints 6 decimals
+        assert np.allclose(S, kat[f"{name}_ref"], atol=5e-7)
+
+
+def test_cube_is_correctly_rounded():
+    """The oracle's pow(h,3) is the once-rounded cube; check against exact rationals."""
+    rng = np.random.default_rng(3)
+    xs = np.concatenate([rng.random(3000) * 10 - 5, rng.random(1000) * 1e-3, [0.5, 1.0, 2.0, 3.0, 1.1]])
+    for x in xs:
+        x = float(x)
+        assert O.lib().orc_cube(x) == float(Fraction(x) ** 3)
+
+
+def test_find_span_semantics():
+    """findSpan (src/NURBS/Evaluate.cu:504-533): clamping and repeated interior knots."""
+    k = np.array([0, 0, 0, 0.25, 0.25, 0.5, 0.5, 0.75, 0.75, 1, 1, 1], np.float64)
+    f = lambda u: O.lib().orc_find_span(2, 9, k, u)
+    assert f(-1.0) == 2 and f(0.0) == 2
+    assert f(0.25) == 4 and f(0.2499) == 2
+    assert f(1.0) == 8 and f(2.0) == 8
+    assert f(0.75) == 8
+
+
+def test_oracle_inversion_small_recovers_truth():
+    """On the small bicubic surface the converged GN oracle recovers the generating (u,v)."""
+    from gpu_nurbs_gb300 import synth
+    surf = synth.surface_small()
+    o = O.OracleSurface(surf)
+    uv, off = synth.query_params(300, 11, "small")
+    E = o.eval(uv, 7)
+    P = synth.form_queries(E[0:3].T, E[3:6].T, E[6:9].T, off)
+    ruv, st, res, _ = o.invert(P)
+    ok = st == O.FOUND_UNIQUE
+    assert ok.mean() > 0.95
+    assert np.abs(ruv[ok] - uv[ok]).max() < 1e-12
+    assert np.allclose(res[ok], np.abs(off[ok]), rtol=1e-6, atol=1e-12)
