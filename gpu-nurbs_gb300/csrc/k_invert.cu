@@ -103,36 +103,37 @@ __device__ Sol phase64(const SurfDev& s, double px, double py, double pz, double
   Sol o = {u, v, 0.0, false};
   bool newton = (MODE == kModeMixed);
   const int maxit = MODE == kModeMixed ? kMaxFinal64 : kMaxIter64;
+  bool converged = false;
   for (int it = 0; it < maxit; ++it) {
     double du, dv;
-    double rr;
     if (MODE == kModeMixed) {
       fast::SDer<double> d = fast::eval_point<double, P, Q, 1>(s, u, v);
       fast::SDer<float> c = fast::eval_point<float, P, Q, 2>(s, (float)u, (float)v);
       v3<double> r = {d.S.x - px, d.S.y - py, d.S.z - pz};
-      rr = sqrt(dot3(r, r));
       if (!solve_step<double, float>(r, d.Su, d.Sv, c.Suu, c.Suv, c.Svv, true, du, dv)) return o;
     } else {
       fast::SDer<double> d = fast::eval_point<double, P, Q, 2>(s, u, v);
       v3<double> r = {d.S.x - px, d.S.y - py, d.S.z - pz};
-      rr = sqrt(dot3(r, r));
       if (!solve_step<double, double>(r, d.Su, d.Sv, d.Suu, d.Suv, d.Svv, newton, du, dv)) return o;
     }
     if (!(isfinite(du) && isfinite(dv))) return o;
     u -= du;
     v -= dv;
     double step = fmax(fabs(du), fabs(dv));
-    // the residual is the one of the last FP64 evaluation, |S(C) - P|; C then moves by the
-    // final (converged) step, which changes the distance only to second order
-    o.u = u;
-    o.v = v;
-    o.r = rr;
     if ((newton && step <= kTolNewton64) || step <= kTolAny64) {
-      o.ok = (u >= s.dom_u0 && u <= s.dom_u1 && v >= s.dom_v0 && v <= s.dom_v1);
-      return o;
+      converged = true;
+      break;
     }
     if (MODE != kModeMixed) newton = step < kNewtonSwitch64;
   }
+  if (!converged) return o;
+  // residual check in FP64 at the returned point: |S(C) - P|
+  fast::SDer<double> d = fast::eval_point<double, P, Q, 0>(s, u, v);
+  v3<double> r = {d.S.x - px, d.S.y - py, d.S.z - pz};
+  o.u = u;
+  o.v = v;
+  o.r = sqrt(dot3(r, r));
+  o.ok = (u >= s.dom_u0 && u <= s.dom_u1 && v >= s.dom_v0 && v <= s.dom_v1) && isfinite(o.r);
   return o;
 }
 

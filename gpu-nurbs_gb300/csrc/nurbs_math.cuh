@@ -242,7 +242,8 @@ template <typename T, int D>
 struct Horner {
   v4<T> p, dp, ddp;
   int k;
-  GN_HD Horner() : k(0) {}
+  // dp/ddp start at zero: a polynomial of degree < D has vanishing higher derivatives
+  GN_HD Horner() : dp{T(0), T(0), T(0), T(0)}, ddp{T(0), T(0), T(0), T(0)}, k(0) {}
   GN_HD void push(const v4<T>& c, T x) {
     if (k == 0) {
       p = c;

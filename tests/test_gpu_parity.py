@@ -128,8 +128,8 @@ def test_invert_small_parity(nurbs, cuda, precision):
     ouv, ost, ores, _ = o.invert(P)
     s = nurbs.Surface(surf)
     uv, st, res = (x.cpu().numpy() for x in s.invert(T(P, cuda), precision))
-    c = classify_inversion(uv, st, res, ouv, ost, ores)
-    print(c)
+    c = classify_inversion(uv, st, res, ouv, ost, ores, P)
+    print("small", precision, {k: v for k, v in c.items() if k != "fail_idx"})
     assert c["fail_unique"] == 0 and c["fail_ambiguous"] == 0 and c["fail_no_candidate"] == 0, c
     assert c["same"] >= 0.95 * c["unique"]
     ok = st == 0
@@ -144,8 +144,8 @@ def test_invert_large_parity(nurbs, cuda, precision):
     ouv, ost, ores, _ = o.invert(P)
     s = nurbs.Surface(surf)
     uv, st, res = (x.cpu().numpy() for x in s.invert(T(P, cuda), precision))
-    c = classify_inversion(uv, st, res, ouv, ost, ores)
-    print(c)
+    c = classify_inversion(uv, st, res, ouv, ost, ores, P)
+    print("large", precision, {k: v for k, v in c.items() if k != "fail_idx"})
     assert c["fail_no_candidate"] == 0
     assert c["fail_unique"] + c["fail_ambiguous"] <= 0.01 * c["n"], c
 
@@ -160,9 +160,12 @@ def test_invert_models_parity(nurbs, cuda, path):
     s = nurbs.Surface(surf)
     for precision in (0, 1):
         uv, st, res = (x.cpu().numpy() for x in s.invert(T(P, cuda), precision))
-        c = classify_inversion(uv, st, res, ouv, ost, ores)
+        c = classify_inversion(uv, st, res, ouv, ost, ores, P)
+        print(os.path.basename(path), precision, {k: v for k, v in c.items() if k != "fail_idx"})
+        for k in c["fail_idx"][:4]:
+            print("  fail", k, P[k], "gpu", uv[k], st[k], res[k], "oracle", ouv[k], ost[k], ores[k])
         assert c["fail_no_candidate"] == 0, c
-        assert c["fail_unique"] + c["fail_ambiguous"] <= 1, c
+        assert c["fail_unique"] + c["fail_ambiguous"] == 0, c
 
 
 def test_invert_host_matches_device(nurbs, cuda):
@@ -185,8 +188,11 @@ def test_eval_f32_close(nurbs, cuda):
     s = nurbs.Surface(surf)
     ev = s.eval_f32(T(uv, cuda, torch.float32), 63).cpu().numpy().astype(np.float64)
     errs = eval_errors(ev, ref)
-    assert max(errs[:3]) < 1e-5, errs
-    assert max(errs) < 2e-3, errs
+    # FP32 contraction of FP32-rounded span matrices: ~1e-6 on points, derivatives lose a
+    # further factor to cancellation in the power basis
+    assert errs[0] < 1e-5, errs
+    assert max(errs[1:3]) < 2e-4, errs
+    assert max(errs[3:]) < 5e-3, errs
 
 
 def test_invalid_arguments_return_status(nurbs, cuda):
