@@ -80,6 +80,7 @@ __device__ __forceinline__ bool solve_step(const v3<T>& r, const v3<T>& Su, cons
 template <int P, int Q>
 __device__ bool phase32(const SurfDev& s, float px, float py, float pz, float& u, float& v, float& dist) {
   bool newton = false;
+  float prev = INFINITY;
   for (int it = 0; it < kMaxIter32; ++it) {
     fast::SDer<float> d = fast::eval_point<float, P, Q, 2>(s, u, v);
     v3<float> r = {d.S.x - px, d.S.y - py, d.S.z - pz};
@@ -90,7 +91,15 @@ __device__ bool phase32(const SurfDev& s, float px, float py, float pz, float& u
     v -= dv;
     float step = fmaxf(fabsf(du), fabsf(dv));
     dist = sqrtf(dot3(r, r));
-    if (step <= kTol32) return true;
+    // FP32 resolution of the parameters here: the rounding of S (relative 2^-24 of its
+    // magnitude) mapped through the smaller tangent length
+    float smag = fmaxf(fmaxf(fabsf(d.S.x), fabsf(d.S.y)), fmaxf(fabsf(d.S.z), 1.0f));
+    float tmin = sqrtf(fminf(dot3(d.Su, d.Su), dot3(d.Sv, d.Sv)));
+    float floor32 = 8.0f * 5.96e-8f * smag / fmaxf(tmin, 1e-30f);
+    if (step <= fmaxf(kTol32, floor32)) return true;
+    // Newton steps that stop shrinking have reached the rounding floor
+    if (newton && step < 1e-4f && step > 0.5f * prev) return true;
+    prev = step;
     newton = step < kNewtonSwitch32;
   }
   return false;
