@@ -68,6 +68,7 @@ SIGNATURES = {
     "nurbs_matrix_n_position": (_i64, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]),
     "nurbs_get_matrix_n": (C.c_int, [_vp, _vp, _vp]),
     "nurbs_get_matrix_n_raw": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int, _vp, _vp, _vp, _vp, _vp]),
+    "nurbs_get_matrix_n_noalloc": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int, _vp, _vp, _vp, _vp, _vp]),
     "nurbs_eval": (C.c_int, [_vp, _vp, _i64, C.c_uint, _vp, C.c_int, _vp]),
     "nurbs_eval_f32": (C.c_int, [_vp, _vp, _i64, C.c_uint, _vp, _vp]),
     "nurbs_evaluate_random": (C.c_int, [_vp, _vp, _i64, _vp, C.c_int, C.c_int, C.c_int, C.c_int, _vp, _vp, _vp]),

@@ -120,6 +120,25 @@ int nurbs_get_matrix_n_raw(double* matrix_n_dev, int degree_u, int degree_v, int
                            const double* knots_u_dev, const double* knots_v_dev,
                            const double* control_points_dev, const double* weights_dev, void* stream);
 
+/* GetMatrixN into a caller buffer that allocates nothing.  No counterpart in the reference:
+ * it is for callers that cannot allocate device memory when they convert a surface — code
+ * running under a device allocator it does not own (an application's caching allocator, a
+ * budget admitter that forbids allocations outside its pool) or a real-time / serving loop
+ * that must not enter the allocator between requests.  Same arguments and bit-identical
+ * output as nurbs_get_matrix_n_raw; its scratch (span tables and basis matrices) is a
+ * file-scope device array of NURBS_NOALLOC_SCRATCH_BYTES held by every GPU that loads the
+ * library until the process exits.  Surfaces whose worst-case scratch
+ * (cp_u-degree_u + cp_v-degree_v) * 4 + (cp_u-degree_u)*(degree_u+1)^2*8 +
+ * (cp_v-degree_v)*(degree_v+1)^2*8 bytes (plus alignment) exceeds it return
+ * NURBS_E_UNSUPPORTED.  The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress, with that device current); make that first call before any stream
+ * capture.  All calls share the array, so calls that overlap on the GPU race: serialise them.
+ * Synchronises `stream` once (to read the span counts back). */
+#define NURBS_NOALLOC_SCRATCH_BYTES (1u << 20)
+int nurbs_get_matrix_n_noalloc(double* matrix_n_dev, int degree_u, int degree_v, int cp_u, int cp_v,
+                               const double* knots_u_dev, const double* knots_v_dev,
+                               const double* control_points_dev, const double* weights_dev, void* stream);
+
 /* -------------------------------------------------------------- stage b: evaluation */
 /* Batched evaluation at n parameter pairs uv_dev[2n] (global parameters).  out_dev is SoA:
  * for each set bit of mask, in the order S,Su,Sv,Suu,Suv,Svv, three planes of n doubles.
