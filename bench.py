@@ -192,10 +192,9 @@ def run_ours(a):
     barrier()
     t_mixed = timed(inv_mixed, a.steps)
     barrier()
+    t_fp64 = timed(inv_fp64, max(3, a.steps // 4))
+    barrier()
     clk = clocks.stop()
-    barrier()
-    t_fp64 = timed(inv_fp64, max(3, a.steps // 2))
-    barrier()
     # e2e through the C-ABI with host buffers
     for _ in range(2):
         inv_host()
@@ -320,7 +319,7 @@ def run_reference(a):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="large", choices=["large", "small", "quintic"])
