@@ -8,17 +8,28 @@
 //      reference's Gauss-Newton update  C <- C - (J^T J)^-1 J^T (S(C) - P)  (kernel.cu:195-243)
 //      until the step is small, then with Newton steps (Hessian J^T J + sum r_k d2S_k) whose
 //      fixed point is the same stationary point but which converge quadratically;
-//   3. results inside the knot domain are kept; the closest wins (ties: first in node order).
+//   3. results inside the knot domain are kept; the closest wins.
+//
+// Work distribution.  A query has anywhere from 0 to 65 candidate seeds and a seed needs from
+// 2 to 24 iterations, so one thread per query leaves most lanes of a warp idle.  Each warp
+// owns 32 queries, flattens their (query, seed) pairs into a task list (warp prefix sum over
+// the candidate counts) and every lane pulls the next task as soon as its seed converges or
+// fails, so all 32 lanes iterate until the warp's list is exhausted.  Finished seeds are merged
+// into per-query records in shared memory, one lane at a time.  A seed whose iterate (in the
+// Newton regime) arrives within 1e-3 of a minimum its query has already found stops there:
+// it would converge to that minimum.
 //
 // Precision schedules (template MODE):
 //   FP64  — every evaluation, solve and update in FP64.
-//   MIXED — phase 1 for every candidate in FP32 (FP32 span matrices, FP32 breakpoints); the
-//           best candidate (plus a second one when it is nearly as close) then takes the final
-//           two Newton steps in FP64: S, Su, Sv and the gradient J^T r in FP64, the Hessian's
-//           curvature term from FP32 second derivatives (it only sets the convergence rate),
-//           the 2x2 solve and the residual |S - P| in FP64.  Extra FP64 steps (at most 4) run
+//   MIXED — the seed exploration in FP32 (FP32 span matrices, FP32 breakpoints); the best
+//           minimum (plus a runner-up within 0.1 %) then takes the final two Newton steps in
+//           FP64: S, Su, Sv and the gradient J^T r in FP64, the Hessian's curvature term from
+//           FP32 second derivatives (it only sets the convergence rate), the 2x2 solve and the
+//           residual |S - P| at the returned point in FP64.  Extra FP64 steps (at most 4) run
 //           only when the second step is not yet below tolerance (near-singular or boundary
-//           cases).  FP64 work per query is thus ~2 evaluations instead of ~20.
+//           cases).
+#include <type_traits>
+
 #include "nurbs_internal.h"
 #include "nurbs_math.cuh"
 
@@ -29,21 +40,19 @@ namespace {
 constexpr int kModeFP64 = 0;
 constexpr int kModeMixed = 1;
 
-constexpr int kMaxIter32 = 24;     // FP32 phase iterations per candidate
-constexpr int kMaxIter64 = 40;     // FP64-mode iterations per candidate
+constexpr int kWarps = 4;          // warps per CTA
+constexpr int kThreads = 32 * kWarps;
+constexpr int kMaxIter32 = 24;     // FP32 iterations per seed
+constexpr int kMaxIter64 = 40;     // FP64-mode iterations per seed
 constexpr int kMaxFinal64 = 6;     // MIXED: FP64 steps (2 normally)
-constexpr float kNewtonSwitch32 = 1e-3f;
-constexpr double kNewtonSwitch64 = 1e-3;
-constexpr float kTol32 = 3e-7f;    // FP32 phase: stop when the step is at FP32 resolution
+constexpr double kNewtonSwitch = 1e-3;
+constexpr float kTol32 = 3e-7f;
 constexpr double kTolNewton64 = 1e-10;  // a Newton step this small leaves < 1e-19 error
 constexpr double kTolAny64 = 1e-14;
-constexpr double kDistinct = 1e-7;      // two solutions are the same minimum within this (uv)
-constexpr float kDistinct32 = 1e-4f;
-
-struct Sol {
-  double u, v, r;
-  bool ok;
-};
+constexpr double kDistinct = 1e-7;      // two FP64 solutions are the same minimum within this
+constexpr float kDistinct32 = 1e-4f;    // ... two FP32 solutions
+constexpr float kJoin = 1e-3f;          // a Newton iterate this close to a known minimum joins it
+constexpr int kSols = 4;                // FP64 mode: distinct minima kept per query
 
 template <typename T>
 __device__ __forceinline__ T dot3(const v3<T>& a, const v3<T>& b) {
@@ -58,10 +67,9 @@ __device__ __forceinline__ bool solve_step(const v3<T>& r, const v3<T>& Su, cons
   T a00 = dot3(Su, Su), a01 = dot3(Su, Sv), a11 = dot3(Sv, Sv);
   T g0 = dot3(Su, r), g1 = dot3(Sv, r);
   if (newton) {
-    v3<T> rr = r;
-    T h00 = a00 + (T)(rr.x * (T)Suu.x + rr.y * (T)Suu.y + rr.z * (T)Suu.z);
-    T h01 = a01 + (T)(rr.x * (T)Suv.x + rr.y * (T)Suv.y + rr.z * (T)Suv.z);
-    T h11 = a11 + (T)(rr.x * (T)Svv.x + rr.y * (T)Svv.y + rr.z * (T)Svv.z);
+    T h00 = a00 + (T)(r.x * (T)Suu.x + r.y * (T)Suu.y + r.z * (T)Suu.z);
+    T h01 = a01 + (T)(r.x * (T)Suv.x + r.y * (T)Suv.y + r.z * (T)Suv.z);
+    T h11 = a11 + (T)(r.x * (T)Svv.x + r.y * (T)Svv.y + r.z * (T)Svv.z);
     T det = h00 * h11 - h01 * h01;
     if (h00 > T(0) && det > T(0)) {
       du = (h11 * g0 - h01 * g1) / det;
@@ -76,127 +84,152 @@ __device__ __forceinline__ bool solve_step(const v3<T>& r, const v3<T>& Su, cons
   return true;
 }
 
-// FP32 phase from seed (u,v).  On success returns the iterate and its distance.
+// Per-seed iteration state.
+template <typename T>
+struct Seed {
+  T u, v, prev;
+  int it;
+  bool newton;
+};
+
+enum StepResult { kContinue = 0, kConverged = 1, kFailed = 2 };
+
+// One FP32 iteration of a seed.  Convergence: the step is at the FP32 resolution of the
+// parameters (rounding of S mapped through the shorter tangent), or Newton steps stop shrinking.
 template <int P, int Q>
-__device__ bool phase32(const SurfDev& s, float px, float py, float pz, float& u, float& v, float& dist) {
-  bool newton = false;
-  float prev = INFINITY;
-  for (int it = 0; it < kMaxIter32; ++it) {
-    fast::SDer<float> d = fast::eval_point<float, P, Q, 2>(s, u, v);
-    v3<float> r = {d.S.x - px, d.S.y - py, d.S.z - pz};
-    float du, dv;
-    if (!solve_step<float, float>(r, d.Su, d.Sv, d.Suu, d.Suv, d.Svv, newton, du, dv)) return false;
+__device__ __forceinline__ int iterate32(const SurfDev& s, float px, float py, float pz, Seed<float>& st,
+                                         float& dist) {
+  fast::SDer<float> d = fast::eval_point<float, P, Q, 2>(s, st.u, st.v);
+  v3<float> r = {d.S.x - px, d.S.y - py, d.S.z - pz};
+  float du, dv;
+  if (!solve_step<float, float>(r, d.Su, d.Sv, d.Suu, d.Suv, d.Svv, st.newton, du, dv)) return kFailed;
+  if (!(isfinite(du) && isfinite(dv))) return kFailed;
+  st.u -= du;
+  st.v -= dv;
+  float step = fmaxf(fabsf(du), fabsf(dv));
+  dist = sqrtf(dot3(r, r));
+  float smag = fmaxf(fmaxf(fabsf(d.S.x), fabsf(d.S.y)), fmaxf(fabsf(d.S.z), 1.0f));
+  float tmin = sqrtf(fminf(dot3(d.Su, d.Su), dot3(d.Sv, d.Sv)));
+  float floor32 = 8.0f * 5.96e-8f * smag / fmaxf(tmin, 1e-30f);
+  if (step <= fmaxf(kTol32, floor32)) return kConverged;
+  if (st.newton && step < 1e-4f && step > 0.5f * st.prev) return kConverged;
+  st.prev = step;
+  st.newton = step < (float)kNewtonSwitch;
+  if (++st.it >= kMaxIter32) return kFailed;
+  return kContinue;
+}
+
+// One FP64 iteration of a seed (FP64 mode).
+template <int P, int Q>
+__device__ __forceinline__ int iterate64(const SurfDev& s, double px, double py, double pz, Seed<double>& st) {
+  fast::SDer<double> d = fast::eval_point<double, P, Q, 2>(s, st.u, st.v);
+  v3<double> r = {d.S.x - px, d.S.y - py, d.S.z - pz};
+  double du, dv;
+  if (!solve_step<double, double>(r, d.Su, d.Sv, d.Suu, d.Suv, d.Svv, st.newton, du, dv)) return kFailed;
+  if (!(isfinite(du) && isfinite(dv))) return kFailed;
+  st.u -= du;
+  st.v -= dv;
+  double step = fmax(fabs(du), fabs(dv));
+  if ((st.newton && step <= kTolNewton64) || step <= kTolAny64) return kConverged;
+  st.prev = step;
+  st.newton = step < kNewtonSwitch;
+  if (++st.it >= kMaxIter64) return kFailed;
+  return kContinue;
+}
+
+// FP64 residual at (u,v), with the domain test.
+template <int P, int Q>
+__device__ __forceinline__ bool finish64(const SurfDev& s, double px, double py, double pz, double u, double v,
+                                         double& res) {
+  fast::SDer<double> d = fast::eval_point<double, P, Q, 0>(s, u, v);
+  v3<double> r = {d.S.x - px, d.S.y - py, d.S.z - pz};
+  res = sqrt(dot3(r, r));
+  return (u >= s.dom_u0 && u <= s.dom_u1 && v >= s.dom_v0 && v <= s.dom_v1) && isfinite(res);
+}
+
+// MIXED: the final FP64 Newton steps from an FP32 minimum, then the residual.
+template <int P, int Q>
+__device__ bool final64(const SurfDev& s, double px, double py, double pz, double& u, double& v, double& res) {
+  for (int it = 0; it < kMaxFinal64; ++it) {
+    fast::SDer<double> d = fast::eval_point<double, P, Q, 1>(s, u, v);
+    fast::SDer<float> c = fast::eval_point<float, P, Q, 2>(s, (float)u, (float)v);
+    v3<double> r = {d.S.x - px, d.S.y - py, d.S.z - pz};
+    double du, dv;
+    if (!solve_step<double, float>(r, d.Su, d.Sv, c.Suu, c.Suv, c.Svv, true, du, dv)) return false;
     if (!(isfinite(du) && isfinite(dv))) return false;
     u -= du;
     v -= dv;
-    float step = fmaxf(fabsf(du), fabsf(dv));
-    dist = sqrtf(dot3(r, r));
-    // FP32 resolution of the parameters here: the rounding of S (relative 2^-24 of its
-    // magnitude) mapped through the smaller tangent length
-    float smag = fmaxf(fmaxf(fabsf(d.S.x), fabsf(d.S.y)), fmaxf(fabsf(d.S.z), 1.0f));
-    float tmin = sqrtf(fminf(dot3(d.Su, d.Su), dot3(d.Sv, d.Sv)));
-    float floor32 = 8.0f * 5.96e-8f * smag / fmaxf(tmin, 1e-30f);
-    if (step <= fmaxf(kTol32, floor32)) return true;
-    // Newton steps that stop shrinking have reached the rounding floor
-    if (newton && step < 1e-4f && step > 0.5f * prev) return true;
-    prev = step;
-    newton = step < kNewtonSwitch32;
+    if (fmax(fabs(du), fabs(dv)) <= kTolNewton64) return finish64<P, Q>(s, px, py, pz, u, v, res);
   }
   return false;
 }
 
-// FP64 iterations from (u,v).  MIXED: curvature from FP32 second derivatives and at most
-// kMaxFinal64 steps; FP64: full FP64 with the GN -> Newton switch.
-template <int P, int Q, int MODE>
-__device__ Sol phase64(const SurfDev& s, double px, double py, double pz, double u, double v) {
-  Sol o = {u, v, 0.0, false};
-  bool newton = (MODE == kModeMixed);
-  const int maxit = MODE == kModeMixed ? kMaxFinal64 : kMaxIter64;
-  bool converged = false;
-  for (int it = 0; it < maxit; ++it) {
-    double du, dv;
-    if (MODE == kModeMixed) {
-      fast::SDer<double> d = fast::eval_point<double, P, Q, 1>(s, u, v);
-      fast::SDer<float> c = fast::eval_point<float, P, Q, 2>(s, (float)u, (float)v);
-      v3<double> r = {d.S.x - px, d.S.y - py, d.S.z - pz};
-      if (!solve_step<double, float>(r, d.Su, d.Sv, c.Suu, c.Suv, c.Svv, true, du, dv)) return o;
-    } else {
-      fast::SDer<double> d = fast::eval_point<double, P, Q, 2>(s, u, v);
-      v3<double> r = {d.S.x - px, d.S.y - py, d.S.z - pz};
-      if (!solve_step<double, double>(r, d.Su, d.Sv, d.Suu, d.Suv, d.Svv, newton, du, dv)) return o;
-    }
-    if (!(isfinite(du) && isfinite(dv))) return o;
-    u -= du;
-    v -= dv;
-    double step = fmax(fabs(du), fabs(dv));
-    if ((newton && step <= kTolNewton64) || step <= kTolAny64) {
-      converged = true;
-      break;
-    }
-    if (MODE != kModeMixed) newton = step < kNewtonSwitch64;
-  }
-  if (!converged) return o;
-  // residual check in FP64 at the returned point: |S(C) - P|
-  fast::SDer<double> d = fast::eval_point<double, P, Q, 0>(s, u, v);
-  v3<double> r = {d.S.x - px, d.S.y - py, d.S.z - pz};
-  o.u = u;
-  o.v = v;
-  o.r = sqrt(dot3(r, r));
-  o.ok = (u >= s.dom_u0 && u <= s.dom_u1 && v >= s.dom_v0 && v <= s.dom_v1) && isfinite(o.r);
-  return o;
-}
-
-struct Best {
-  Sol sol[4];
+struct Rec32 {  // per-query FP32 record: best and best distinct runner-up
+  float u1, v1, d1, u2, v2, d2;
+};
+struct Rec64 {  // per-query FP64 record: distinct minima
+  double u[kSols], v[kSols], r[kSols];
   int n;
 };
 
-__device__ __forceinline__ void add_solution(Best& b, const Sol& s) {
-  // merge with an existing copy of the same minimum (keep the closer estimate)
-  for (int k = 0; k < b.n; ++k) {
-    if (fabs(b.sol[k].u - s.u) <= kDistinct && fabs(b.sol[k].v - s.v) <= kDistinct) {
-      if (s.r < b.sol[k].r) b.sol[k] = s;
-      return;
-    }
+__device__ __forceinline__ void merge32(Rec32& R, float u, float v, float d) {
+  bool same1 = R.d1 < INFINITY && fabsf(u - R.u1) <= kDistinct32 && fabsf(v - R.v1) <= kDistinct32;
+  if (same1) {
+    if (d < R.d1) { R.u1 = u; R.v1 = v; R.d1 = d; }
+  } else if (d < R.d1) {
+    R.u2 = R.u1; R.v2 = R.v1; R.d2 = R.d1;
+    R.u1 = u; R.v1 = v; R.d1 = d;
+  } else if (d < R.d2) {
+    R.u2 = u; R.v2 = v; R.d2 = d;
   }
-  if (b.n < 4) {
-    b.sol[b.n++] = s;
-    return;
-  }
-  int worst = 0;
-  for (int k = 1; k < 4; ++k)
-    if (b.sol[k].r > b.sol[worst].r) worst = k;
-  if (s.r < b.sol[worst].r) b.sol[worst] = s;
 }
 
-// best solution and status (FOUND / AMBIGUOUS), as the oracle decides it
-__device__ __forceinline__ int finish(const Best& b, double& u, double& v, double& r) {
-  int bi = 0;
-  for (int k = 1; k < b.n; ++k)
-    if (b.sol[k].r < b.sol[bi].r) bi = k;
-  u = b.sol[bi].u;
-  v = b.sol[bi].v;
-  r = b.sol[bi].r;
-  for (int k = 0; k < b.n; ++k) {
-    if (k == bi) continue;
-    if (b.sol[k].r <= r * (1 + 1e-6) + 1e-12) return 1;  // NURBS_INV_AMBIGUOUS
+__device__ __forceinline__ void merge64(Rec64& R, double u, double v, double r) {
+  for (int k = 0; k < R.n; ++k)
+    if (fabs(R.u[k] - u) <= kDistinct && fabs(R.v[k] - v) <= kDistinct) {
+      if (r < R.r[k]) { R.u[k] = u; R.v[k] = v; R.r[k] = r; }
+      return;
+    }
+  int slot = R.n;
+  if (R.n >= kSols) {
+    slot = 0;
+    for (int k = 1; k < kSols; ++k)
+      if (R.r[k] > R.r[slot]) slot = k;
+    if (!(r < R.r[slot])) return;
+  } else {
+    ++R.n;
   }
+  R.u[slot] = u; R.v[slot] = v; R.r[slot] = r;
+}
+
+// best minimum and status (FOUND / AMBIGUOUS), as the oracle decides them
+__device__ __forceinline__ int finish_status(const double* us, const double* vs, const double* rs, int n, double& u,
+                                             double& v, double& r) {
+  int bi = 0;
+  for (int k = 1; k < n; ++k)
+    if (rs[k] < rs[bi]) bi = k;
+  u = us[bi];
+  v = vs[bi];
+  r = rs[bi];
+  for (int k = 0; k < n; ++k)
+    if (k != bi && rs[k] <= r * (1 + 1e-6) + 1e-12) return 1;  // NURBS_INV_AMBIGUOUS
   return 0;
 }
 
-__device__ __forceinline__ float round_down_f(double x) { return __double2float_rd(x); }
-__device__ __forceinline__ float round_up_f(double x) { return __double2float_ru(x); }
-
 template <int P, int Q, int MODE>
-__global__ void __launch_bounds__(128) k_invert(SurfDev s, const double* __restrict__ Pq, int64_t n,
-                                                double* __restrict__ uv_out, int* __restrict__ st_out,
-                                                double* __restrict__ res_out) {
+__global__ void __launch_bounds__(kThreads) k_invert(SurfDev s, const double* __restrict__ Pq, int64_t n,
+                                                     double* __restrict__ uv_out, int* __restrict__ st_out,
+                                                     double* __restrict__ res_out) {
   __shared__ float box32[kTreeNodes][6];
   __shared__ double box64[kTreeNodes][6];
   __shared__ double ctr[kTreeNodes][2];
   __shared__ float ctr32[kTreeNodes][2];
   __shared__ float dom32[4];
   __shared__ int nb;
+  __shared__ unsigned long long smask0[kWarps][32];
+  __shared__ unsigned char smask1[kWarps][32];
+  __shared__ int spref[kWarps][33];
+  __shared__ typename std::conditional<MODE == kModeMixed, Rec32, Rec64>::type rec[kWarps][32];
   if (threadIdx.x == 0) {
     int c = 0;
     for (int k = 0; k < kTreeNodes; ++k) {
@@ -205,8 +238,8 @@ __global__ void __launch_bounds__(128) k_invert(SurfDev s, const double* __restr
       for (int j = 0; j < 3; ++j) {
         box64[c][j] = T.lb[j];
         box64[c][3 + j] = T.rt[j];
-        box32[c][j] = round_down_f(T.lb[j]);
-        box32[c][3 + j] = round_up_f(T.rt[j]);
+        box32[c][j] = __double2float_rd(T.lb[j]);
+        box32[c][3 + j] = __double2float_ru(T.rt[j]);
       }
       ctr[c][0] = (T.uv_lb[0] + T.uv_rt[0]) / 2;  // kernel.cu:154
       ctr[c][1] = (T.uv_lb[1] + T.uv_rt[1]) / 2;
@@ -223,92 +256,229 @@ __global__ void __launch_bounds__(128) k_invert(SurfDev s, const double* __restr
   }
   __syncthreads();
   const int nbl = nb;
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-    const double px = Pq[3 * i], py = Pq[3 * i + 1], pz = Pq[3 * i + 2];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const unsigned FULL = 0xffffffffu;
+  const unsigned lt_mask = (1u << lane) - 1u;
+  const int64_t chunks = (n + 31) / 32;
+  for (int64_t ch = (int64_t)blockIdx.x * kWarps + warp; ch < chunks; ch += (int64_t)gridDim.x * kWarps) {
+    const int64_t q = ch * 32 + lane;
+    const bool valid = q < n;
+    double px = 0, py = 0, pz = 0;
+    if (valid) {
+      px = Pq[3 * q];
+      py = Pq[3 * q + 1];
+      pz = Pq[3 * q + 2];
+    }
     const float fx = (float)px, fy = (float)py, fz = (float)pz;
     // ---- cull (exact candidate set, ascending node order)
-    uint64_t m0 = 0, m1 = 0;
-    for (int k = 0; k < nbl; ++k) {
-      if (fx >= box32[k][0] && fy >= box32[k][1] && fz >= box32[k][2] && fx <= box32[k][3] && fy <= box32[k][4] &&
-          fz <= box32[k][5]) {
-        if (px >= box64[k][0] && py >= box64[k][1] && pz >= box64[k][2] && px <= box64[k][3] &&
-            py <= box64[k][4] && pz <= box64[k][5]) {
-          if (k < 64) m0 |= 1ull << k;
-          else m1 |= 1ull << (k - 64);
-        }
-      }
-    }
-    int status;
-    double ou = __longlong_as_double(0x7ff8000000000000ll), ov = ou, orr = ou;
-    if (m0 == 0 && m1 == 0) {
-      status = 2;  // NURBS_INV_NO_CANDIDATE
-    } else if (MODE == kModeFP64) {
-      Best b;
-      b.n = 0;
-      for (int w = 0; w < 2; ++w) {
-        uint64_t m = w == 0 ? m0 : m1;
-        while (m) {
-          int k = __ffsll((long long)m) - 1 + 64 * w;
-          m &= m - 1;
-          Sol so = phase64<P, Q, kModeFP64>(s, px, py, pz, ctr[k][0], ctr[k][1]);
-          if (so.ok) add_solution(b, so);
-        }
-      }
-      if (b.n == 0) status = 3;
-      else status = finish(b, ou, ov, orr);
-    } else {
-      // FP32 phase over all candidates: keep the best and the best distinct runner-up
-      float bu1 = 0, bv1 = 0, bd1 = INFINITY, bu2 = 0, bv2 = 0, bd2 = INFINITY;
-      for (int w = 0; w < 2; ++w) {
-        uint64_t m = w == 0 ? m0 : m1;
-        while (m) {
-          int k = __ffsll((long long)m) - 1 + 64 * w;
-          m &= m - 1;
-          float u = ctr32[k][0], v = ctr32[k][1], d;
-          if (!phase32<P, Q>(s, fx, fy, fz, u, v, d)) continue;
-          if (!(u >= dom32[0] && u <= dom32[1] && v >= dom32[2] && v <= dom32[3])) continue;
-          bool same1 = fabsf(u - bu1) <= kDistinct32 && fabsf(v - bv1) <= kDistinct32 && bd1 < INFINITY;
-          if (same1) {
-            if (d < bd1) { bu1 = u; bv1 = v; bd1 = d; }
-          } else if (d < bd1) {
-            bu2 = bu1; bv2 = bv1; bd2 = bd1;
-            bu1 = u; bv1 = v; bd1 = d;
-          } else if (d < bd2) {
-            bu2 = u; bv2 = v; bd2 = d;
+    uint64_t m0 = 0;
+    unsigned m1 = 0;
+    if (valid) {
+      for (int k = 0; k < nbl; ++k) {
+        if (fx >= box32[k][0] && fy >= box32[k][1] && fz >= box32[k][2] && fx <= box32[k][3] &&
+            fy <= box32[k][4] && fz <= box32[k][5]) {
+          if (px >= box64[k][0] && py >= box64[k][1] && pz >= box64[k][2] && px <= box64[k][3] &&
+              py <= box64[k][4] && pz <= box64[k][5]) {
+            if (k < 64) m0 |= 1ull << k;
+            else m1 = 1u;
           }
         }
       }
-      Best b;
-      b.n = 0;
-      if (bd1 < INFINITY) {
-        Sol s1 = phase64<P, Q, kModeMixed>(s, px, py, pz, (double)bu1, (double)bv1);
-        if (s1.ok) add_solution(b, s1);
-        if (bd2 < INFINITY && (!s1.ok || bd2 <= bd1 * 1.001f + 1e-5f)) {
-          Sol s2 = phase64<P, Q, kModeMixed>(s, px, py, pz, (double)bu2, (double)bv2);
-          if (s2.ok) add_solution(b, s2);
+    }
+    const int cnt = __popcll(m0) + (int)m1;
+    // warp prefix sum of candidate counts -> task list
+    int incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int t = __shfl_up_sync(FULL, incl, o);
+      if (lane >= o) incl += t;
+    }
+    const int total = __shfl_sync(FULL, incl, 31);
+    smask0[warp][lane] = m0;
+    smask1[warp][lane] = (unsigned char)m1;
+    spref[warp][lane] = incl - cnt;
+    if (lane == 0) spref[warp][32] = total;
+    if constexpr (MODE == kModeMixed) {
+      Rec32& R = rec[warp][lane];
+      R.d1 = INFINITY;
+      R.d2 = INFINITY;
+      R.u1 = R.v1 = R.u2 = R.v2 = 0.f;
+    } else {
+      rec[warp][lane].n = 0;
+    }
+    __syncwarp();
+
+    // decode task t -> (owner lane, node) and seed
+    auto decode = [&](int t, int& ql, int& node) {
+      int lo = 0;
+#pragma unroll
+      for (int step = 16; step > 0; step >>= 1)
+        if (spref[warp][lo + step] <= t) lo += step;
+      // lo = the largest lane whose exclusive prefix is <= t: the owner of task t (a lane with
+      // no candidates shares its prefix with the next lane and is never the largest)
+      ql = lo;
+      int k = t - spref[warp][lo];
+      uint64_t mm = smask0[warp][lo];
+      int c0 = __popcll(mm);
+      if (k < c0) {
+        for (int i = 0; i < k; ++i) mm &= mm - 1;
+        node = __ffsll((long long)mm) - 1;
+      } else {
+        node = 64;
+      }
+    };
+    // owner's query coordinates are needed by the lane working on its seed
+    auto owner_point = [&](int ql, double& x, double& y, double& z) {
+      const int64_t qq = ch * 32 + ql;
+      x = Pq[3 * qq];
+      y = Pq[3 * qq + 1];
+      z = Pq[3 * qq + 2];
+    };
+
+    int next = 32;
+    int task = lane;
+    bool active = task < total;
+    int ql = 0, node = 0;
+    double tx = 0, ty = 0, tz = 0;
+    if constexpr (MODE == kModeMixed) {
+      Seed<float> sd;
+      float dist = 0.f;
+      auto start = [&]() {
+        decode(task, ql, node);
+        owner_point(ql, tx, ty, tz);
+        sd.u = ctr32[node][0];
+        sd.v = ctr32[node][1];
+        sd.prev = INFINITY;
+        sd.it = 0;
+        sd.newton = false;
+      };
+      if (active) start();
+      while (__any_sync(FULL, active)) {
+        int res = kContinue;
+        if (active) {
+          res = iterate32<P, Q>(s, (float)tx, (float)ty, (float)tz, sd, dist);
+          if (res == kContinue && sd.newton) {
+            const Rec32& R = rec[warp][ql];
+            if ((R.d1 < INFINITY && fabsf(sd.u - R.u1) <= kJoin && fabsf(sd.v - R.v1) <= kJoin) ||
+                (R.d2 < INFINITY && fabsf(sd.u - R.u2) <= kJoin && fabsf(sd.v - R.v2) <= kJoin))
+              res = kFailed;  // joins a minimum already found: nothing new
+          }
+        }
+        const bool done = active && res != kContinue;
+        const bool keep = res == kConverged && sd.u >= dom32[0] && sd.u <= dom32[1] && sd.v >= dom32[2] &&
+                          sd.v <= dom32[3];
+        __syncwarp();
+        unsigned fm = __ballot_sync(FULL, done && keep);
+        while (fm) {
+          int j = __ffs(fm) - 1;
+          if (lane == j) merge32(rec[warp][ql], sd.u, sd.v, dist);
+          __syncwarp();
+          fm &= fm - 1;
+        }
+        unsigned dm = __ballot_sync(FULL, done);
+        if (done) {
+          task = next + __popc(dm & lt_mask);
+          active = task < total;
+          if (active) start();
+        }
+        next += __popc(dm);
+      }
+    } else {
+      Seed<double> sd;
+      auto start = [&]() {
+        decode(task, ql, node);
+        owner_point(ql, tx, ty, tz);
+        sd.u = ctr[node][0];
+        sd.v = ctr[node][1];
+        sd.prev = INFINITY;
+        sd.it = 0;
+        sd.newton = false;
+      };
+      if (active) start();
+      while (__any_sync(FULL, active)) {
+        int res = kContinue;
+        double rr = 0;
+        bool keep = false;
+        if (active) {
+          res = iterate64<P, Q>(s, tx, ty, tz, sd);
+          if (res == kContinue && sd.newton) {
+            const Rec64& R = rec[warp][ql];
+            for (int k = 0; k < R.n; ++k)
+              if (fabs(sd.u - R.u[k]) <= kJoin && fabs(sd.v - R.v[k]) <= kJoin) res = kFailed;
+          }
+          if (res == kConverged) keep = finish64<P, Q>(s, tx, ty, tz, sd.u, sd.v, rr);
+        }
+        const bool done = active && res != kContinue;
+        __syncwarp();
+        unsigned fm = __ballot_sync(FULL, done && keep);
+        while (fm) {
+          int j = __ffs(fm) - 1;
+          if (lane == j) merge64(rec[warp][ql], sd.u, sd.v, rr);
+          __syncwarp();
+          fm &= fm - 1;
+        }
+        unsigned dm = __ballot_sync(FULL, done);
+        if (done) {
+          task = next + __popc(dm & lt_mask);
+          active = task < total;
+          if (active) start();
+        }
+        next += __popc(dm);
+      }
+    }
+    __syncwarp();
+
+    // ---- per query: final FP64 steps (MIXED) and the result
+    int status;
+    double ou = __longlong_as_double(0x7ff8000000000000ll), ov = ou, orr = ou;
+    if (cnt == 0) {
+      status = 2;  // NURBS_INV_NO_CANDIDATE
+    } else if constexpr (MODE == kModeMixed) {
+      const Rec32 R = rec[warp][lane];
+      double us[2], vs[2], rs[2];
+      int ns = 0;
+      if (R.d1 < INFINITY) {
+        double u = R.u1, v = R.v1, r;
+        bool ok1 = final64<P, Q>(s, px, py, pz, u, v, r);
+        if (ok1) { us[ns] = u; vs[ns] = v; rs[ns] = r; ++ns; }
+        if (R.d2 < INFINITY && (!ok1 || R.d2 <= R.d1 * 1.001f + 1e-5f)) {
+          double u2 = R.u2, v2 = R.v2, r2;
+          if (final64<P, Q>(s, px, py, pz, u2, v2, r2)) {
+            bool same = ns == 1 && fabs(u2 - us[0]) <= kDistinct && fabs(v2 - vs[0]) <= kDistinct;
+            if (same) {
+              if (r2 < rs[0]) { us[0] = u2; vs[0] = v2; rs[0] = r2; }
+            } else {
+              us[ns] = u2; vs[ns] = v2; rs[ns] = r2; ++ns;
+            }
+          }
         }
       }
-      if (b.n == 0) status = 3;
-      else status = finish(b, ou, ov, orr);
+      status = ns == 0 ? 3 : finish_status(us, vs, rs, ns, ou, ov, orr);
+    } else {
+      const Rec64& R = rec[warp][lane];
+      status = R.n == 0 ? 3 : finish_status(R.u, R.v, R.r, R.n, ou, ov, orr);
     }
-    uv_out[2 * i] = ou;
-    uv_out[2 * i + 1] = ov;
-    st_out[i] = status;
-    res_out[i] = orr;
+    if (valid) {
+      uv_out[2 * q] = ou;
+      uv_out[2 * q + 1] = ov;
+      st_out[q] = status;
+      res_out[q] = orr;
+    }
+    __syncwarp();
   }
 }
 
 template <int P, int Q>
 cudaError_t launch_pq(const SurfDev& s, const double* P_, int64_t n, double* uv, int* st_, double* res, int prec,
                       cudaStream_t st) {
-  int64_t blocks = (n + 127) / 128;
-  const int64_t cap = 152 * 64;
+  int64_t chunks = (n + 31) / 32;
+  int64_t blocks = (chunks + kWarps - 1) / kWarps;
+  const int64_t cap = 152 * 16;
   if (blocks > cap) blocks = cap;
   if (prec == 1)
-    k_invert<P, Q, kModeMixed><<<(unsigned)blocks, 128, 0, st>>>(s, P_, n, uv, st_, res);
+    k_invert<P, Q, kModeMixed><<<(unsigned)blocks, kThreads, 0, st>>>(s, P_, n, uv, st_, res);
   else
-    k_invert<P, Q, kModeFP64><<<(unsigned)blocks, 128, 0, st>>>(s, P_, n, uv, st_, res);
+    k_invert<P, Q, kModeFP64><<<(unsigned)blocks, kThreads, 0, st>>>(s, P_, n, uv, st_, res);
   return cudaGetLastError();
 }
 
