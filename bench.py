@@ -180,7 +180,7 @@ def run_ours(a):
     torch.cuda.synchronize()
     # accuracy of this run's mixed results against the generating parameters
     inv_mixed()
-    g_uv, g_st = uv.cpu().numpy(), st.cpu().numpy()
+    g_uv, g_st, res_mixed = uv.cpu().numpy(), st.cpu().numpy(), res.cpu().numpy()
     found = g_st == 0
     err = np.abs(g_uv - uv_true).max(1)
     acc = {"found_frac": float(found.mean()),
@@ -261,24 +261,29 @@ def run_ours(a):
         "gpu_launches": a.steps,
     }
     if not a.no_cpu:
-        line["cpu_baseline"] = cpu_baseline(surf, P, a.cpu_sample)
+        line["cpu_baseline"], line["parity_sample"] = cpu_baseline(surf, P, a.cpu_sample, g_uv, g_st, res_mixed)
     print(json.dumps(line))
     if world > 1:
         dist.destroy_process_group()
 
 
-def cpu_baseline(surf, P, sample):
-    """The oracle (C restatement of the reference FP64 path) on all host cores, bounded sample."""
+def cpu_baseline(surf, P, sample, g_uv, g_st, g_res):
+    """The oracle (C restatement of the reference FP64 path) on all host cores, bounded sample;
+    its results on that sample also check this run's mixed-precision results."""
     import oracle as O
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from parity import classify_inversion
     cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
     o = O.OracleSurface(surf)
     o.tree()
     Ps = P[:sample]
     t0 = time.perf_counter()
-    o.invert(Ps, threads=cores)
+    ouv, ost, ores, _ = o.invert(Ps, threads=cores)
     dt = time.perf_counter() - t0
-    return {"value": len(Ps) / dt, "unit": "inversions/s", "cores": cores, "kind": "port",
-            "sample": f"{len(Ps)} queries of the same workload, converged-GN oracle, {dt:.2f} s wall"}
+    c = classify_inversion(g_uv[:sample], g_st[:sample], g_res[:sample], ouv, ost, ores, Ps)
+    par = {k: v for k, v in c.items() if k != "fail_idx"}
+    return ({"value": len(Ps) / dt, "unit": "inversions/s", "cores": cores, "kind": "port",
+             "sample": f"{len(Ps)} queries of the same workload, converged-GN oracle, {dt:.2f} s wall"}, par)
 
 
 def run_reference(a):

@@ -42,10 +42,13 @@ constexpr int kModeMixed = 1;
 
 constexpr int kWarps = 4;          // warps per CTA
 constexpr int kThreads = 32 * kWarps;
+constexpr int kMinBlocksMixed = 4;  // CTAs per SM the mixed kernel is register-budgeted for
+  // CTAs per SM the mixed kernel is register-budgeted for
+  // CTAs per SM the mixed kernel is register-budgeted for
 constexpr int kMaxIter32 = 24;     // FP32 iterations per seed
 constexpr int kMaxIter64 = 40;     // FP64-mode iterations per seed
 constexpr int kMaxFinal64 = 6;     // MIXED: FP64 steps (2 normally)
-constexpr double kNewtonSwitch = 1e-3;
+constexpr double kNewtonSwitch = 1e-2;  // GN while the step is larger, Newton below
 constexpr float kTol32 = 3e-7f;
 constexpr double kTolNewton64 = 1e-10;  // a Newton step this small leaves < 1e-19 error
 constexpr double kTolAny64 = 1e-14;
@@ -53,6 +56,7 @@ constexpr double kDistinct = 1e-7;      // two FP64 solutions are the same minim
 constexpr float kDistinct32 = 1e-4f;    // ... two FP32 solutions
 constexpr float kJoin = 1e-3f;          // a Newton iterate this close to a known minimum joins it
 constexpr int kSols = 4;                // FP64 mode: distinct minima kept per query
+constexpr int kSmemSpans = 256;         // breakpoint tables staged in shared memory up to this
 
 template <typename T>
 __device__ __forceinline__ T dot3(const v3<T>& a, const v3<T>& b) {
@@ -84,11 +88,21 @@ __device__ __forceinline__ bool solve_step(const v3<T>& r, const v3<T>& Su, cons
   return true;
 }
 
-// Per-seed iteration state.
+// Where one kernel finds the span tables: breakpoints in shared memory when they fit.
+struct Ctx {
+  fast::Locator<float> L32;
+  fast::Locator<double> L64;
+  const float* m32;
+  const double* m64;
+  int p, q;
+  double dom_u0, dom_u1, dom_v0, dom_v1;
+};
+
+// Per-seed iteration state (hu/hv: span hints for the warm-started span search).
 template <typename T>
 struct Seed {
   T u, v, prev;
-  int it;
+  int it, hu, hv;
   bool newton;
 };
 
@@ -97,9 +111,8 @@ enum StepResult { kContinue = 0, kConverged = 1, kFailed = 2 };
 // One FP32 iteration of a seed.  Convergence: the step is at the FP32 resolution of the
 // parameters (rounding of S mapped through the shorter tangent), or Newton steps stop shrinking.
 template <int P, int Q>
-__device__ __forceinline__ int iterate32(const SurfDev& s, float px, float py, float pz, Seed<float>& st,
-                                         float& dist) {
-  fast::SDer<float> d = fast::eval_point<float, P, Q, 2>(s, st.u, st.v);
+__device__ __forceinline__ int iterate32(const Ctx& c, float px, float py, float pz, Seed<float>& st, float& dist) {
+  fast::SDer<float> d = fast::eval_at<float, P, Q, 2>(c.L32, c.m32, c.p, c.q, st.u, st.v, st.hu, st.hv);
   v3<float> r = {d.S.x - px, d.S.y - py, d.S.z - pz};
   float du, dv;
   if (!solve_step<float, float>(r, d.Su, d.Sv, d.Suu, d.Suv, d.Svv, st.newton, du, dv)) return kFailed;
@@ -121,8 +134,8 @@ __device__ __forceinline__ int iterate32(const SurfDev& s, float px, float py, f
 
 // One FP64 iteration of a seed (FP64 mode).
 template <int P, int Q>
-__device__ __forceinline__ int iterate64(const SurfDev& s, double px, double py, double pz, Seed<double>& st) {
-  fast::SDer<double> d = fast::eval_point<double, P, Q, 2>(s, st.u, st.v);
+__device__ __forceinline__ int iterate64(const Ctx& c, double px, double py, double pz, Seed<double>& st) {
+  fast::SDer<double> d = fast::eval_at<double, P, Q, 2>(c.L64, c.m64, c.p, c.q, st.u, st.v, st.hu, st.hv);
   v3<double> r = {d.S.x - px, d.S.y - py, d.S.z - pz};
   double du, dv;
   if (!solve_step<double, double>(r, d.Su, d.Sv, d.Suu, d.Suv, d.Svv, st.newton, du, dv)) return kFailed;
@@ -139,27 +152,28 @@ __device__ __forceinline__ int iterate64(const SurfDev& s, double px, double py,
 
 // FP64 residual at (u,v), with the domain test.
 template <int P, int Q>
-__device__ __forceinline__ bool finish64(const SurfDev& s, double px, double py, double pz, double u, double v,
-                                         double& res) {
-  fast::SDer<double> d = fast::eval_point<double, P, Q, 0>(s, u, v);
+__device__ __forceinline__ bool finish64(const Ctx& c, double px, double py, double pz, double u, double v,
+                                         int hu, int hv, double& res) {
+  fast::SDer<double> d = fast::eval_at<double, P, Q, 0>(c.L64, c.m64, c.p, c.q, u, v, hu, hv);
   v3<double> r = {d.S.x - px, d.S.y - py, d.S.z - pz};
   res = sqrt(dot3(r, r));
-  return (u >= s.dom_u0 && u <= s.dom_u1 && v >= s.dom_v0 && v <= s.dom_v1) && isfinite(res);
+  return (u >= c.dom_u0 && u <= c.dom_u1 && v >= c.dom_v0 && v <= c.dom_v1) && isfinite(res);
 }
 
 // MIXED: the final FP64 Newton steps from an FP32 minimum, then the residual.
 template <int P, int Q>
-__device__ bool final64(const SurfDev& s, double px, double py, double pz, double& u, double& v, double& res) {
+__device__ bool final64(const Ctx& c, double px, double py, double pz, double& u, double& v, double& res) {
+  int hu = 0, hv = 0, hu32 = 0, hv32 = 0;
   for (int it = 0; it < kMaxFinal64; ++it) {
-    fast::SDer<double> d = fast::eval_point<double, P, Q, 1>(s, u, v);
-    fast::SDer<float> c = fast::eval_point<float, P, Q, 2>(s, (float)u, (float)v);
+    fast::SDer<double> d = fast::eval_at<double, P, Q, 1>(c.L64, c.m64, c.p, c.q, u, v, hu, hv);
+    fast::SDer<float> e = fast::eval_at<float, P, Q, 2>(c.L32, c.m32, c.p, c.q, (float)u, (float)v, hu32, hv32);
     v3<double> r = {d.S.x - px, d.S.y - py, d.S.z - pz};
     double du, dv;
-    if (!solve_step<double, float>(r, d.Su, d.Sv, c.Suu, c.Suv, c.Svv, true, du, dv)) return false;
+    if (!solve_step<double, float>(r, d.Su, d.Sv, e.Suu, e.Suv, e.Svv, true, du, dv)) return false;
     if (!(isfinite(du) && isfinite(dv))) return false;
     u -= du;
     v -= dv;
-    if (fmax(fabs(du), fabs(dv)) <= kTolNewton64) return finish64<P, Q>(s, px, py, pz, u, v, res);
+    if (fmax(fabs(du), fabs(dv)) <= kTolNewton64) return finish64<P, Q>(c, px, py, pz, u, v, hu, hv, res);
   }
   return false;
 }
@@ -217,7 +231,7 @@ __device__ __forceinline__ int finish_status(const double* us, const double* vs,
 }
 
 template <int P, int Q, int MODE>
-__global__ void __launch_bounds__(kThreads) k_invert(SurfDev s, const double* __restrict__ Pq, int64_t n,
+__global__ void __launch_bounds__(kThreads, MODE == kModeMixed ? kMinBlocksMixed : 4) k_invert(SurfDev s, const double* __restrict__ Pq, int64_t n,
                                                      double* __restrict__ uv_out, int* __restrict__ st_out,
                                                      double* __restrict__ res_out) {
   __shared__ float box32[kTreeNodes][6];
@@ -228,8 +242,39 @@ __global__ void __launch_bounds__(kThreads) k_invert(SurfDev s, const double* __
   __shared__ int nb;
   __shared__ unsigned long long smask0[kWarps][32];
   __shared__ unsigned char smask1[kWarps][32];
-  __shared__ int spref[kWarps][33];
+  __shared__ unsigned srmask[kWarps][kTreeNodes];
+  __shared__ int srpref[kWarps][kTreeNodes + 1];
+  __shared__ int slpref[kWarps][32];
   __shared__ typename std::conditional<MODE == kModeMixed, Rec32, Rec64>::type rec[kWarps][32];
+  __shared__ float sp32[kWarps][32][3];
+  __shared__ double sp64[kWarps][32][3];
+  __shared__ float sb32[2][kSmemSpans + 1], si32[2][kSmemSpans];
+  __shared__ double sb64[2][kSmemSpans + 1], si64[2][kSmemSpans];
+  const bool smem_tables = s.ns_u <= kSmemSpans && s.ns_v <= kSmemSpans;
+  if (smem_tables) {
+    for (int k = threadIdx.x; k <= s.ns_u; k += blockDim.x) {
+      sb32[0][k] = s.bu32[k];
+      sb64[0][k] = s.bu[k];
+      if (k < s.ns_u) { si32[0][k] = s.inv_du32[k]; si64[0][k] = s.inv_du[k]; }
+    }
+    for (int k = threadIdx.x; k <= s.ns_v; k += blockDim.x) {
+      sb32[1][k] = s.bv32[k];
+      sb64[1][k] = s.bv[k];
+      if (k < s.ns_v) { si32[1][k] = s.inv_dv32[k]; si64[1][k] = s.inv_dv[k]; }
+    }
+  }
+  Ctx cx;
+  cx.L32 = fast::global_locator<float>(s);
+  cx.L64 = fast::global_locator<double>(s);
+  if (smem_tables) {
+    cx.L32.bu = sb32[0]; cx.L32.bv = sb32[1]; cx.L32.iu = si32[0]; cx.L32.iv = si32[1];
+    cx.L64.bu = sb64[0]; cx.L64.bv = sb64[1]; cx.L64.iu = si64[0]; cx.L64.iv = si64[1];
+  }
+  cx.m32 = s.m32;
+  cx.m64 = s.m64;
+  cx.p = s.p;
+  cx.q = s.q;
+  cx.dom_u0 = s.dom_u0; cx.dom_u1 = s.dom_u1; cx.dom_v0 = s.dom_v0; cx.dom_v1 = s.dom_v1;
   if (threadIdx.x == 0) {
     int c = 0;
     for (int k = 0; k < kTreeNodes; ++k) {
@@ -286,18 +331,37 @@ __global__ void __launch_bounds__(kThreads) k_invert(SurfDev s, const double* __
       }
     }
     const int cnt = __popcll(m0) + (int)m1;
-    // warp prefix sum of candidate counts -> task list
-    int incl = cnt;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      int t = __shfl_up_sync(FULL, incl, o);
-      if (lane >= o) incl += t;
+    // Task list in round-major order: round r holds seed r of every query that has more than
+    // r seeds, so each query's first seeds run first and its later seeds can join the minima
+    // those found.  rmask[r] = lanes with a seed in round r, rpref[r] = tasks before round r.
+    const int maxc = __reduce_max_sync(FULL, (unsigned)cnt);
+    int total = 0;
+    for (int r = 0; r < maxc; ++r) {
+      unsigned m = __ballot_sync(FULL, cnt > r);
+      if (lane == 0) {
+        srmask[warp][r] = m;
+        srpref[warp][r] = total;
+      }
+      total += __popc(m);
     }
-    const int total = __shfl_sync(FULL, incl, 31);
+    if (lane == 0) srpref[warp][maxc] = total;
+    if constexpr (MODE == kModeMixed) {
+      int incl = cnt;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        int t = __shfl_up_sync(FULL, incl, o);
+        if (lane >= o) incl += t;
+      }
+      slpref[warp][lane] = incl - cnt;
+    }
+    sp32[warp][lane][0] = fx;
+    sp32[warp][lane][1] = fy;
+    sp32[warp][lane][2] = fz;
+    sp64[warp][lane][0] = px;
+    sp64[warp][lane][1] = py;
+    sp64[warp][lane][2] = pz;
     smask0[warp][lane] = m0;
     smask1[warp][lane] = (unsigned char)m1;
-    spref[warp][lane] = incl - cnt;
-    if (lane == 0) spref[warp][32] = total;
     if constexpr (MODE == kModeMixed) {
       Rec32& R = rec[warp][lane];
       R.d1 = INFINITY;
@@ -308,17 +372,40 @@ __global__ void __launch_bounds__(kThreads) k_invert(SurfDev s, const double* __
     }
     __syncwarp();
 
-    // decode task t -> (owner lane, node) and seed
+    // decode task t -> (owner lane, node)
     auto decode = [&](int t, int& ql, int& node) {
-      int lo = 0;
+      if constexpr (MODE == kModeMixed) {
+        // lane-major: the largest lane whose exclusive prefix is <= t owns task t (a lane with
+        // no candidates shares its prefix with the next lane and is never the largest)
+        int lo = 0;
 #pragma unroll
-      for (int step = 16; step > 0; step >>= 1)
-        if (spref[warp][lo + step] <= t) lo += step;
-      // lo = the largest lane whose exclusive prefix is <= t: the owner of task t (a lane with
-      // no candidates shares its prefix with the next lane and is never the largest)
-      ql = lo;
-      int k = t - spref[warp][lo];
-      uint64_t mm = smask0[warp][lo];
+        for (int step = 16; step > 0; step >>= 1)
+          if (slpref[warp][lo + step] <= t) lo += step;
+        ql = lo;
+        uint64_t mm = smask0[warp][ql];
+        int k = t - slpref[warp][lo];
+        if (k < __popcll(mm)) {
+          for (int i = 0; i < k; ++i) mm &= mm - 1;
+          node = __ffsll((long long)mm) - 1;
+        } else {
+          node = 64;
+        }
+        return;
+      }
+      // round: the largest r with rpref[r] <= t (rounds are non-empty, so rpref is increasing)
+      int r = 0;
+#pragma unroll
+      for (int step = 64; step > 0; step >>= 1)
+        if (r + step < maxc && srpref[warp][r + step] <= t) r += step;
+      // lane: the (t - rpref[r])-th set bit of rmask[r]
+      const unsigned m = srmask[warp][r];
+      int i = t - srpref[warp][r], pos = 0;
+#pragma unroll
+      for (int w = 16; w > 0; w >>= 1)
+        if (__popc(m & ((1u << (pos + w)) - 1u)) <= i) pos += w;
+      ql = pos;
+      int k = r;  // seed r of that query: its r-th candidate node in ascending order
+      uint64_t mm = smask0[warp][ql];
       int c0 = __popcll(mm);
       if (k < c0) {
         for (int i = 0; i < k; ++i) mm &= mm - 1;
@@ -327,36 +414,33 @@ __global__ void __launch_bounds__(kThreads) k_invert(SurfDev s, const double* __
         node = 64;
       }
     };
-    // owner's query coordinates are needed by the lane working on its seed
-    auto owner_point = [&](int ql, double& x, double& y, double& z) {
-      const int64_t qq = ch * 32 + ql;
-      x = Pq[3 * qq];
-      y = Pq[3 * qq + 1];
-      z = Pq[3 * qq + 2];
-    };
 
     int next = 32;
     int task = lane;
     bool active = task < total;
     int ql = 0, node = 0;
-    double tx = 0, ty = 0, tz = 0;
     if constexpr (MODE == kModeMixed) {
       Seed<float> sd;
       float dist = 0.f;
+      float tx = 0, ty = 0, tz = 0;
       auto start = [&]() {
         decode(task, ql, node);
-        owner_point(ql, tx, ty, tz);
+        tx = sp32[warp][ql][0];
+        ty = sp32[warp][ql][1];
+        tz = sp32[warp][ql][2];
         sd.u = ctr32[node][0];
         sd.v = ctr32[node][1];
         sd.prev = INFINITY;
         sd.it = 0;
+        sd.hu = 0;
+        sd.hv = 0;
         sd.newton = false;
       };
       if (active) start();
       while (__any_sync(FULL, active)) {
         int res = kContinue;
         if (active) {
-          res = iterate32<P, Q>(s, (float)tx, (float)ty, (float)tz, sd, dist);
+          res = iterate32<P, Q>(cx, tx, ty, tz, sd, dist);
           if (res == kContinue && sd.newton) {
             const Rec32& R = rec[warp][ql];
             if ((R.d1 < INFINITY && fabsf(sd.u - R.u1) <= kJoin && fabsf(sd.v - R.v1) <= kJoin) ||
@@ -385,13 +469,18 @@ __global__ void __launch_bounds__(kThreads) k_invert(SurfDev s, const double* __
       }
     } else {
       Seed<double> sd;
+      double tx = 0, ty = 0, tz = 0;
       auto start = [&]() {
         decode(task, ql, node);
-        owner_point(ql, tx, ty, tz);
+        tx = sp64[warp][ql][0];
+        ty = sp64[warp][ql][1];
+        tz = sp64[warp][ql][2];
         sd.u = ctr[node][0];
         sd.v = ctr[node][1];
         sd.prev = INFINITY;
         sd.it = 0;
+        sd.hu = 0;
+        sd.hv = 0;
         sd.newton = false;
       };
       if (active) start();
@@ -400,13 +489,13 @@ __global__ void __launch_bounds__(kThreads) k_invert(SurfDev s, const double* __
         double rr = 0;
         bool keep = false;
         if (active) {
-          res = iterate64<P, Q>(s, tx, ty, tz, sd);
+          res = iterate64<P, Q>(cx, tx, ty, tz, sd);
           if (res == kContinue && sd.newton) {
             const Rec64& R = rec[warp][ql];
             for (int k = 0; k < R.n; ++k)
               if (fabs(sd.u - R.u[k]) <= kJoin && fabs(sd.v - R.v[k]) <= kJoin) res = kFailed;
           }
-          if (res == kConverged) keep = finish64<P, Q>(s, tx, ty, tz, sd.u, sd.v, rr);
+          if (res == kConverged) keep = finish64<P, Q>(cx, tx, ty, tz, sd.u, sd.v, sd.hu, sd.hv, rr);
         }
         const bool done = active && res != kContinue;
         __syncwarp();
@@ -439,11 +528,11 @@ __global__ void __launch_bounds__(kThreads) k_invert(SurfDev s, const double* __
       int ns = 0;
       if (R.d1 < INFINITY) {
         double u = R.u1, v = R.v1, r;
-        bool ok1 = final64<P, Q>(s, px, py, pz, u, v, r);
+        bool ok1 = final64<P, Q>(cx, px, py, pz, u, v, r);
         if (ok1) { us[ns] = u; vs[ns] = v; rs[ns] = r; ++ns; }
         if (R.d2 < INFINITY && (!ok1 || R.d2 <= R.d1 * 1.001f + 1e-5f)) {
           double u2 = R.u2, v2 = R.v2, r2;
-          if (final64<P, Q>(s, px, py, pz, u2, v2, r2)) {
+          if (final64<P, Q>(cx, px, py, pz, u2, v2, r2)) {
             bool same = ns == 1 && fabs(u2 - us[0]) <= kDistinct && fabs(v2 - vs[0]) <= kDistinct;
             if (same) {
               if (r2 < rs[0]) { us[0] = u2; vs[0] = v2; rs[0] = r2; }

@@ -413,5 +413,58 @@ __device__ __forceinline__ SDer<T> eval_point(const SurfDev& s, T u, T v) {
   return quotient<T, ORDER>(d, scu, scv);
 }
 
+// Breakpoint tables of one precision, wherever they live (global memory, or a copy the calling
+// kernel staged in shared memory).
+template <typename T>
+struct Locator {
+  const T* bu;
+  const T* bv;
+  const T* iu;
+  const T* iv;
+  int ns_u, ns_v;
+  T ru, rv;
+};
+
+template <typename T>
+__device__ __forceinline__ Locator<T> global_locator(const SurfDev& s) {
+  Locator<T> L;
+  if constexpr (sizeof(T) == 8) {
+    L.bu = s.bu; L.bv = s.bv; L.iu = s.inv_du; L.iv = s.inv_dv; L.ru = s.range_u; L.rv = s.range_v;
+  } else {
+    L.bu = s.bu32; L.bv = s.bv32; L.iu = s.inv_du32; L.iv = s.inv_dv32; L.ru = s.range_u32; L.rv = s.range_v32;
+  }
+  L.ns_u = s.ns_u;
+  L.ns_v = s.ns_v;
+  return L;
+}
+
+// find_seg with a warm start: keeps `hint` when it is still the span of x, else bisects.
+template <typename T>
+__device__ __forceinline__ int find_seg_hint(const T* b, int ns, T x, int hint) {
+  if ((hint == 0 || b[hint] <= x) && (hint == ns - 1 || x < b[hint + 1])) return hint;
+  int lo = 0;
+  int step = 1 << (31 - __clz(ns));
+  for (; step > 0; step >>= 1) {
+    int t = lo + step;
+    if (t < ns && b[t] <= x) lo = t;
+  }
+  return lo;
+}
+
+// eval_point with explicit breakpoint tables and span hints (updated in place).
+template <typename T, int P, int Q, int ORDER>
+__device__ __forceinline__ SDer<T> eval_at(const Locator<T>& L, const T* __restrict__ m, int p, int q, T u, T v,
+                                           int& hu, int& hv) {
+  hu = find_seg_hint(L.bu, L.ns_u, u, hu);
+  hv = find_seg_hint(L.bv, L.ns_v, v, hv);
+  T idu = L.iu[hu], idv = L.iv[hv];
+  T lu = (u - L.bu[hu]) * idu;
+  T lv = (v - L.bv[hv]) * idv;
+  const int k12 = (p + 1) * (q + 1);
+  const T* span = m + (size_t)(hu * L.ns_v + hv) * k12 * 4;
+  RDer<T> d = span_contract<T, P, Q, ORDER>(span, p, q, lu, lv);
+  return quotient<T, ORDER>(d, L.ru * idu, L.rv * idv);
+}
+
 }  // namespace fast
 }  // namespace gnurbs
