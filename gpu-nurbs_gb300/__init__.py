@@ -43,6 +43,16 @@ class NuDesc(C.Structure):
                 ("cps", C.POINTER(C.c_double)), ("weights", C.POINTER(C.c_double))]
 
 
+class SurfaceDesc(C.Structure):
+    _fields_ = [("degree_u", C.c_int), ("degree_v", C.c_int), ("cp_u", C.c_int), ("cp_v", C.c_int),
+                ("knots_u", C.c_void_p), ("knots_v", C.c_void_p), ("cps", C.c_void_p), ("weights", C.c_void_p)]
+
+
+class PoolInfo(C.Structure):
+    _fields_ = [("budget_bytes", C.c_int64), ("used_bytes", C.c_int64), ("surfaces", C.c_int),
+                ("max_surfaces", C.c_int), ("tile_queries", C.c_int), ("ctas_per_sm", C.c_int)]
+
+
 class SurfaceInfo(C.Structure):
     _fields_ = [("degree_u", C.c_int), ("degree_v", C.c_int), ("cp_u", C.c_int), ("cp_v", C.c_int),
                 ("spans_u", C.c_int), ("spans_v", C.c_int), ("device_bytes", C.c_int64), ("tree_built", C.c_int)]
@@ -78,6 +88,21 @@ SIGNATURES = {
     "nurbs_invert": (C.c_int, [_vp, _vp, _i64, _vp, _vp, _vp, C.c_int, _vp]),
     "nurbs_invert_host": (C.c_int, [_vp, _vp, _i64, _vp, _vp, _vp, C.c_int, _vp]),
     "nurbs_probe_fp_peak": (C.c_int, [C.c_int, C.POINTER(C.c_double), _vp]),
+    "nurbs_pool_create": (C.c_int, [_i64, C.c_int, C.POINTER(_vp)]),
+    "nurbs_pool_destroy": (C.c_int, [_vp]),
+    "nurbs_pool_add": (C.c_int, [_vp, C.c_int, C.POINTER(SurfaceDesc), _vp, _vp]),
+    "nurbs_pool_remove": (C.c_int, [_vp, C.c_int, _vp]),
+    "nurbs_pool_info": (C.c_int, [_vp, C.POINTER(PoolInfo)]),
+    "nurbs_pool_surface_bytes": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, _vp, _vp, C.POINTER(_i64)]),
+    "nurbs_pool_last_error": (C.c_char_p, []),
+    "nurbs_pool_set_config": (C.c_int, [_vp, C.c_int, C.c_int]),
+    "nurbs_pool_invert": (C.c_int, [_vp, C.c_int, _vp, _vp, _vp, _vp, _vp, _vp, C.c_int, _vp]),
+    "nurbs_pool_eval": (C.c_int, [_vp, C.c_int, _vp, _vp, _vp, _i64, C.c_uint, _vp, _vp]),
+    "nurbs_pool_autotune": (C.c_int, [_vp, C.c_int, _vp, _vp, _vp, _vp, _vp, _vp, C.c_int, _i64, C.c_char_p, _vp,
+                                      C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_float)]),
+    "nurbs_pool_graph_create": (C.c_int, [_vp, C.c_int, _vp, _vp, _vp, _vp, _vp, _vp, C.c_int, C.POINTER(_vp)]),
+    "nurbs_graph_launch": (C.c_int, [_vp, _vp]),
+    "nurbs_graph_destroy": (C.c_int, [_vp]),
 }
 
 _lib = None
@@ -293,3 +318,138 @@ def evaluate_random(uv, matrix_n, p, q, nu, nv, knots_u, knots_v, stream=None):
     check(lib().nurbs_evaluate_random(_ptr(uv), _ptr(out), n, _ptr(matrix_n), p, q, nu, nv, _ptr(knots_u),
                                       _ptr(knots_v), _stream(stream)), "nurbs_evaluate_random")
     return out
+
+
+# ----------------------------------------------------------------------------- pools
+def pool_check(rc: int, what: str = ""):
+    if rc != OK:
+        msg = lib().nurbs_pool_last_error().decode(errors="replace")
+        raise NurbsError(rc, f"{what}: {msg or lib().nurbs_status_string(rc).decode()}")
+
+
+class Batch:
+    """CSR description of a batch: surface ids[k] owns queries [offsets[k], offsets[k+1])."""
+
+    def __init__(self, ids, offsets):
+        self.ids = np.ascontiguousarray(ids, np.int32)
+        self.offsets = np.ascontiguousarray(offsets, np.int64)
+        assert len(self.offsets) == len(self.ids) + 1
+
+    @property
+    def n(self):
+        return int(self.offsets[-1] - self.offsets[0]) if len(self.ids) else 0
+
+
+class Graph:
+    def __init__(self, h, keep):
+        self.h = h
+        self._keep = keep  # device buffers the captured graph reads and writes
+
+    def launch(self, stream=None):
+        pool_check(lib().nurbs_graph_launch(self.h, _stream(stream)), "nurbs_graph_launch")
+
+    def close(self):
+        if getattr(self, "h", None) and self.h.value:
+            lib().nurbs_graph_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Pool:
+    """Many surfaces in one device arena under a memory budget (batched workloads, serving)."""
+
+    def __init__(self, budget_bytes: int, max_surfaces: int = 1 << 16):
+        h = C.c_void_p()
+        pool_check(lib().nurbs_pool_create(int(budget_bytes), int(max_surfaces), C.byref(h)), "nurbs_pool_create")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None) and self.h.value:
+            lib().nurbs_pool_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add(self, surfs, stream=None):
+        keep, descs = [], (SurfaceDesc * len(surfs))()
+        for k, sf in enumerate(surfs):
+            arrs = [np.ascontiguousarray(sf[key], np.float64).reshape(-1) for key in ("knots_u", "knots_v", "cps", "weights")]
+            keep.append(arrs)
+            descs[k] = SurfaceDesc(int(sf["p"]), int(sf["q"]), int(sf["nu"]), int(sf["nv"]),
+                                   *(a.ctypes.data for a in arrs))
+        ids = np.zeros(len(surfs), np.int32)
+        pool_check(lib().nurbs_pool_add(self.h, len(surfs), descs, _stream(stream), ids.ctypes.data), "nurbs_pool_add")
+        return ids
+
+    def remove(self, sid: int, stream=None):
+        pool_check(lib().nurbs_pool_remove(self.h, int(sid), _stream(stream)), "nurbs_pool_remove")
+
+    def info(self) -> PoolInfo:
+        i = PoolInfo()
+        pool_check(lib().nurbs_pool_info(self.h, C.byref(i)), "nurbs_pool_info")
+        return i
+
+    def set_config(self, tile_queries: int, ctas_per_sm: int):
+        pool_check(lib().nurbs_pool_set_config(self.h, tile_queries, ctas_per_sm), "nurbs_pool_set_config")
+
+    def _outs(self, n, dev, out):
+        if out is not None:
+            return out
+        torch = _torch()
+        return (torch.empty((n, 2), dtype=torch.float64, device=dev), torch.empty(n, dtype=torch.int32, device=dev),
+                torch.empty(n, dtype=torch.float64, device=dev))
+
+    def invert(self, batch: Batch, P, precision: int = PREC_MIXED, stream=None, out=None):
+        P = P.contiguous()
+        uv, st, res = self._outs(P.shape[0], P.device, out)
+        pool_check(lib().nurbs_pool_invert(self.h, len(batch.ids), batch.ids.ctypes.data, batch.offsets.ctypes.data,
+                                           _ptr(P), _ptr(uv), _ptr(st), _ptr(res), precision, _stream(stream)),
+                   "nurbs_pool_invert")
+        return uv, st, res
+
+    def eval(self, batch: Batch, uv, mask: int = S, stream=None):
+        torch = _torch()
+        uv = uv.contiguous()
+        n = uv.shape[0]
+        nb = bin(mask & 63).count("1")
+        out = torch.empty((3 * nb, n), dtype=torch.float64, device=uv.device)
+        pool_check(lib().nurbs_pool_eval(self.h, len(batch.ids), batch.ids.ctypes.data, batch.offsets.ctypes.data,
+                                         _ptr(uv), n, mask, _ptr(out), _stream(stream)), "nurbs_pool_eval")
+        return out
+
+    def autotune(self, batch: Batch, P, out, precision: int = PREC_MIXED, max_queries: int = 0,
+                 cache_path: Optional[str] = None, stream=None):
+        uv, st, res = out
+        bt, bc, ms = C.c_int(), C.c_int(), C.c_float()
+        pool_check(lib().nurbs_pool_autotune(self.h, len(batch.ids), batch.ids.ctypes.data, batch.offsets.ctypes.data,
+                                             _ptr(P), _ptr(uv), _ptr(st), _ptr(res), precision, int(max_queries),
+                                             cache_path.encode() if cache_path else None, _stream(stream),
+                                             C.byref(bt), C.byref(bc), C.byref(ms)), "nurbs_pool_autotune")
+        return bt.value, bc.value, ms.value
+
+    def graph(self, batch: Batch, P, out, precision: int = PREC_MIXED) -> Graph:
+        uv, st, res = out
+        h = C.c_void_p()
+        pool_check(lib().nurbs_pool_graph_create(self.h, len(batch.ids), batch.ids.ctypes.data, batch.offsets.ctypes.data,
+                                                 _ptr(P), _ptr(uv), _ptr(st), _ptr(res), precision, C.byref(h)),
+                   "nurbs_pool_graph_create")
+        return Graph(h, (P, uv, st, res))
+
+
+def surface_bytes(surf: dict) -> int:
+    """Device bytes one surface takes in a pool."""
+    b = C.c_int64()
+    ku = np.ascontiguousarray(surf["knots_u"], np.float64)
+    kv = np.ascontiguousarray(surf["knots_v"], np.float64)
+    pool_check(lib().nurbs_pool_surface_bytes(int(surf["p"]), int(surf["q"]), int(surf["nu"]), int(surf["nv"]),
+                                              ku.ctypes.data, kv.ctypes.data, C.byref(b)), "nurbs_pool_surface_bytes")
+    return b.value

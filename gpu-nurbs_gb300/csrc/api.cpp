@@ -15,6 +15,7 @@
 
 #include "gpu_nurbs.h"
 #include "nurbs_internal.h"
+#include "surface_host.h"
 
 using namespace gnurbs;
 
@@ -42,21 +43,12 @@ int cuda_fail(cudaError_t e, const char* what) {
     if (e_ != cudaSuccess) return cuda_fail(e_, what); \
   } while (0)
 
-size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
-
-// Distinct breakpoints of the domain [k[p], k[n]] and the knot index of each non-empty span.
-// Spans are the m in [p, cp-1] with k[m] < k[m+1]: exactly those findSpan can return for a
-// parameter in the domain (src/NURBS/Evaluate.cu:504-533).
-void breakpoints(const double* k, int p, int cp, std::vector<double>& b, std::vector<int>& idx) {
-  b.clear();
-  idx.clear();
-  for (int m = p; m < cp; ++m) {
-    if (k[m] < k[m + 1]) {
-      if (b.empty()) b.push_back(k[m]);
-      idx.push_back(m);
-      b.push_back(k[m + 1]);
-    }
-  }
+int validate_dims(int p, int q, int nu, int nv) {
+  if (p < 1 || q < 1 || p > NURBS_MAX_DEGREE || q > NURBS_MAX_DEGREE)
+    return fail(NURBS_E_INVALID, "degrees (%d,%d) outside 1..%d", p, q, NURBS_MAX_DEGREE);
+  if (nu < p + 1 || nv < q + 1) return fail(NURBS_E_INVALID, "control net %dx%d too small for degree (%d,%d)", nu, nv, p, q);
+  if ((int64_t)nu * nv > (int64_t)1 << 28) return fail(NURBS_E_UNSUPPORTED, "control net %dx%d too large", nu, nv);
+  return NURBS_OK;
 }
 
 int validate_knots(const double* k, int p, int cp, const char* name) {
@@ -66,14 +58,6 @@ int validate_knots(const double* k, int p, int cp, const char* name) {
   for (int i = 0; i + 1 < nk; ++i)
     if (k[i] > k[i + 1]) return fail(NURBS_E_INVALID, "%s is not non-decreasing at %d", name, i);
   if (!(k[p] < k[cp])) return fail(NURBS_E_INVALID, "%s: empty parameter domain [k[%d], k[%d]]", name, p, cp);
-  return NURBS_OK;
-}
-
-int validate_dims(int p, int q, int nu, int nv) {
-  if (p < 1 || q < 1 || p > NURBS_MAX_DEGREE || q > NURBS_MAX_DEGREE)
-    return fail(NURBS_E_INVALID, "degrees (%d,%d) outside 1..%d", p, q, NURBS_MAX_DEGREE);
-  if (nu < p + 1 || nv < q + 1) return fail(NURBS_E_INVALID, "control net %dx%d too small for degree (%d,%d)", nu, nv, p, q);
-  if ((int64_t)nu * nv > (int64_t)1 << 28) return fail(NURBS_E_UNSUPPORTED, "control net %dx%d too large", nu, nv);
   return NURBS_OK;
 }
 
@@ -141,51 +125,21 @@ int nurbs_surface_create(int p, int q, int nu, int nv, const double* knots_u, co
   int rc = validate_dims(p, q, nu, nv);
   if (rc) return rc;
   cudaStream_t st = (cudaStream_t)stream;
+  // device inputs are read back once: validation and breakpoint tables are host work
   std::vector<double> ku, kv, hc, hw;
+  const size_t ncp = (size_t)nu * nv;
   if ((rc = fetch(knots_u, p + nu + 1, ptr_kind, ku, st))) return rc;
   if ((rc = fetch(knots_v, q + nv + 1, ptr_kind, kv, st))) return rc;
-  if ((rc = validate_knots(ku.data(), p, nu, "knots_u"))) return rc;
-  if ((rc = validate_knots(kv.data(), q, nv, "knots_v"))) return rc;
-  const size_t ncp = (size_t)nu * nv;
-  if (ptr_kind == NURBS_PTR_HOST) {
-    for (size_t i = 0; i < ncp; ++i) {
-      if (!(weights[i] > 0) || !std::isfinite(weights[i]))
-        return fail(NURBS_E_INVALID, "weight %zu is not a finite positive number", i);
-      for (int c = 0; c < 3; ++c)
-        if (!std::isfinite(cps[3 * i + c])) return fail(NURBS_E_INVALID, "control point %zu is not finite", i);
-    }
-  }
-  std::vector<double> bu, bv;
-  std::vector<int> iu, iv;
-  breakpoints(ku.data(), p, nu, bu, iu);
-  breakpoints(kv.data(), q, nv, bv, iv);
-  const int nsu = (int)iu.size(), nsv = (int)iv.size();
-  const int k1 = p + 1, k2 = q + 1, k12 = k1 * k2;
-  const size_t nspan = (size_t)nsu * nsv;
-
-  // arena layout
-  size_t off = 0;
-  auto take = [&](size_t bytes) {
-    size_t o = off;
-    off = align256(off + bytes);
-    return o;
-  };
-  size_t o_bu = take((nsu + 1) * 8), o_bv = take((nsv + 1) * 8);
-  size_t o_idu = take(nsu * 8), o_idv = take(nsv * 8);
-  size_t o_bu32 = take((nsu + 1) * 4), o_bv32 = take((nsv + 1) * 4);
-  size_t o_idu32 = take(nsu * 4), o_idv32 = take(nsv * 4);
-  size_t o_iu = take(nsu * 4), o_iv = take(nsv * 4);
-  size_t o_ku = take(ku.size() * 8), o_kv = take(kv.size() * 8);
-  size_t o_cps = take(ncp * 3 * 8), o_w = take(ncp * 8);
-  size_t o_m64 = take(nspan * k12 * 4 * 8), o_m32 = take(nspan * k12 * 4 * 4);
-  size_t o_bas_u = take((size_t)nsu * k1 * k1 * 8), o_bas_v = take((size_t)nsv * k2 * k2 * 8);
-  size_t o_tree = take(kTreeNodes * sizeof(TreeNodeDev));
-  size_t o_div = take(kTreeNodes), o_built = take(kTreeNodes);
-  const size_t total = off;
-
+  if ((rc = fetch(cps, ncp * 3, ptr_kind, hc, st))) return rc;
+  if ((rc = fetch(weights, ncp, ptr_kind, hw, st))) return rc;
+  SurfaceHost S;
+  std::string err;
+  if ((rc = prepare_surface(p, q, nu, nv, ku.data(), kv.data(), hc.data(), hw.data(), S, err)))
+    return fail(rc, "%s", err.c_str());
   nurbs_surface_s* s = new (std::nothrow) nurbs_surface_s();
   if (!s) return fail(NURBS_E_NOMEM, "host allocation failed");
   cudaGetDevice(&s->device);
+  const size_t total = S.in_bytes + S.out_bytes;
   cudaError_t e = cudaMalloc(&s->arena, total);
   if (e != cudaSuccess) {
     delete s;
@@ -194,68 +148,21 @@ int nurbs_surface_create(int p, int q, int nu, int nv, const double* knots_u, co
   }
   s->arena_bytes = total;
   char* A = (char*)s->arena;
-  std::vector<double> idu(nsu), idv(nsv);
-  std::vector<float> bu32(bu.begin(), bu.end()), bv32(bv.begin(), bv.end()), idu32(nsu), idv32(nsv);
-  for (int i = 0; i < nsu; ++i) idu[i] = 1.0 / (bu[i + 1] - bu[i]), idu32[i] = (float)idu[i];
-  for (int i = 0; i < nsv; ++i) idv[i] = 1.0 / (bv[i + 1] - bv[i]), idv32[i] = (float)idv[i];
-
+  std::vector<char> img(S.in_bytes, 0);
+  fill_surface(S, img.data(), A, A + S.in_bytes, s->dev);
   SurfDev& d = s->dev;
-  d.p = p; d.q = q; d.nu = nu; d.nv = nv; d.ns_u = nsu; d.ns_v = nsv;
-  d.range_u = ku[p + nu] - ku[0];  // kernel.cu:167
-  d.range_v = kv[q + nv] - kv[0];
-  d.range_u32 = (float)d.range_u;
-  d.range_v32 = (float)d.range_v;
-  d.dom_u0 = ku[p]; d.dom_u1 = ku[nu]; d.dom_v0 = kv[q]; d.dom_v1 = kv[nv];
-  d.bu = (const double*)(A + o_bu); d.bv = (const double*)(A + o_bv);
-  d.inv_du = (const double*)(A + o_idu); d.inv_dv = (const double*)(A + o_idv);
-  d.bu32 = (const float*)(A + o_bu32); d.bv32 = (const float*)(A + o_bv32);
-  d.inv_du32 = (const float*)(A + o_idu32); d.inv_dv32 = (const float*)(A + o_idv32);
-  d.knot_u = (const int*)(A + o_iu); d.knot_v = (const int*)(A + o_iv);
-  d.knots_u = (const double*)(A + o_ku); d.knots_v = (const double*)(A + o_kv);
-  d.cps = (const double*)(A + o_cps); d.weights = (const double*)(A + o_w);
-  d.m64 = (const double*)(A + o_m64); d.m32 = (const float*)(A + o_m32);
-  d.tree = (TreeNodeDev*)(A + o_tree);
-  d.divided = (unsigned char*)(A + o_div);
-  d.built = (unsigned char*)(A + o_built);
-  s->basis_u = (double*)(A + o_bas_u);
-  s->basis_v = (double*)(A + o_bas_v);
-
-  auto up = [&](size_t o, const void* src, size_t bytes) {
-    return cudaMemcpyAsync(A + o, src, bytes, cudaMemcpyHostToDevice, st);
-  };
-  cudaMemcpyKind ck = ptr_kind == NURBS_PTR_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
-  cudaError_t errs[16];
-  int ne = 0;
-  errs[ne++] = up(o_bu, bu.data(), bu.size() * 8);
-  errs[ne++] = up(o_bv, bv.data(), bv.size() * 8);
-  errs[ne++] = up(o_idu, idu.data(), nsu * 8);
-  errs[ne++] = up(o_idv, idv.data(), nsv * 8);
-  errs[ne++] = up(o_bu32, bu32.data(), bu32.size() * 4);
-  errs[ne++] = up(o_bv32, bv32.data(), bv32.size() * 4);
-  errs[ne++] = up(o_idu32, idu32.data(), nsu * 4);
-  errs[ne++] = up(o_idv32, idv32.data(), nsv * 4);
-  errs[ne++] = up(o_iu, iu.data(), nsu * 4);
-  errs[ne++] = up(o_iv, iv.data(), nsv * 4);
-  errs[ne++] = up(o_ku, ku.data(), ku.size() * 8);
-  errs[ne++] = up(o_kv, kv.data(), kv.size() * 8);
-  errs[ne++] = cudaMemcpyAsync(A + o_cps, cps, ncp * 3 * 8, ck, st);
-  errs[ne++] = cudaMemcpyAsync(A + o_w, weights, ncp * 8, ck, st);
-  errs[ne++] = cudaMemsetAsync(A + o_tree, 0, o_built + kTreeNodes - o_tree, st);
-  for (int i = 0; i < ne; ++i)
-    if (errs[i] != cudaSuccess) {
-      cudaFree(s->arena);
-      delete s;
-      return cuda_fail(errs[i], "surface upload");
-    }
-  cudaError_t le = launch_basis(d.knots_u, p, d.knot_u, nsu, s->basis_u, st);
-  if (le == cudaSuccess) le = launch_basis(d.knots_v, q, d.knot_v, nsv, s->basis_v, st);
-  if (le == cudaSuccess) le = launch_span_matrices(d, s->basis_u, s->basis_v, (double*)d.m64, (float*)d.m32, st);
-  if (le == cudaSuccess) le = launch_tree(d, st);
-  if (le == cudaSuccess) le = cudaStreamSynchronize(st);
-  if (le != cudaSuccess) {
+  s->basis_u = d.basis_u;
+  s->basis_v = d.basis_v;
+  e = cudaMemcpyAsync(A, img.data(), S.in_bytes, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = launch_basis(d.knots_u, p, d.knot_u, d.ns_u, s->basis_u, st);
+  if (e == cudaSuccess) e = launch_basis(d.knots_v, q, d.knot_v, d.ns_v, s->basis_v, st);
+  if (e == cudaSuccess) e = launch_span_matrices(d, s->basis_u, s->basis_v, (double*)d.m64, (float*)d.m32, st);
+  if (e == cudaSuccess) e = launch_tree(d, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // img must outlive the copy
+  if (e != cudaSuccess) {
     cudaFree(s->arena);
     delete s;
-    return cuda_fail(le, "matrix-form conversion");
+    return cuda_fail(e, "matrix-form conversion");
   }
   s->tree_built = true;
   *out = s;

@@ -18,15 +18,9 @@
 namespace gnurbs {
 
 // Nrc table for one span and one column c (1-based), see nurbs_oracle.c span_basis_matrix.
-// N[r-1][c-1] = Nrc(knot, d, r, c, I, I, d), I = span - (d-1).
-__global__ void k_basis(const double* __restrict__ knot, int d, const int* __restrict__ knot_idx,
-                        int nspans, double* __restrict__ basis) {
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
-  int k = d + 1;
-  if (t >= nspans * k) return;
-  int sidx = t / k;
-  int c = t % k + 1;
-  const int span = knot_idx[sidx];
+// N[r-1][c-1] = Nrc(knot, d, r, c, I, I, d), I = span - (d-1); out is the span's (d+1)^2 matrix.
+__device__ void basis_column(const double* __restrict__ knot, int d, int span, int c, double* __restrict__ out) {
+  const int k = d + 1;
   const int I = span - (d - 1);
   const int R0 = 1 - d, RN = 2 * d + 1;
   const int J0 = I - d, JN = d + 1;
@@ -57,18 +51,40 @@ __global__ void k_basis(const double* __restrict__ knot, int d, const int* __res
     for (int r = 1 - (d - m); r <= d + 1; ++r)
       for (int j = I - (d - m); j <= I; ++j) prev[(r - R0) * JN + (j - J0)] = cur[(r - R0) * JN + (j - J0)];
   }
-  double* out = basis + (size_t)sidx * k * k;
   for (int r = 1; r <= d + 1; ++r) out[(r - 1) * k + (c - 1)] = prev[(r - R0) * JN + (I - J0)];
 }
 
-// out_c = Nu . (Mid_c . NvT), one thread per (span, component).  Dense output (m64/m32) or,
-// when ref_out != nullptr, the reference MatrixN layout.
-__global__ void k_span_matrices(SurfDev s, const double* __restrict__ basis_u, const double* __restrict__ basis_v,
-                                double* __restrict__ m64, float* __restrict__ m32, double* __restrict__ ref_out) {
+__global__ void k_basis(const double* __restrict__ knot, int d, const int* __restrict__ knot_idx, int nspans,
+                        double* __restrict__ basis) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
-  int nsp = s.ns_u * s.ns_v;
-  if (t >= nsp * 4) return;
-  int span = t >> 2, c = t & 3;
+  int k = d + 1;
+  if (t >= nspans * k) return;
+  int sidx = t / k;
+  basis_column(knot, d, knot_idx[sidx], t % k + 1, basis + (size_t)sidx * k * k);
+}
+
+// Batched over many (surface, direction) jobs: item t belongs to the job with the largest item0 <= t.
+__global__ void k_basis_batched(const BasisJob* __restrict__ jobs, int njobs, int64_t nitems) {
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nitems) return;
+  int lo = 0, hi = njobs - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (jobs[mid].item0 <= t) lo = mid;
+    else hi = mid - 1;
+  }
+  const BasisJob J = jobs[lo];
+  const int k = J.degree + 1;
+  int64_t local = t - J.item0;
+  int sidx = (int)(local / k);
+  basis_column(J.knots, J.degree, J.knot_idx[sidx], (int)(local % k) + 1, J.out + (size_t)sidx * k * k);
+}
+
+// out_c = Nu . (Mid_c . NvT) for one (span, component).  Dense output (m64/m32) or, when
+// ref_out != nullptr, the reference MatrixN layout.
+__device__ void span_component(const SurfDev& s, const double* __restrict__ basis_u,
+                               const double* __restrict__ basis_v, int span, int c, double* __restrict__ m64,
+                               float* __restrict__ m32, double* __restrict__ ref_out) {
   int su = span / s.ns_v, sv = span % s.ns_v;
   const int p = s.p, q = s.q, k1 = p + 1, k2 = q + 1;
   const int i = s.knot_u[su], j = s.knot_v[sv];
@@ -106,6 +122,29 @@ __global__ void k_span_matrices(SurfDev s, const double* __restrict__ basis_u, c
     }
 }
 
+__global__ void k_span_matrices(SurfDev s, const double* __restrict__ basis_u, const double* __restrict__ basis_v,
+                                double* __restrict__ m64, float* __restrict__ m32, double* __restrict__ ref_out) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= s.ns_u * s.ns_v * 4) return;
+  span_component(s, basis_u, basis_v, t >> 2, t & 3, m64, m32, ref_out);
+}
+
+__global__ void k_span_matrices_batched(const SurfDev* __restrict__ table, const SpanJob* __restrict__ jobs,
+                                        int njobs, int64_t nitems) {
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nitems) return;
+  int lo = 0, hi = njobs - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (jobs[mid].item0 <= t) lo = mid;
+    else hi = mid - 1;
+  }
+  const SurfDev s = table[jobs[lo].surf];
+  int64_t local = t - jobs[lo].item0;
+  span_component(s, s.basis_u, s.basis_v, (int)(local >> 2), (int)(local & 3), const_cast<double*>(s.m64),
+                 const_cast<float*>(s.m32), nullptr);
+}
+
 // Dense -> reference MatrixN layout, one thread per double.
 __global__ void k_export_ref(SurfDev s, double* __restrict__ ref_out) {
   const int k1 = s.p + 1, k2 = s.q + 1, k12 = k1 * k2;
@@ -137,6 +176,19 @@ cudaError_t launch_span_matrices(const SurfDev& s, const double* basis_u, const 
   double* ref_out = (m32 == nullptr) ? m64 : nullptr;
   k_span_matrices<<<(threads + 127) / 128, 128, 0, st>>>(s, basis_u, basis_v, ref_out ? nullptr : m64, m32,
                                                           ref_out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_basis_batched(const BasisJob* jobs, int njobs, int64_t nitems, cudaStream_t st) {
+  if (nitems <= 0) return cudaSuccess;
+  k_basis_batched<<<(unsigned)((nitems + 127) / 128), 128, 0, st>>>(jobs, njobs, nitems);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_span_matrices_batched(const SurfDev* table, const SpanJob* jobs, int njobs, int64_t nitems,
+                                         cudaStream_t st) {
+  if (nitems <= 0) return cudaSuccess;
+  k_span_matrices_batched<<<(unsigned)((nitems + 127) / 128), 128, 0, st>>>(table, jobs, njobs, nitems);
   return cudaGetLastError();
 }
 

@@ -28,533 +28,25 @@
 //           residual |S - P| at the returned point in FP64.  Extra FP64 steps (at most 4) run
 //           only when the second step is not yet below tolerance (near-singular or boundary
 //           cases).
-#include <type_traits>
-
-#include "nurbs_internal.h"
-#include "nurbs_math.cuh"
+#include "invert_core.cuh"
 
 namespace gnurbs {
-
 namespace {
 
-constexpr int kModeFP64 = 0;
-constexpr int kModeMixed = 1;
-
-constexpr int kWarps = 4;          // warps per CTA
-constexpr int kThreads = 32 * kWarps;
-constexpr int kMinBlocksMixed = 4;  // CTAs per SM the mixed kernel is register-budgeted for
-  // CTAs per SM the mixed kernel is register-budgeted for
-  // CTAs per SM the mixed kernel is register-budgeted for
-constexpr int kMaxIter32 = 24;     // FP32 iterations per seed
-constexpr int kMaxIter64 = 40;     // FP64-mode iterations per seed
-constexpr int kMaxFinal64 = 6;     // MIXED: FP64 steps (2 normally)
-constexpr double kNewtonSwitch = 1e-2;  // GN while the step is larger, Newton below
-constexpr float kTol32 = 3e-7f;
-constexpr double kTolNewton64 = 1e-10;  // a Newton step this small leaves < 1e-19 error
-constexpr double kTolAny64 = 1e-14;
-constexpr double kDistinct = 1e-7;      // two FP64 solutions are the same minimum within this
-constexpr float kDistinct32 = 1e-4f;    // ... two FP32 solutions
-constexpr float kJoin = 1e-3f;          // a Newton iterate this close to a known minimum joins it
-constexpr int kSols = 4;                // FP64 mode: distinct minima kept per query
-constexpr int kSmemSpans = 256;         // breakpoint tables staged in shared memory up to this
-
-template <typename T>
-__device__ __forceinline__ T dot3(const v3<T>& a, const v3<T>& b) {
-  return a.x * b.x + a.y * b.y + a.z * b.z;
-}
-
-// One (Gauss-)Newton step from the derivatives at C.  Returns false when the system is
-// singular.  Newton uses H = J^T J + r.d2S when that H is positive definite.
-template <typename T, typename TH>
-__device__ __forceinline__ bool solve_step(const v3<T>& r, const v3<T>& Su, const v3<T>& Sv, const v3<TH>& Suu,
-                                           const v3<TH>& Suv, const v3<TH>& Svv, bool newton, T& du, T& dv) {
-  T a00 = dot3(Su, Su), a01 = dot3(Su, Sv), a11 = dot3(Sv, Sv);
-  T g0 = dot3(Su, r), g1 = dot3(Sv, r);
-  if (newton) {
-    T h00 = a00 + (T)(r.x * (T)Suu.x + r.y * (T)Suu.y + r.z * (T)Suu.z);
-    T h01 = a01 + (T)(r.x * (T)Suv.x + r.y * (T)Suv.y + r.z * (T)Suv.z);
-    T h11 = a11 + (T)(r.x * (T)Svv.x + r.y * (T)Svv.y + r.z * (T)Svv.z);
-    T det = h00 * h11 - h01 * h01;
-    if (h00 > T(0) && det > T(0)) {
-      du = (h11 * g0 - h01 * g1) / det;
-      dv = (h00 * g1 - h01 * g0) / det;
-      return true;
-    }
-  }
-  T det = a00 * a11 - a01 * a01;
-  if (!(det > T(0))) return false;
-  du = (a11 * g0 - a01 * g1) / det;
-  dv = (a00 * g1 - a01 * g0) / det;
-  return true;
-}
-
-// Where one kernel finds the span tables: breakpoints in shared memory when they fit.
-struct Ctx {
-  fast::Locator<float> L32;
-  fast::Locator<double> L64;
-  const float* m32;
-  const double* m64;
-  int p, q;
-  double dom_u0, dom_u1, dom_v0, dom_v1;
-};
-
-// Per-seed iteration state (hu/hv: span hints for the warm-started span search).
-template <typename T>
-struct Seed {
-  T u, v, prev;
-  int it, hu, hv;
-  bool newton;
-};
-
-enum StepResult { kContinue = 0, kConverged = 1, kFailed = 2 };
-
-// One FP32 iteration of a seed.  Convergence: the step is at the FP32 resolution of the
-// parameters (rounding of S mapped through the shorter tangent), or Newton steps stop shrinking.
-template <int P, int Q>
-__device__ __forceinline__ int iterate32(const Ctx& c, float px, float py, float pz, Seed<float>& st, float& dist) {
-  fast::SDer<float> d = fast::eval_at<float, P, Q, 2>(c.L32, c.m32, c.p, c.q, st.u, st.v, st.hu, st.hv);
-  v3<float> r = {d.S.x - px, d.S.y - py, d.S.z - pz};
-  float du, dv;
-  if (!solve_step<float, float>(r, d.Su, d.Sv, d.Suu, d.Suv, d.Svv, st.newton, du, dv)) return kFailed;
-  if (!(isfinite(du) && isfinite(dv))) return kFailed;
-  st.u -= du;
-  st.v -= dv;
-  float step = fmaxf(fabsf(du), fabsf(dv));
-  dist = sqrtf(dot3(r, r));
-  float smag = fmaxf(fmaxf(fabsf(d.S.x), fabsf(d.S.y)), fmaxf(fabsf(d.S.z), 1.0f));
-  float tmin = sqrtf(fminf(dot3(d.Su, d.Su), dot3(d.Sv, d.Sv)));
-  float floor32 = 8.0f * 5.96e-8f * smag / fmaxf(tmin, 1e-30f);
-  if (step <= fmaxf(kTol32, floor32)) return kConverged;
-  if (st.newton && step < 1e-4f && step > 0.5f * st.prev) return kConverged;
-  st.prev = step;
-  st.newton = step < (float)kNewtonSwitch;
-  if (++st.it >= kMaxIter32) return kFailed;
-  return kContinue;
-}
-
-// One FP64 iteration of a seed (FP64 mode).
-template <int P, int Q>
-__device__ __forceinline__ int iterate64(const Ctx& c, double px, double py, double pz, Seed<double>& st) {
-  fast::SDer<double> d = fast::eval_at<double, P, Q, 2>(c.L64, c.m64, c.p, c.q, st.u, st.v, st.hu, st.hv);
-  v3<double> r = {d.S.x - px, d.S.y - py, d.S.z - pz};
-  double du, dv;
-  if (!solve_step<double, double>(r, d.Su, d.Sv, d.Suu, d.Suv, d.Svv, st.newton, du, dv)) return kFailed;
-  if (!(isfinite(du) && isfinite(dv))) return kFailed;
-  st.u -= du;
-  st.v -= dv;
-  double step = fmax(fabs(du), fabs(dv));
-  if ((st.newton && step <= kTolNewton64) || step <= kTolAny64) return kConverged;
-  st.prev = step;
-  st.newton = step < kNewtonSwitch;
-  if (++st.it >= kMaxIter64) return kFailed;
-  return kContinue;
-}
-
-// FP64 residual at (u,v), with the domain test.
-template <int P, int Q>
-__device__ __forceinline__ bool finish64(const Ctx& c, double px, double py, double pz, double u, double v,
-                                         int hu, int hv, double& res) {
-  fast::SDer<double> d = fast::eval_at<double, P, Q, 0>(c.L64, c.m64, c.p, c.q, u, v, hu, hv);
-  v3<double> r = {d.S.x - px, d.S.y - py, d.S.z - pz};
-  res = sqrt(dot3(r, r));
-  return (u >= c.dom_u0 && u <= c.dom_u1 && v >= c.dom_v0 && v <= c.dom_v1) && isfinite(res);
-}
-
-// MIXED: the final FP64 Newton steps from an FP32 minimum, then the residual.
-template <int P, int Q>
-__device__ bool final64(const Ctx& c, double px, double py, double pz, double& u, double& v, double& res) {
-  int hu = 0, hv = 0, hu32 = 0, hv32 = 0;
-  for (int it = 0; it < kMaxFinal64; ++it) {
-    fast::SDer<double> d = fast::eval_at<double, P, Q, 1>(c.L64, c.m64, c.p, c.q, u, v, hu, hv);
-    fast::SDer<float> e = fast::eval_at<float, P, Q, 2>(c.L32, c.m32, c.p, c.q, (float)u, (float)v, hu32, hv32);
-    v3<double> r = {d.S.x - px, d.S.y - py, d.S.z - pz};
-    double du, dv;
-    if (!solve_step<double, float>(r, d.Su, d.Sv, e.Suu, e.Suv, e.Svv, true, du, dv)) return false;
-    if (!(isfinite(du) && isfinite(dv))) return false;
-    u -= du;
-    v -= dv;
-    if (fmax(fabs(du), fabs(dv)) <= kTolNewton64) return finish64<P, Q>(c, px, py, pz, u, v, hu, hv, res);
-  }
-  return false;
-}
-
-struct Rec32 {  // per-query FP32 record: best and best distinct runner-up
-  float u1, v1, d1, u2, v2, d2;
-};
-struct Rec64 {  // per-query FP64 record: distinct minima
-  double u[kSols], v[kSols], r[kSols];
-  int n;
-};
-
-__device__ __forceinline__ void merge32(Rec32& R, float u, float v, float d) {
-  bool same1 = R.d1 < INFINITY && fabsf(u - R.u1) <= kDistinct32 && fabsf(v - R.v1) <= kDistinct32;
-  if (same1) {
-    if (d < R.d1) { R.u1 = u; R.v1 = v; R.d1 = d; }
-  } else if (d < R.d1) {
-    R.u2 = R.u1; R.v2 = R.v1; R.d2 = R.d1;
-    R.u1 = u; R.v1 = v; R.d1 = d;
-  } else if (d < R.d2) {
-    R.u2 = u; R.v2 = v; R.d2 = d;
-  }
-}
-
-__device__ __forceinline__ void merge64(Rec64& R, double u, double v, double r) {
-  for (int k = 0; k < R.n; ++k)
-    if (fabs(R.u[k] - u) <= kDistinct && fabs(R.v[k] - v) <= kDistinct) {
-      if (r < R.r[k]) { R.u[k] = u; R.v[k] = v; R.r[k] = r; }
-      return;
-    }
-  int slot = R.n;
-  if (R.n >= kSols) {
-    slot = 0;
-    for (int k = 1; k < kSols; ++k)
-      if (R.r[k] > R.r[slot]) slot = k;
-    if (!(r < R.r[slot])) return;
-  } else {
-    ++R.n;
-  }
-  R.u[slot] = u; R.v[slot] = v; R.r[slot] = r;
-}
-
-// best minimum and status (FOUND / AMBIGUOUS), as the oracle decides them
-__device__ __forceinline__ int finish_status(const double* us, const double* vs, const double* rs, int n, double& u,
-                                             double& v, double& r) {
-  int bi = 0;
-  for (int k = 1; k < n; ++k)
-    if (rs[k] < rs[bi]) bi = k;
-  u = us[bi];
-  v = vs[bi];
-  r = rs[bi];
-  for (int k = 0; k < n; ++k)
-    if (k != bi && rs[k] <= r * (1 + 1e-6) + 1e-12) return 1;  // NURBS_INV_AMBIGUOUS
-  return 0;
-}
+using namespace inv;
 
 template <int P, int Q, int MODE>
-__global__ void __launch_bounds__(kThreads, MODE == kModeMixed ? kMinBlocksMixed : 4) k_invert(SurfDev s, const double* __restrict__ Pq, int64_t n,
-                                                     double* __restrict__ uv_out, int* __restrict__ st_out,
-                                                     double* __restrict__ res_out) {
-  __shared__ float box32[kTreeNodes][6];
-  __shared__ double box64[kTreeNodes][6];
-  __shared__ double ctr[kTreeNodes][2];
-  __shared__ float ctr32[kTreeNodes][2];
-  __shared__ float dom32[4];
-  __shared__ int nb;
-  __shared__ unsigned long long smask0[kWarps][32];
-  __shared__ unsigned char smask1[kWarps][32];
-  __shared__ unsigned srmask[kWarps][kTreeNodes];
-  __shared__ int srpref[kWarps][kTreeNodes + 1];
-  __shared__ int slpref[kWarps][32];
-  __shared__ typename std::conditional<MODE == kModeMixed, Rec32, Rec64>::type rec[kWarps][32];
-  __shared__ float sp32[kWarps][32][3];
-  __shared__ double sp64[kWarps][32][3];
-  __shared__ float sb32[2][kSmemSpans + 1], si32[2][kSmemSpans];
-  __shared__ double sb64[2][kSmemSpans + 1], si64[2][kSmemSpans];
-  const bool smem_tables = s.ns_u <= kSmemSpans && s.ns_v <= kSmemSpans;
-  if (smem_tables) {
-    for (int k = threadIdx.x; k <= s.ns_u; k += blockDim.x) {
-      sb32[0][k] = s.bu32[k];
-      sb64[0][k] = s.bu[k];
-      if (k < s.ns_u) { si32[0][k] = s.inv_du32[k]; si64[0][k] = s.inv_du[k]; }
-    }
-    for (int k = threadIdx.x; k <= s.ns_v; k += blockDim.x) {
-      sb32[1][k] = s.bv32[k];
-      sb64[1][k] = s.bv[k];
-      if (k < s.ns_v) { si32[1][k] = s.inv_dv32[k]; si64[1][k] = s.inv_dv[k]; }
-    }
-  }
+__global__ void __launch_bounds__(kThreads, MODE == kModeMixed ? kMinBlocksMixed : 4)
+    k_invert(SurfDev s, const double* __restrict__ Pq, int64_t n, double* __restrict__ uv_out,
+             int* __restrict__ st_out, double* __restrict__ res_out) {
+  __shared__ InvSmem<MODE> sm;
   Ctx cx;
-  cx.L32 = fast::global_locator<float>(s);
-  cx.L64 = fast::global_locator<double>(s);
-  if (smem_tables) {
-    cx.L32.bu = sb32[0]; cx.L32.bv = sb32[1]; cx.L32.iu = si32[0]; cx.L32.iv = si32[1];
-    cx.L64.bu = sb64[0]; cx.L64.bv = sb64[1]; cx.L64.iu = si64[0]; cx.L64.iv = si64[1];
-  }
-  cx.m32 = s.m32;
-  cx.m64 = s.m64;
-  cx.p = s.p;
-  cx.q = s.q;
-  cx.dom_u0 = s.dom_u0; cx.dom_u1 = s.dom_u1; cx.dom_v0 = s.dom_v0; cx.dom_v1 = s.dom_v1;
-  if (threadIdx.x == 0) {
-    int c = 0;
-    for (int k = 0; k < kTreeNodes; ++k) {
-      if (!s.built[k]) continue;
-      const TreeNodeDev& T = s.tree[k];
-      for (int j = 0; j < 3; ++j) {
-        box64[c][j] = T.lb[j];
-        box64[c][3 + j] = T.rt[j];
-        box32[c][j] = __double2float_rd(T.lb[j]);
-        box32[c][3 + j] = __double2float_ru(T.rt[j]);
-      }
-      ctr[c][0] = (T.uv_lb[0] + T.uv_rt[0]) / 2;  // kernel.cu:154
-      ctr[c][1] = (T.uv_lb[1] + T.uv_rt[1]) / 2;
-      ctr32[c][0] = (float)ctr[c][0];
-      ctr32[c][1] = (float)ctr[c][1];
-      ++c;
-    }
-    nb = c;
-    const float slack = 1e-4f;  // FP32 domain test is a prefilter; the FP64 phase decides
-    dom32[0] = (float)s.dom_u0 - slack;
-    dom32[1] = (float)s.dom_u1 + slack;
-    dom32[2] = (float)s.dom_v0 - slack;
-    dom32[3] = (float)s.dom_v1 + slack;
-  }
+  stage_surface<MODE>(s, sm, cx);
   __syncthreads();
-  const int nbl = nb;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const unsigned FULL = 0xffffffffu;
-  const unsigned lt_mask = (1u << lane) - 1u;
+  const int warp = threadIdx.x >> 5;
   const int64_t chunks = (n + 31) / 32;
-  for (int64_t ch = (int64_t)blockIdx.x * kWarps + warp; ch < chunks; ch += (int64_t)gridDim.x * kWarps) {
-    const int64_t q = ch * 32 + lane;
-    const bool valid = q < n;
-    double px = 0, py = 0, pz = 0;
-    if (valid) {
-      px = Pq[3 * q];
-      py = Pq[3 * q + 1];
-      pz = Pq[3 * q + 2];
-    }
-    const float fx = (float)px, fy = (float)py, fz = (float)pz;
-    // ---- cull (exact candidate set, ascending node order)
-    uint64_t m0 = 0;
-    unsigned m1 = 0;
-    if (valid) {
-      for (int k = 0; k < nbl; ++k) {
-        if (fx >= box32[k][0] && fy >= box32[k][1] && fz >= box32[k][2] && fx <= box32[k][3] &&
-            fy <= box32[k][4] && fz <= box32[k][5]) {
-          if (px >= box64[k][0] && py >= box64[k][1] && pz >= box64[k][2] && px <= box64[k][3] &&
-              py <= box64[k][4] && pz <= box64[k][5]) {
-            if (k < 64) m0 |= 1ull << k;
-            else m1 = 1u;
-          }
-        }
-      }
-    }
-    const int cnt = __popcll(m0) + (int)m1;
-    // Task list in round-major order: round r holds seed r of every query that has more than
-    // r seeds, so each query's first seeds run first and its later seeds can join the minima
-    // those found.  rmask[r] = lanes with a seed in round r, rpref[r] = tasks before round r.
-    const int maxc = __reduce_max_sync(FULL, (unsigned)cnt);
-    int total = 0;
-    for (int r = 0; r < maxc; ++r) {
-      unsigned m = __ballot_sync(FULL, cnt > r);
-      if (lane == 0) {
-        srmask[warp][r] = m;
-        srpref[warp][r] = total;
-      }
-      total += __popc(m);
-    }
-    if (lane == 0) srpref[warp][maxc] = total;
-    if constexpr (MODE == kModeMixed) {
-      int incl = cnt;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        int t = __shfl_up_sync(FULL, incl, o);
-        if (lane >= o) incl += t;
-      }
-      slpref[warp][lane] = incl - cnt;
-    }
-    sp32[warp][lane][0] = fx;
-    sp32[warp][lane][1] = fy;
-    sp32[warp][lane][2] = fz;
-    sp64[warp][lane][0] = px;
-    sp64[warp][lane][1] = py;
-    sp64[warp][lane][2] = pz;
-    smask0[warp][lane] = m0;
-    smask1[warp][lane] = (unsigned char)m1;
-    if constexpr (MODE == kModeMixed) {
-      Rec32& R = rec[warp][lane];
-      R.d1 = INFINITY;
-      R.d2 = INFINITY;
-      R.u1 = R.v1 = R.u2 = R.v2 = 0.f;
-    } else {
-      rec[warp][lane].n = 0;
-    }
-    __syncwarp();
-
-    // decode task t -> (owner lane, node)
-    auto decode = [&](int t, int& ql, int& node) {
-      if constexpr (MODE == kModeMixed) {
-        // lane-major: the largest lane whose exclusive prefix is <= t owns task t (a lane with
-        // no candidates shares its prefix with the next lane and is never the largest)
-        int lo = 0;
-#pragma unroll
-        for (int step = 16; step > 0; step >>= 1)
-          if (slpref[warp][lo + step] <= t) lo += step;
-        ql = lo;
-        uint64_t mm = smask0[warp][ql];
-        int k = t - slpref[warp][lo];
-        if (k < __popcll(mm)) {
-          for (int i = 0; i < k; ++i) mm &= mm - 1;
-          node = __ffsll((long long)mm) - 1;
-        } else {
-          node = 64;
-        }
-        return;
-      }
-      // round: the largest r with rpref[r] <= t (rounds are non-empty, so rpref is increasing)
-      int r = 0;
-#pragma unroll
-      for (int step = 64; step > 0; step >>= 1)
-        if (r + step < maxc && srpref[warp][r + step] <= t) r += step;
-      // lane: the (t - rpref[r])-th set bit of rmask[r]
-      const unsigned m = srmask[warp][r];
-      int i = t - srpref[warp][r], pos = 0;
-#pragma unroll
-      for (int w = 16; w > 0; w >>= 1)
-        if (__popc(m & ((1u << (pos + w)) - 1u)) <= i) pos += w;
-      ql = pos;
-      int k = r;  // seed r of that query: its r-th candidate node in ascending order
-      uint64_t mm = smask0[warp][ql];
-      int c0 = __popcll(mm);
-      if (k < c0) {
-        for (int i = 0; i < k; ++i) mm &= mm - 1;
-        node = __ffsll((long long)mm) - 1;
-      } else {
-        node = 64;
-      }
-    };
-
-    int next = 32;
-    int task = lane;
-    bool active = task < total;
-    int ql = 0, node = 0;
-    if constexpr (MODE == kModeMixed) {
-      Seed<float> sd;
-      float dist = 0.f;
-      float tx = 0, ty = 0, tz = 0;
-      auto start = [&]() {
-        decode(task, ql, node);
-        tx = sp32[warp][ql][0];
-        ty = sp32[warp][ql][1];
-        tz = sp32[warp][ql][2];
-        sd.u = ctr32[node][0];
-        sd.v = ctr32[node][1];
-        sd.prev = INFINITY;
-        sd.it = 0;
-        sd.hu = 0;
-        sd.hv = 0;
-        sd.newton = false;
-      };
-      if (active) start();
-      while (__any_sync(FULL, active)) {
-        int res = kContinue;
-        if (active) {
-          res = iterate32<P, Q>(cx, tx, ty, tz, sd, dist);
-          if (res == kContinue && sd.newton) {
-            const Rec32& R = rec[warp][ql];
-            if ((R.d1 < INFINITY && fabsf(sd.u - R.u1) <= kJoin && fabsf(sd.v - R.v1) <= kJoin) ||
-                (R.d2 < INFINITY && fabsf(sd.u - R.u2) <= kJoin && fabsf(sd.v - R.v2) <= kJoin))
-              res = kFailed;  // joins a minimum already found: nothing new
-          }
-        }
-        const bool done = active && res != kContinue;
-        const bool keep = res == kConverged && sd.u >= dom32[0] && sd.u <= dom32[1] && sd.v >= dom32[2] &&
-                          sd.v <= dom32[3];
-        __syncwarp();
-        unsigned fm = __ballot_sync(FULL, done && keep);
-        while (fm) {
-          int j = __ffs(fm) - 1;
-          if (lane == j) merge32(rec[warp][ql], sd.u, sd.v, dist);
-          __syncwarp();
-          fm &= fm - 1;
-        }
-        unsigned dm = __ballot_sync(FULL, done);
-        if (done) {
-          task = next + __popc(dm & lt_mask);
-          active = task < total;
-          if (active) start();
-        }
-        next += __popc(dm);
-      }
-    } else {
-      Seed<double> sd;
-      double tx = 0, ty = 0, tz = 0;
-      auto start = [&]() {
-        decode(task, ql, node);
-        tx = sp64[warp][ql][0];
-        ty = sp64[warp][ql][1];
-        tz = sp64[warp][ql][2];
-        sd.u = ctr[node][0];
-        sd.v = ctr[node][1];
-        sd.prev = INFINITY;
-        sd.it = 0;
-        sd.hu = 0;
-        sd.hv = 0;
-        sd.newton = false;
-      };
-      if (active) start();
-      while (__any_sync(FULL, active)) {
-        int res = kContinue;
-        double rr = 0;
-        bool keep = false;
-        if (active) {
-          res = iterate64<P, Q>(cx, tx, ty, tz, sd);
-          if (res == kContinue && sd.newton) {
-            const Rec64& R = rec[warp][ql];
-            for (int k = 0; k < R.n; ++k)
-              if (fabs(sd.u - R.u[k]) <= kJoin && fabs(sd.v - R.v[k]) <= kJoin) res = kFailed;
-          }
-          if (res == kConverged) keep = finish64<P, Q>(cx, tx, ty, tz, sd.u, sd.v, sd.hu, sd.hv, rr);
-        }
-        const bool done = active && res != kContinue;
-        __syncwarp();
-        unsigned fm = __ballot_sync(FULL, done && keep);
-        while (fm) {
-          int j = __ffs(fm) - 1;
-          if (lane == j) merge64(rec[warp][ql], sd.u, sd.v, rr);
-          __syncwarp();
-          fm &= fm - 1;
-        }
-        unsigned dm = __ballot_sync(FULL, done);
-        if (done) {
-          task = next + __popc(dm & lt_mask);
-          active = task < total;
-          if (active) start();
-        }
-        next += __popc(dm);
-      }
-    }
-    __syncwarp();
-
-    // ---- per query: final FP64 steps (MIXED) and the result
-    int status;
-    double ou = __longlong_as_double(0x7ff8000000000000ll), ov = ou, orr = ou;
-    if (cnt == 0) {
-      status = 2;  // NURBS_INV_NO_CANDIDATE
-    } else if constexpr (MODE == kModeMixed) {
-      const Rec32 R = rec[warp][lane];
-      double us[2], vs[2], rs[2];
-      int ns = 0;
-      if (R.d1 < INFINITY) {
-        double u = R.u1, v = R.v1, r;
-        bool ok1 = final64<P, Q>(cx, px, py, pz, u, v, r);
-        if (ok1) { us[ns] = u; vs[ns] = v; rs[ns] = r; ++ns; }
-        if (R.d2 < INFINITY && (!ok1 || R.d2 <= R.d1 * 1.001f + 1e-5f)) {
-          double u2 = R.u2, v2 = R.v2, r2;
-          if (final64<P, Q>(cx, px, py, pz, u2, v2, r2)) {
-            bool same = ns == 1 && fabs(u2 - us[0]) <= kDistinct && fabs(v2 - vs[0]) <= kDistinct;
-            if (same) {
-              if (r2 < rs[0]) { us[0] = u2; vs[0] = v2; rs[0] = r2; }
-            } else {
-              us[ns] = u2; vs[ns] = v2; rs[ns] = r2; ++ns;
-            }
-          }
-        }
-      }
-      status = ns == 0 ? 3 : finish_status(us, vs, rs, ns, ou, ov, orr);
-    } else {
-      const Rec64& R = rec[warp][lane];
-      status = R.n == 0 ? 3 : finish_status(R.u, R.v, R.r, R.n, ou, ov, orr);
-    }
-    if (valid) {
-      uv_out[2 * q] = ou;
-      uv_out[2 * q + 1] = ov;
-      st_out[q] = status;
-      res_out[q] = orr;
-    }
-    __syncwarp();
-  }
+  for (int64_t ch = (int64_t)blockIdx.x * kWarps + warp; ch < chunks; ch += (int64_t)gridDim.x * kWarps)
+    invert_chunk<P, Q, MODE>(sm, cx, Pq, ch * 32, n, uv_out, st_out, res_out);
 }
 
 template <int P, int Q>

@@ -21,9 +21,9 @@ __device__ __forceinline__ bool need_divide(const TreeNodeDev& n) {  // kernel.c
   return true;
 }
 
-__global__ void __launch_bounds__(96) k_tree_level(SurfDev s, int level) {
+// One node of the given level for CTA index blk (block linear index bx*g + by); 96 threads.
+__device__ __forceinline__ void tree_node(const SurfDev& s, int level, unsigned blk) {
   const unsigned g = level == 0 ? 1u : (unsigned)kGap;
-  const unsigned blk = blockIdx.x;
   const unsigned bx = blk / g, by = blk % g;
   const int tree_index = level == 0 ? 0 : 1 + (int)blk;
   if (level == 1 && !s.divided[0]) {  // parent not divided: node not built
@@ -106,6 +106,15 @@ __global__ void __launch_bounds__(96) k_tree_level(SurfDev s, int level) {
   }
 }
 
+__global__ void __launch_bounds__(96) k_tree_level(SurfDev s, int level) { tree_node(s, level, blockIdx.x); }
+
+// Many surfaces: blockIdx.y selects the surface of ids[] in the device table.
+__global__ void __launch_bounds__(96) k_tree_level_batched(const SurfDev* __restrict__ table,
+                                                            const int* __restrict__ ids, int level) {
+  const SurfDev s = table[ids[blockIdx.y]];
+  tree_node(s, level, blockIdx.x);
+}
+
 // NewInverse's scan (kernel.cu:456-457) over built nodes, NewBoundingBoxCheck (:466-469).
 __global__ void k_candidates(SurfDev s, const double* __restrict__ P, int64_t n, int* __restrict__ list,
                              int* __restrict__ counts) {
@@ -137,6 +146,20 @@ cudaError_t launch_tree(const SurfDev& s, cudaStream_t st) {
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   k_tree_level<<<kGap * kGap, 96, 0, st>>>(s, 1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_tree_batched(const SurfDev* table, const int* ids, int count, cudaStream_t st) {
+  for (int off = 0; off < count; off += 65535) {
+    int c = count - off < 65535 ? count - off : 65535;
+    k_tree_level_batched<<<dim3(1, c), 96, 0, st>>>(table, ids + off, 0);
+  }
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  for (int off = 0; off < count; off += 65535) {
+    int c = count - off < 65535 ? count - off : 65535;
+    k_tree_level_batched<<<dim3(kGap * kGap, c), 96, 0, st>>>(table, ids + off, 1);
+  }
   return cudaGetLastError();
 }
 

@@ -46,6 +46,8 @@ struct SurfDev {
   struct TreeNodeDev* tree;
   unsigned char* divided;
   unsigned char* built;
+  double* basis_u;        // per-span basis-to-power matrices (conversion scratch kept with the surface)
+  double* basis_v;
 };
 
 // Tree node in the reference TreeNode order (src/kernel/kernel.cuh:30-39), 80 bytes.
@@ -73,6 +75,33 @@ cudaError_t launch_evaluate_random(const double* uv, double* xyz, int64_t n, con
 cudaError_t launch_tree(const SurfDev& s, cudaStream_t st);
 cudaError_t launch_candidates(const SurfDev& s, const double* P, int64_t n, int* list, int* counts,
                               cudaStream_t st);
+// batched (pool) variants: surfaces are read from a device table of SurfDev records
+struct BasisJob {        // one (surface, direction): its spans' columns are items [item0, item0 + ns*(d+1))
+  const double* knots;
+  const int* knot_idx;
+  double* out;
+  int degree, nspans;
+  int64_t item0;
+};
+struct SpanJob {         // one surface: its spans x 4 components are items [item0, item0 + 4*ns_u*ns_v)
+  int surf;
+  int64_t item0;
+};
+struct InvTile {         // a range of queries of one surface
+  int surf;
+  int count;
+  int64_t begin;
+};
+cudaError_t launch_basis_batched(const BasisJob* jobs, int njobs, int64_t nitems, cudaStream_t st);
+cudaError_t launch_span_matrices_batched(const SurfDev* table, const SpanJob* jobs, int njobs, int64_t nitems,
+                                         cudaStream_t st);
+cudaError_t launch_tree_batched(const SurfDev* table, const int* ids, int count, cudaStream_t st);
+cudaError_t launch_eval_pool(const SurfDev* table, const InvTile* tiles, int ntiles, const double* uv, int64_t n,
+                             unsigned mask, double* out, cudaStream_t st);
+cudaError_t launch_invert_pool(const SurfDev* table, const InvTile* tiles, int ntiles, int* counter,
+                               const double* P, double* uv, int* status, double* residual, int precision,
+                               int ctas, int tile_warp_chunks, cudaStream_t st);
+
 // stage d
 cudaError_t launch_invert(const SurfDev& s, const double* P, int64_t n, double* uv, int* status,
                           double* residual, int precision, cudaStream_t st);

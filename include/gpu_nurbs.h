@@ -183,6 +183,67 @@ int nurbs_invert(nurbs_surface_t s, const double* P_dev, int64_t n, double* uv_d
 int nurbs_invert_host(nurbs_surface_t s, const double* P_host, int64_t n, double* uv_host, int* status_host,
                       double* residual_host, int precision, void* stream);
 
+/* ------------------------------------------------------------- surface pools */
+/* Many surfaces resident in one device arena under a memory budget, inverted together in one
+ * persistent launch.  No counterpart in the reference (one surface per process); the per
+ * surface work is the same stages a-d as above. */
+typedef struct nurbs_pool_s* nurbs_pool_t;
+typedef struct nurbs_graph_s* nurbs_graph_t;
+
+typedef struct {                   /* host arrays of one surface (layouts as in nurbs_surface_create) */
+    int degree_u, degree_v, cp_u, cp_v;
+    const double* knots_u;
+    const double* knots_v;
+    const double* cps;
+    const double* weights;
+} nurbs_surface_desc;
+
+typedef struct {
+    int64_t budget_bytes, used_bytes;
+    int surfaces, max_surfaces;
+    int tile_queries, ctas_per_sm;  /* current launch configuration */
+} nurbs_pool_info_t;
+
+/* Allocates the whole budget at once; surfaces and workspaces are carved from it. */
+int nurbs_pool_create(int64_t budget_bytes, int max_surfaces, nurbs_pool_t* out);
+int nurbs_pool_destroy(nurbs_pool_t pool);
+/* Uploads and converts `count` surfaces in one batch (one copy, one launch per stage); returns
+ * their ids.  NURBS_E_BUDGET when the budget (or max_surfaces) cannot hold them.  Synchronous. */
+int nurbs_pool_add(nurbs_pool_t pool, int count, const nurbs_surface_desc* descs, void* stream, int* ids_out);
+/* Frees a surface's memory.  Waits for `stream`; work queued on other streams must be done. */
+int nurbs_pool_remove(nurbs_pool_t pool, int id, void* stream);
+int nurbs_pool_info(nurbs_pool_t pool, nurbs_pool_info_t* info);
+/* Device bytes one surface would take (for admission decisions before uploading it). */
+int nurbs_pool_surface_bytes(int degree_u, int degree_v, int cp_u, int cp_v, const double* knots_u,
+                             const double* knots_v, int64_t* bytes);
+const char* nurbs_pool_last_error(void);
+/* Launch configuration: queries per tile (multiple of 32) and persistent CTAs per SM. */
+int nurbs_pool_set_config(nurbs_pool_t pool, int tile_queries, int ctas_per_sm);
+/* Batched inversion.  Queries are grouped by surface: surface ids_host[k] owns the queries
+ * [offsets_host[k], offsets_host[k+1]) of P_dev (3 doubles each); outputs are indexed like P.
+ * Asynchronous on `stream`. */
+int nurbs_pool_invert(nurbs_pool_t pool, int nbatch, const int* ids_host, const int64_t* offsets_host,
+                      const double* P_dev, double* uv_dev, int* status_dev, double* residual_dev, int precision,
+                      void* stream);
+/* Batched FP64 evaluation: surface ids_host[k] evaluates the (u,v) pairs [offsets[k], offsets[k+1])
+ * of uv_dev; out_dev is SoA over all n pairs as in nurbs_eval.  Asynchronous on `stream`. */
+int nurbs_pool_eval(nurbs_pool_t pool, int nbatch, const int* ids_host, const int64_t* offsets_host,
+                    const double* uv_dev, int64_t n, unsigned mask, double* out_dev, void* stream);
+/* Times tile size x CTAs per SM on the batch (or its prefix of at most max_queries queries, 0 =
+ * all), keeps the fastest configuration in the pool and returns it.  With cache_path, a result
+ * cached for the same GPU, precision and batch signature is reused, and new results appended. */
+int nurbs_pool_autotune(nurbs_pool_t pool, int nbatch, const int* ids_host, const int64_t* offsets_host,
+                        const double* P_dev, double* uv_dev, int* status_dev, double* residual_dev, int precision,
+                        int64_t max_queries, const char* cache_path, void* stream, int* best_tile, int* best_ctas,
+                        float* best_ms);
+/* Captures the batched inversion of one batch layout as a CUDA graph (tile list uploaded once);
+ * replay it with nurbs_graph_launch for new query values in the same buffers. */
+int nurbs_pool_graph_create(nurbs_pool_t pool, int nbatch, const int* ids_host, const int64_t* offsets_host,
+                            const double* P_dev, double* uv_dev, int* status_dev, double* residual_dev,
+                            int precision, nurbs_graph_t* out);
+int nurbs_graph_launch(nurbs_graph_t graph, void* stream);
+int nurbs_graph_destroy(nurbs_graph_t graph);
+
 /* ------------------------------------------------------------------ diagnostics */
 /* Measured FMA throughput of the current GPU in TFLOP/s (bits = 64 or 32): independent FMA
  * chains over 8 CTAs per SM, timed with CUDA events.  No reference counterpart; used as the
