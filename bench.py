@@ -142,6 +142,8 @@ def run_ours(a):
         dist.init_process_group("nccl")
     gn = load_pkg()
     n = a.queries
+    if a.workload == "quintic" and n == (1 << 20):
+        n = 1 << 24   # the quintic workload's query count
     surf, s, uv_true, P = make_workload(gn, torch, a.workload, n, 1000 + rank)
     Pd = torch.as_tensor(P, device="cuda")
     uv = torch.empty((n, 2), dtype=torch.float64, device="cuda")
@@ -243,8 +245,9 @@ def run_ours(a):
         "vs_baseline": None,
         "dtype": "fp32+fp64 (mixed)",
         "data": "synthetic (seeded)",
-        "config": {"workload": f"{a.workload}: bicubic 64x64 net, 2^{int(np.log2(n))} queries, offsets |N(0,1e-2)|"
-                   if a.workload == "large" else a.workload,
+        "config": {"workload": {"large": f"large: bicubic 64x64 net, 2^{int(np.log2(n))} queries, offsets |N(0,1e-2)|",
+                                "small": f"small: bicubic 8x8 net, {n} queries, offsets N(0,1e-3)",
+                                "quintic": f"quintic: degree 5x5 256x256 net, 2^{int(np.log2(n))} queries, offsets N(0,1e-3)"}[a.workload],
                    "queries_per_step": n, "precision": "mixed", "l2": "flushed (512 MB write) before each step",
                    "parallelism": f"replicas x{world}"},
         "fp64_value": n * world / (ms_fp64 / 1e3),
@@ -265,6 +268,217 @@ def run_ours(a):
     print(json.dumps(line))
     if world > 1:
         dist.destroy_process_group()
+
+
+def run_batched(a):
+    """Batched uneven workload: 4096 surfaces (p,q in {2,3,5}, nets 4..48), per-surface query
+    counts log-uniform in 16..65536, queries S(u,v) + N(0,1e-3) n; one persistent launch per
+    step, replayed from a CUDA graph, launch configuration picked by the pool's autotuner."""
+    import torch
+    gn = load_pkg()
+    from gpu_nurbs_gb300 import synth
+    t_start = time.perf_counter()
+
+    def phase(msg):
+        print(f"[batched] {time.perf_counter() - t_start:8.2f}s {msg}", file=sys.stderr, flush=True)
+
+    surfs, nq = synth.batched_surfaces(a.surfaces)
+    phase("surfaces generated")
+    t0 = time.perf_counter()
+    budget = int(sum(gn.surface_bytes(sf) for sf in surfs) * 1.05) + (512 << 20)
+    pool = gn.Pool(budget, max_surfaces=len(surfs))
+    ids = pool.add(surfs)
+    torch.cuda.synchronize()
+    t_upload = time.perf_counter() - t0
+    phase(f"pool filled ({t_upload:.2f}s)")
+    offsets = np.concatenate([[0], np.cumsum(nq)]).astype(np.int64)
+    n = int(offsets[-1])
+    batch = gn.Batch(ids, offsets)
+    r = synth.Rng(synth.SEED_BASE + 2 + 1000)
+    uv_true = np.stack([r.uniform(n), r.uniform(n)], 1)
+    off = torch.as_tensor(r.normal(n, 1e-3), device="cuda")
+    E = pool.eval(batch, torch.as_tensor(uv_true, device="cuda"), gn.S | gn.SU | gn.SV)
+    nrm = torch.linalg.cross(E[3:6].T, E[6:9].T, dim=1)
+    nrm = nrm / nrm.norm(dim=1, keepdim=True)
+    Pd = (E[0:3].T + off[:, None] * nrm).contiguous()
+    del E, nrm
+    torch.cuda.synchronize()
+    phase(f"{n} queries formed")
+    out = (torch.empty((n, 2), dtype=torch.float64, device="cuda"), torch.empty(n, dtype=torch.int32, device="cuda"),
+           torch.empty(n, dtype=torch.float64, device="cuda"))
+    cache = os.path.join(os.path.expanduser("~"), ".cache", "gpu_nurbs_gb300", "autotune.txt")
+    os.makedirs(os.path.dirname(cache), exist_ok=True)
+    tile, ctas, tune_ms = pool.autotune(batch, Pd, out, gn.PREC_MIXED, max_queries=a.tune_queries, cache_path=cache)
+    phase(f"autotuned: tile {tile}, ctas/SM {ctas}, {tune_ms:.2f} ms")
+    g_mixed = pool.graph(batch, Pd, out, gn.PREC_MIXED)
+    g_fp64 = pool.graph(batch, Pd, out, gn.PREC_FP64)
+    phase("graphs captured")
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+
+    def timed(fn, steps):
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        for k in range(steps):
+            flush.fill_(float(k))
+            evs[k][0].record(stream)
+            fn()
+            evs[k][1].record(stream)
+        torch.cuda.synchronize()
+        return [e0.elapsed_time(e1) for e0, e1 in evs]
+
+    for _ in range(a.warmup):
+        g_mixed.launch()
+    torch.cuda.synchronize()
+    phase("mixed warm-up done")
+    g_fp64.launch()
+    torch.cuda.synchronize()
+    phase("fp64 warm-up done")
+    clocks = Clocks(0)
+    t_mixed = timed(g_mixed.launch, a.steps)
+    phase("mixed timed")
+    t_fp64 = timed(g_fp64.launch, max(2, a.steps // 8))
+    phase("fp64 timed")
+    clk = clocks.stop()
+    phase("clocks read")
+    g_mixed.launch()
+    torch.cuda.synchronize()
+    g_uv, g_st, g_res = (x.cpu().numpy() for x in out)
+    phase("results copied")
+    # end to end: pinned host queries in, results out, every step
+    Ph = Pd.cpu().pin_memory()
+    hout = [torch.empty(x.shape, dtype=x.dtype).pin_memory() for x in out]
+    t_e2e = []
+    for k in range(max(3, a.steps // 2)):
+        flush.fill_(float(k))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        Pd.copy_(Ph, non_blocking=True)
+        g_mixed.launch()
+        for h, d in zip(hout, out):
+            h.copy_(d, non_blocking=True)
+        torch.cuda.synchronize()
+        t_e2e.append((time.perf_counter() - t0) * 1e3)
+    phase("e2e timed")
+    ms_mixed = sum(t_mixed) / len(t_mixed)
+    ms_fp64 = sum(t_fp64) / len(t_fp64)
+    ms_e2e = sum(t_e2e) / len(t_e2e)
+    found = g_st == 0
+    err = np.abs(g_uv - uv_true).max(1)
+    line = {
+        "metric": METRIC, "value": n / (ms_mixed / 1e3), "unit": "inversions/s", "n_gpus": 1, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": ms_mixed, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "fp32+fp64 (mixed)", "data": "synthetic (seeded)",
+        "config": {"workload": f"batched: {len(surfs)} surfaces, p,q in {{2,3,5}}, nets 4..48, {n} queries "
+                               "(log-uniform 16..65536 per surface), offsets N(0,1e-3)",
+                   "queries_per_step": n, "precision": "mixed", "launch": "one persistent kernel per step, CUDA graph",
+                   "autotuned": {"tile_queries": tile, "ctas_per_sm": ctas, "tune_ms": tune_ms},
+                   "l2": "flushed (512 MB write) before each step", "parallelism": "replicas x1"},
+        "fp64_value": n / (ms_fp64 / 1e3), "fp64_ms_per_step": ms_fp64, "mixed_vs_fp64": ms_fp64 / ms_mixed,
+        "upload_convert_s": t_upload,
+        "accuracy": {"found_frac": float(found.mean()),
+                     "frac_found_within_1e9_of_truth": float((err[found] <= 1e-9).mean()) if found.any() else None},
+        "e2e": {"value": n / (ms_e2e / 1e3), "unit": "inversions/s", "h2d_bytes_per_step": n * 24,
+                "d2h_bytes_per_step": n * 28, "ms_per_step": ms_e2e},
+        "clocks": clk, "gpu_launches": a.steps,
+    }
+    if not a.no_cpu:
+        # oracle on the first surfaces' queries (a bounded sample), checking this run's results
+        import oracle as O
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+        from parity import classify_inversion
+        cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
+        P_h = Ph.numpy()
+        tot = dict()
+        dt = 0.0
+        done = 0
+        k = 0
+        while done < a.cpu_sample and k < len(surfs):
+            sl = slice(int(offsets[k]), int(min(offsets[k + 1], offsets[k] + a.cpu_sample - done)))
+            o = O.OracleSurface(surfs[k])
+            o.tree()
+            t0 = time.perf_counter()
+            ouv, ost, ores, _ = o.invert(P_h[sl], threads=cores)
+            dt += time.perf_counter() - t0
+            c = classify_inversion(g_uv[sl], g_st[sl], g_res[sl], ouv, ost, ores, P_h[sl])
+            for kk, v in c.items():
+                if kk not in ("fail_idx", "max_uv_err_same"):
+                    tot[kk] = tot.get(kk, 0) + v
+            done += sl.stop - sl.start
+            k += 1
+        line["cpu_baseline"] = {"value": done / dt, "unit": "inversions/s", "cores": cores, "kind": "port",
+                                "sample": f"{done} queries of the first {k} surfaces, converged-GN oracle"}
+        line["parity_sample"] = tot
+    print(json.dumps(line))
+
+
+def run_eval(a):
+    """Batched evaluation throughput: 'eval-small' = 2^20 (u,v) on the 8x8 bicubic surface with
+    S, Su, Sv; 'eval-large' = 2^26 (u,v) on the 64x64 bicubic surface with S..Svv.  FP64 and FP32."""
+    import torch
+    gn = load_pkg()
+    from gpu_nurbs_gb300 import synth
+    small = a.workload == "eval-small"
+    surf = synth.surface_small() if small else synth.surface_large()
+    mask = 7 if small else 63
+    n = a.queries if a.queries != (1 << 20) or small else (1 << 26)
+    s = gn.Surface(surf)
+    r = synth.Rng(synth.SEED_BASE + 77)
+    uv = torch.as_tensor(np.stack([r.uniform(n), r.uniform(n)], 1), device="cuda")
+    uv32 = uv.float()
+    nb = bin(mask).count("1")
+    out = torch.empty((3 * nb, n), dtype=torch.float64, device="cuda")
+    out32 = torch.empty((3 * nb, n), dtype=torch.float32, device="cuda")
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+    L = gn.lib()
+
+    def ev64():
+        gn.check(L.nurbs_eval(s.h, uv.data_ptr(), n, mask, out.data_ptr(), gn.PREC_FP64, gn._stream()), "eval")
+
+    def ev32():
+        gn.check(L.nurbs_eval_f32(s.h, uv32.data_ptr(), n, mask, out32.data_ptr(), gn._stream()), "eval")
+
+    def timed(fn, steps):
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        for k in range(steps):
+            flush.fill_(float(k))
+            evs[k][0].record(stream)
+            fn()
+            evs[k][1].record(stream)
+        torch.cuda.synchronize()
+        return [e0.elapsed_time(e1) for e0, e1 in evs]
+
+    for _ in range(a.warmup):
+        ev64()
+        ev32()
+    torch.cuda.synchronize()
+    clocks = Clocks(0)
+    t64 = timed(ev64, a.steps)
+    t32 = timed(ev32, a.steps)
+    clk = clocks.stop()
+    ms64, ms32 = sum(t64) / len(t64), sum(t32) / len(t32)
+    peak64, peak32 = fp64_peak_tflops(torch)
+    k1, k2 = surf["p"] + 1, surf["q"] + 1
+    nv_, nout = (2, 3) if small else (3, 6)
+    flop = 2 * (4 * k1 * k2 * nv_ + 4 * k1 * nout)       # algorithmic flops per point
+    bytes64 = 16 + 24 * nout
+    ach64 = flop * n / (ms64 / 1e3) / 1e12
+    line = {
+        "metric": "evaluations/s (FP64, " + ("S,Su,Sv" if small else "S..Svv") + ")", "value": n / (ms64 / 1e3),
+        "unit": "points/s", "n_gpus": 1, "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms64,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp64", "data": "synthetic (seeded)",
+        "config": {"workload": a.workload, "points_per_step": n, "outputs": "SoA FP64",
+                   "l2": "flushed (512 MB write) before each step"},
+        "fp32_value": n / (ms32 / 1e3), "fp32_ms_per_step": ms32,
+        "roofline": {"bound": "fp64", "achieved": ach64, "peak": peak64, "unit": "TFLOP/s",
+                     "frac": ach64 / peak64 if peak64 else None, "traffic": None,
+                     "flop_per_point": flop, "bytes_per_point_fp64": bytes64,
+                     "hbm_achieved_gbs": bytes64 * n / (ms64 / 1e3) / 1e9,
+                     "fp32_hbm_achieved_gbs": (8 + 12 * nout) * n / (ms32 / 1e3) / 1e9,
+                     "fp32_achieved_tflops": flop * n / (ms32 / 1e3) / 1e12, "fp32_peak": peak32},
+        "clocks": clk, "gpu_launches": 2 * a.steps,
+    }
+    print(json.dumps(line))
 
 
 def cpu_baseline(surf, P, sample, g_uv, g_st, g_res):
@@ -327,13 +541,20 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="large", choices=["large", "small", "quintic"])
+    ap.add_argument("--workload", default="large",
+                    choices=["large", "small", "quintic", "batched", "eval-small", "eval-large"])
+    ap.add_argument("--surfaces", type=int, default=4096)
+    ap.add_argument("--tune-queries", type=int, default=4 << 20)
     ap.add_argument("--queries", type=int, default=1 << 20)
     ap.add_argument("--cpu-sample", type=int, default=1 << 14)
     ap.add_argument("--no-cpu", action="store_true")
     a = ap.parse_args()
     if a.impl == "reference":
         run_reference(a)
+    elif a.workload == "batched":
+        run_batched(a)
+    elif a.workload.startswith("eval"):
+        run_eval(a)
     else:
         run_ours(a)
 

@@ -341,9 +341,10 @@ class Batch:
 
 
 class Graph:
-    def __init__(self, h, keep):
+    def __init__(self, h, keep, pool):
         self.h = h
         self._keep = keep  # device buffers the captured graph reads and writes
+        self._pool = pool  # the pool outlives its graphs
 
     def launch(self, stream=None):
         pool_check(lib().nurbs_graph_launch(self.h, _stream(stream)), "nurbs_graph_launch")
@@ -442,7 +443,7 @@ class Pool:
         pool_check(lib().nurbs_pool_graph_create(self.h, len(batch.ids), batch.ids.ctypes.data, batch.offsets.ctypes.data,
                                                  _ptr(P), _ptr(uv), _ptr(st), _ptr(res), precision, C.byref(h)),
                    "nurbs_pool_graph_create")
-        return Graph(h, (P, uv, st, res))
+        return Graph(h, (P, uv, st, res), self)
 
 
 def surface_bytes(surf: dict) -> int:

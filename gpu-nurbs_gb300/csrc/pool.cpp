@@ -22,6 +22,7 @@
 #include <map>
 #include <mutex>
 #include <new>
+#include <set>
 #include <sstream>
 #include <string>
 #include <vector>
@@ -120,6 +121,7 @@ struct nurbs_pool_s {
   int ctas_per_sm = 4;
   int sms = 152;
   std::map<cudaStream_t, Workspace> ws;
+  std::set<struct nurbs_graph_s*> graphs;  // live graphs, detached if the pool goes first
 };
 
 struct nurbs_graph_s {
@@ -279,6 +281,14 @@ int nurbs_pool_create(int64_t budget_bytes, int max_surfaces, nurbs_pool_t* out)
 int nurbs_pool_destroy(nurbs_pool_t P) {
   if (!P) return NURBS_OK;
   cudaDeviceSynchronize();
+  // graphs still alive lose their device resources now; nurbs_graph_destroy frees the rest
+  for (nurbs_graph_s* G : P->graphs) {
+    if (G->exec) cudaGraphExecDestroy(G->exec);
+    if (G->graph) cudaGraphDestroy(G->graph);
+    G->exec = nullptr;
+    G->graph = nullptr;
+    G->pool = nullptr;
+  }
   for (auto& kv : P->ws) {
     if (kv.second.host) cudaFreeHost(kv.second.host);
     if (kv.second.ev) cudaEventDestroy(kv.second.ev);
@@ -584,12 +594,14 @@ int nurbs_pool_graph_create(nurbs_pool_t P, int nbatch, const int* ids, const in
     delete G;
     return pfail(NURBS_E_CUDA, "graph capture: %s", cudaGetErrorString(e));
   }
+  P->graphs.insert(G);
   *out = G;
   return NURBS_OK;
 }
 
 int nurbs_graph_launch(nurbs_graph_t G, void* stream) {
   if (!G) return pfail(NURBS_E_INVALID, "NULL graph");
+  if (!G->pool) return pfail(NURBS_E_STATE, "the graph's pool was destroyed");
   cudaError_t e = cudaGraphLaunch(G->exec, (cudaStream_t)stream);
   if (e != cudaSuccess) return pfail(NURBS_E_CUDA, "graph launch: %s", cudaGetErrorString(e));
   return NURBS_OK;
@@ -597,12 +609,13 @@ int nurbs_graph_launch(nurbs_graph_t G, void* stream) {
 
 int nurbs_graph_destroy(nurbs_graph_t G) {
   if (!G) return NURBS_OK;
-  cudaDeviceSynchronize();
-  if (G->exec) cudaGraphExecDestroy(G->exec);
-  if (G->graph) cudaGraphDestroy(G->graph);
-  {
+  if (G->pool) {
+    cudaDeviceSynchronize();
+    if (G->exec) cudaGraphExecDestroy(G->exec);
+    if (G->graph) cudaGraphDestroy(G->graph);
     std::lock_guard<std::mutex> lock(G->pool->mu);
     G->pool->arena.release(G->off, G->bytes);
+    G->pool->graphs.erase(G);
   }
   delete G;
   return NURBS_OK;

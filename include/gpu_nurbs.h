@@ -242,6 +242,8 @@ int nurbs_pool_graph_create(nurbs_pool_t pool, int nbatch, const int* ids_host, 
                             const double* P_dev, double* uv_dev, int* status_dev, double* residual_dev,
                             int precision, nurbs_graph_t* out);
 int nurbs_graph_launch(nurbs_graph_t graph, void* stream);
+/* Destroying the pool first releases the graph's device resources (launch then returns
+ * NURBS_E_STATE); nurbs_graph_destroy must still be called once to free the handle. */
 int nurbs_graph_destroy(nurbs_graph_t graph);
 
 /* ------------------------------------------------------------------ diagnostics */

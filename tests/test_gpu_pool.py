@@ -151,3 +151,22 @@ def test_pool_surface_limit(nurbs):
     with pytest.raises(nurbs.NurbsError) as e:
         pool.add([s])
     assert e.value.code == nurbs.E_BUDGET
+
+
+def test_graph_outliving_its_pool(nurbs):
+    """Destroying the pool first detaches its graphs: launch reports E_STATE, destroy still works."""
+    from gpu_nurbs_gb300 import synth
+    import ctypes as C
+    s = synth.surface_small()
+    pool = nurbs.Pool(1 << 26, max_surfaces=4)
+    ids = pool.add([s])
+    P = T(np.full((32, 3), 0.5))
+    out = (torch.empty((32, 2), dtype=torch.float64, device="cuda"), torch.empty(32, dtype=torch.int32, device="cuda"),
+           torch.empty(32, dtype=torch.float64, device="cuda"))
+    g = pool.graph(nurbs.Batch(ids, [0, 32]), P, out, 1)
+    h = g.h
+    g.h = C.c_void_p()        # take the handle over from the wrapper
+    pool.close()
+    L = nurbs.lib()
+    assert L.nurbs_graph_launch(h, None) == nurbs.E_STATE
+    assert L.nurbs_graph_destroy(h) == 0
