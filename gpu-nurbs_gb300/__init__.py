@@ -103,6 +103,17 @@ SIGNATURES = {
     "nurbs_pool_graph_create": (C.c_int, [_vp, C.c_int, _vp, _vp, _vp, _vp, _vp, _vp, C.c_int, C.POINTER(_vp)]),
     "nurbs_graph_launch": (C.c_int, [_vp, _vp]),
     "nurbs_graph_destroy": (C.c_int, [_vp]),
+    "nurbs_server_create": (C.c_int, [_vp, _vp, C.POINTER(_vp)]),
+    "nurbs_server_destroy": (C.c_int, [_vp]),
+    "nurbs_server_submit_invert": (C.c_int, [_vp, C.c_int, _vp, _i64, _vp, _vp, _vp, _vp, C.POINTER(C.c_uint64)]),
+    "nurbs_server_submit_upload": (C.c_int, [_vp, C.POINTER(SurfaceDesc), _vp, _vp, C.POINTER(C.c_uint64)]),
+    "nurbs_server_wait": (C.c_int, [_vp, C.c_uint64, C.c_int, C.POINTER(C.c_int)]),
+    "nurbs_server_poll": (C.c_int, [_vp, _vp, _vp, C.c_int, C.POINTER(C.c_int)]),
+    "nurbs_server_drain": (C.c_int, [_vp, C.c_int]),
+    "nurbs_server_pause": (C.c_int, [_vp, C.c_int]),
+    "nurbs_server_stats": (C.c_int, [_vp, _vp]),
+    "nurbs_server_replay": (C.c_int, [_vp, C.c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
+                                      _vp, C.c_int]),
 }
 
 _lib = None
@@ -454,3 +465,104 @@ def surface_bytes(surf: dict) -> int:
     pool_check(lib().nurbs_pool_surface_bytes(int(surf["p"]), int(surf["q"]), int(surf["nu"]), int(surf["nv"]),
                                               ku.ctypes.data, kv.ctypes.data, C.byref(b)), "nurbs_pool_surface_bytes")
     return b.value
+
+
+# ---------------------------------------------------------------------------- serving
+class ServerConfig(C.Structure):
+    _fields_ = [("slots", C.c_int), ("max_batch_queries", C.c_int64), ("max_batch_requests", C.c_int),
+                ("precision", C.c_int)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("completed", C.c_int64), ("batches", C.c_int64), ("batch_queries", C.c_int64), ("in_flight", C.c_int)]
+
+
+class Server:
+    """Continuous-batching inversion service over a pool (threads live in the library)."""
+
+    def __init__(self, pool: Pool, slots: int = 4, max_batch_queries: int = 1 << 16, max_batch_requests: int = 1024,
+                 precision: int = PREC_MIXED):
+        self.pool = pool
+        cfg = ServerConfig(slots, max_batch_queries, max_batch_requests, precision)
+        h = C.c_void_p()
+        check(lib().nurbs_server_create(pool.h, C.byref(cfg), C.byref(h)), "nurbs_server_create")
+        self.h = h
+        self._keep = {}
+
+    def close(self):
+        if getattr(self, "h", None) and self.h.value:
+            lib().nurbs_server_destroy(self.h)
+            self.h = C.c_void_p()
+            self._keep.clear()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def submit_invert(self, sid: int, P: np.ndarray):
+        """Returns (ticket, (uv, status, residual, latency)) host arrays filled on completion."""
+        P = np.ascontiguousarray(P, np.float64).reshape(-1, 3)
+        n = P.shape[0]
+        uv, st, res, lat = np.empty((n, 2)), np.empty(n, np.int32), np.empty(n), np.zeros(1)
+        t = C.c_uint64()
+        check(lib().nurbs_server_submit_invert(self.h, int(sid), P.ctypes.data, n, uv.ctypes.data, st.ctypes.data,
+                                               res.ctypes.data, lat.ctypes.data, C.byref(t)), "submit_invert")
+        self._keep[t.value] = (P, uv, st, res, lat)
+        return t.value, (uv, st, res, lat)
+
+    def submit_upload(self, surf: dict):
+        arrs = [np.ascontiguousarray(surf[k], np.float64).reshape(-1) for k in ("knots_u", "knots_v", "cps", "weights")]
+        d = SurfaceDesc(int(surf["p"]), int(surf["q"]), int(surf["nu"]), int(surf["nv"]), *(a.ctypes.data for a in arrs))
+        sid, lat = np.full(1, -1, np.int32), np.zeros(1)
+        t = C.c_uint64()
+        check(lib().nurbs_server_submit_upload(self.h, C.byref(d), sid.ctypes.data, lat.ctypes.data, C.byref(t)),
+              "submit_upload")
+        self._keep[t.value] = (arrs, d, sid, lat)
+        return t.value, sid
+
+    def wait(self, ticket: int, timeout_ms: int = 10000) -> int:
+        r = C.c_int()
+        rc = lib().nurbs_server_wait(self.h, C.c_uint64(ticket), timeout_ms, C.byref(r))
+        if rc == OK:
+            self._keep.pop(ticket, None)
+            return r.value
+        return rc
+
+    def drain(self, timeout_ms: int = 30000) -> int:
+        return lib().nurbs_server_drain(self.h, timeout_ms)
+
+    def pause(self, paused: bool):
+        check(lib().nurbs_server_pause(self.h, 1 if paused else 0), "pause")
+
+    def stats(self) -> ServerStats:
+        s = ServerStats()
+        check(lib().nurbs_server_stats(self.h, C.byref(s)), "stats")
+        return s
+
+    def replay(self, arrival_us, kind, surf, qoff, P, uploads=(), upload_index=None, timeout_ms=120000):
+        """Native replay of a request trace; returns (uv, status, residual, latency_us, results, upload_ids)."""
+        nreq = len(arrival_us)
+        arrival_us = np.ascontiguousarray(arrival_us, np.float64)
+        kind = np.ascontiguousarray(kind, np.int32)
+        surf = np.ascontiguousarray(surf, np.int32)
+        qoff = np.ascontiguousarray(qoff, np.int64)
+        P = np.ascontiguousarray(P, np.float64).reshape(-1, 3)
+        n = P.shape[0]
+        uv, st, res = np.empty((n, 2)), np.empty(n, np.int32), np.empty(n)
+        lat, results = np.zeros(nreq), np.zeros(nreq, np.int32)
+        keep = []
+        descs = (SurfaceDesc * max(1, len(uploads)))()
+        for k, sf in enumerate(uploads):
+            arrs = [np.ascontiguousarray(sf[key], np.float64).reshape(-1) for key in ("knots_u", "knots_v", "cps", "weights")]
+            keep.append(arrs)
+            descs[k] = SurfaceDesc(int(sf["p"]), int(sf["q"]), int(sf["nu"]), int(sf["nv"]), *(a.ctypes.data for a in arrs))
+        uidx = np.ascontiguousarray(upload_index if upload_index is not None else np.zeros(nreq), np.int32)
+        uids = np.full(max(1, len(uploads)), -1, np.int32)
+        rc = lib().nurbs_server_replay(self.h, nreq, arrival_us.ctypes.data, kind.ctypes.data, surf.ctypes.data,
+                                       qoff.ctypes.data, P.ctypes.data, uv.ctypes.data, st.ctypes.data, res.ctypes.data,
+                                       C.cast(descs, C.c_void_p), uidx.ctypes.data, uids.ctypes.data, lat.ctypes.data,
+                                       results.ctypes.data, timeout_ms)
+        check(rc, "nurbs_server_replay")
+        return uv, st, res, lat, results, uids

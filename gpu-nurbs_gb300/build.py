@@ -23,7 +23,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-I" + INCLUDE, "-I" + CSRC,
           "--expt-relaxed-constexpr", "-Wno-deprecated-gpu-targets"]
 EXACT_TUS = {"k_convert.cu", "k_tree.cu", "k_legacy.cu"}
-SOURCES = ["k_convert.cu", "k_tree.cu", "k_legacy.cu", "k_eval.cu", "k_invert.cu", "api.cpp", "nu_io.cpp", "k_probe.cu", "k_static.cu", "k_pool.cu", "pool.cpp"]
+SOURCES = ["k_convert.cu", "k_tree.cu", "k_legacy.cu", "k_eval.cu", "k_invert.cu", "api.cpp", "nu_io.cpp", "k_probe.cu", "k_static.cu", "k_pool.cu", "pool.cpp", "server.cpp"]
 
 
 def nvcc() -> str:

@@ -29,6 +29,11 @@ constexpr double kTolAny64 = 1e-14;
 constexpr double kDistinct = 1e-7;      // two FP64 solutions are the same minimum within this
 constexpr float kDistinct32 = 1e-4f;    // ... two FP32 solutions
 constexpr float kJoin = 1e-3f;          // a Newton iterate this close to a known minimum joins it
+// Stopping a seed once it nears a minimum its query already found saves ~15-20 % of the
+// iterations, but whether the other seed has finished first depends on the other queries that
+// share the warp, so results would depend on how requests are batched.  Off: every seed runs
+// to its own end, and a query's result does not depend on its batch.
+constexpr bool kJoinSeeds = false;
 constexpr int kSols = 4;                // FP64 mode: distinct minima kept per query
 constexpr int kSmemSpans = 256;         // breakpoint tables staged in shared memory up to this
 
@@ -423,7 +428,7 @@ __device__ __forceinline__ void invert_chunk(InvSmem<MODE>& sm, const Ctx& cx, c
         int res = kContinue;
         if (active) {
           res = iterate32<P, Q>(cx, tx, ty, tz, sd, dist);
-          if (res == kContinue && sd.newton) {
+          if (kJoinSeeds && res == kContinue && sd.newton) {
             const Rec32& R = sm.rec[warp][ql];
             if ((R.d1 < INFINITY && fabsf(sd.u - R.u1) <= kJoin && fabsf(sd.v - R.v1) <= kJoin) ||
                 (R.d2 < INFINITY && fabsf(sd.u - R.u2) <= kJoin && fabsf(sd.v - R.v2) <= kJoin))
@@ -472,7 +477,7 @@ __device__ __forceinline__ void invert_chunk(InvSmem<MODE>& sm, const Ctx& cx, c
         bool keep = false;
         if (active) {
           res = iterate64<P, Q>(cx, tx, ty, tz, sd);
-          if (res == kContinue && sd.newton) {
+          if (kJoinSeeds && res == kContinue && sd.newton) {
             const Rec64& R = sm.rec[warp][ql];
             for (int k = 0; k < R.n; ++k)
               if (fabs(sd.u - R.u[k]) <= kJoin && fabs(sd.v - R.v[k]) <= kJoin) res = kFailed;

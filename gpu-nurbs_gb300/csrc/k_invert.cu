@@ -15,9 +15,9 @@
 // owns 32 queries, flattens their (query, seed) pairs into a task list (warp prefix sum over
 // the candidate counts) and every lane pulls the next task as soon as its seed converges or
 // fails, so all 32 lanes iterate until the warp's list is exhausted.  Finished seeds are merged
-// into per-query records in shared memory, one lane at a time.  A seed whose iterate (in the
-// Newton regime) arrives within 1e-3 of a minimum its query has already found stops there:
-// it would converge to that minimum.
+// into per-query records in shared memory, one lane at a time.  Every seed runs to its own end
+// (convergence, failure or the iteration cap), so a query's result does not depend on which
+// other queries share its warp: results are the same alone and in any batch.
 //
 // Precision schedules (template MODE):
 //   FP64  — every evaluation, solve and update in FP64.

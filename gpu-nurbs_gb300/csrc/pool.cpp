@@ -95,6 +95,7 @@ class Arena {
 
 struct PoolSurface {
   bool live = false;
+  bool reserved = false;  // being converted by a pool_add in progress
   size_t in_off = 0, in_bytes = 0, out_off = 0, out_bytes = 0;
   int p = 0, q = 0;
   int64_t spans = 0;
@@ -248,6 +249,32 @@ std::string batch_key(nurbs_pool_t P, int nbatch, const int* ids, const int64_t*
 
 }  // namespace
 
+// ---- internal entry points for the server (pool_internal.h)
+namespace gnurbs {
+bool pool_is_live(nurbs_pool_t P, int id) {
+  std::lock_guard<std::mutex> lock(P->mu);
+  return id >= 0 && id < (int)P->surf.size() && P->surf[id].live;
+}
+int pool_release_surface(nurbs_pool_t P, int id) {  // caller guarantees no queued work uses it
+  std::lock_guard<std::mutex> lock(P->mu);
+  if (id < 0 || id >= (int)P->surf.size() || !P->surf[id].live) return NURBS_E_INVALID;
+  PoolSurface& s = P->surf[id];
+  P->arena.release(s.in_off, s.in_bytes);
+  P->arena.release(s.out_off, s.out_bytes);
+  s = PoolSurface{};
+  return NURBS_OK;
+}
+char* pool_arena_alloc(nurbs_pool_t P, size_t bytes, size_t* off) {
+  std::lock_guard<std::mutex> lock(P->mu);
+  if (!P->arena.alloc(bytes, *off)) return nullptr;
+  return P->base + *off;
+}
+void pool_arena_release(nurbs_pool_t P, size_t off, size_t bytes) {
+  std::lock_guard<std::mutex> lock(P->mu);
+  P->arena.release(off, bytes);
+}
+}  // namespace gnurbs
+
 extern "C" {
 
 const char* nurbs_pool_last_error(void) { return g_pool_error.c_str(); }
@@ -302,8 +329,8 @@ int nurbs_pool_destroy(nurbs_pool_t P) {
 int nurbs_pool_add(nurbs_pool_t P, int count, const nurbs_surface_desc* descs, void* stream, int* ids_out) {
   if (!P || count < 0 || (count > 0 && (!descs || !ids_out))) return pfail(NURBS_E_INVALID, "bad arguments");
   if (count == 0) return NURBS_OK;
-  std::lock_guard<std::mutex> lock(P->mu);
   cudaStream_t st = (cudaStream_t)stream;
+  // 1. host preparation (no lock)
   std::vector<SurfaceHost> S(count);
   std::string err;
   size_t in_total = 0;
@@ -313,30 +340,44 @@ int nurbs_pool_add(nurbs_pool_t P, int count, const nurbs_surface_desc* descs, v
     if (rc) return pfail(rc, "surface %d: %s", k, err.c_str());
     in_total += S[k].in_bytes;
   }
-  // ids: reuse dead slots, then append
-  std::vector<int> ids;
-  for (int id = 0; id < (int)P->surf.size() && (int)ids.size() < count; ++id)
-    if (!P->surf[id].live) ids.push_back(id);
-  while ((int)ids.size() < count) {
-    if ((int)P->surf.size() >= P->max_surfaces) return pfail(NURBS_E_BUDGET, "the pool holds its maximum of %d surfaces", P->max_surfaces);
-    P->surf.emplace_back();
-    ids.push_back((int)P->surf.size() - 1);
-  }
-  // admission: the input parts of the batch go in one region (one copy), computed parts each
-  size_t in_off = 0;
-  if (!P->arena.alloc(in_total, in_off)) return pfail(NURBS_E_BUDGET, "no room in the pool budget for the batch");
-  std::vector<size_t> out_off(count);
-  for (int k = 0; k < count; ++k) {
-    if (!P->arena.alloc(S[k].out_bytes, out_off[k])) {
-      for (int j = 0; j < k; ++j) P->arena.release(out_off[j], S[j].out_bytes);
-      P->arena.release(in_off, in_total);
-      return pfail(NURBS_E_BUDGET, "no room in the pool budget for surface %d of the batch", k);
-    }
-  }
-  std::vector<char> img(in_total, 0);
-  std::vector<SurfDev> recs(count);
   std::vector<BasisJob> bjobs;
   std::vector<SpanJob> sjobs;
+  const size_t jb = align256(2 * (size_t)count * sizeof(BasisJob)), js = align256((size_t)count * sizeof(SpanJob));
+  const size_t ji = align256((size_t)count * sizeof(int)), scratch_bytes = jb + js + ji;
+  // 2. admission (locked): ids and arena blocks are reserved; the conversion runs unlocked so
+  //    inversions of live surfaces proceed meanwhile
+  std::vector<int> ids;
+  size_t in_off = 0, scratch_off = 0;
+  std::vector<size_t> out_off(count);
+  {
+    std::lock_guard<std::mutex> lock(P->mu);
+    for (int id = 0; id < (int)P->surf.size() && (int)ids.size() < count; ++id)
+      if (!P->surf[id].live && !P->surf[id].reserved) ids.push_back(id);
+    int append = count - (int)ids.size();
+    if ((int)P->surf.size() + append > P->max_surfaces)
+      return pfail(NURBS_E_BUDGET, "the pool holds its maximum of %d surfaces", P->max_surfaces);
+    if (!P->arena.alloc(in_total, in_off)) return pfail(NURBS_E_BUDGET, "no room in the pool budget for the batch");
+    for (int k = 0; k < count; ++k) {
+      if (!P->arena.alloc(S[k].out_bytes, out_off[k])) {
+        for (int j = 0; j < k; ++j) P->arena.release(out_off[j], S[j].out_bytes);
+        P->arena.release(in_off, in_total);
+        return pfail(NURBS_E_BUDGET, "no room in the pool budget for surface %d of the batch", k);
+      }
+    }
+    if (!P->arena.alloc(scratch_bytes, scratch_off)) {
+      for (int j = 0; j < count; ++j) P->arena.release(out_off[j], S[j].out_bytes);
+      P->arena.release(in_off, in_total);
+      return pfail(NURBS_E_BUDGET, "no room in the pool budget for the conversion scratch");
+    }
+    for (int k = 0; k < append; ++k) {
+      P->surf.emplace_back();
+      ids.push_back((int)P->surf.size() - 1);
+    }
+    for (int id : ids) P->surf[id].reserved = true;
+  }
+  // 3. images, one copy, one launch per conversion stage (unlocked)
+  std::vector<char> img(in_total, 0);
+  std::vector<SurfDev> recs(count);
   int64_t bitems = 0, sitems = 0;
   size_t o = 0;
   for (int k = 0; k < count; ++k) {
@@ -350,18 +391,10 @@ int nurbs_pool_add(nurbs_pool_t P, int count, const nurbs_surface_desc* descs, v
     sitems += (int64_t)d.ns_u * d.ns_v * 4;
     o += S[k].in_bytes;
   }
-  // job tables and the id list ride in a scratch region of the arena for the conversion
-  size_t jb = bjobs.size() * sizeof(BasisJob), js = sjobs.size() * sizeof(SpanJob), ji = (size_t)count * sizeof(int);
-  size_t scratch_off = 0, scratch_bytes = align256(jb) + align256(js) + align256(ji);
-  if (!P->arena.alloc(scratch_bytes, scratch_off)) {
-    for (int j = 0; j < count; ++j) P->arena.release(out_off[j], S[j].out_bytes);
-    P->arena.release(in_off, in_total);
-    return pfail(NURBS_E_BUDGET, "no room in the pool budget for the conversion scratch");
-  }
   std::vector<char> scr(scratch_bytes, 0);
-  std::memcpy(scr.data(), bjobs.data(), jb);
-  std::memcpy(scr.data() + align256(jb), sjobs.data(), js);
-  std::memcpy(scr.data() + align256(jb) + align256(js), ids.data(), ji);
+  std::memcpy(scr.data(), bjobs.data(), bjobs.size() * sizeof(BasisJob));
+  std::memcpy(scr.data() + jb, sjobs.data(), sjobs.size() * sizeof(SpanJob));
+  std::memcpy(scr.data() + jb + js, ids.data(), ids.size() * sizeof(int));
   char* sdev = P->base + scratch_off;
   cudaError_t e = cudaMemcpyAsync(P->base + in_off, img.data(), in_total, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = cudaMemcpyAsync(sdev, scr.data(), scratch_bytes, cudaMemcpyHostToDevice, st);
@@ -369,19 +402,23 @@ int nurbs_pool_add(nurbs_pool_t P, int count, const nurbs_surface_desc* descs, v
     e = cudaMemcpyAsync(P->d_table + ids[k], &recs[k], sizeof(SurfDev), cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = launch_basis_batched((const BasisJob*)sdev, (int)bjobs.size(), bitems, st);
   if (e == cudaSuccess)
-    e = launch_span_matrices_batched(P->d_table, (const SpanJob*)(sdev + align256(jb)), (int)sjobs.size(), sitems, st);
-  if (e == cudaSuccess) e = launch_tree_batched(P->d_table, (const int*)(sdev + align256(jb) + align256(js)), count, st);
+    e = launch_span_matrices_batched(P->d_table, (const SpanJob*)(sdev + jb), (int)sjobs.size(), sitems, st);
+  if (e == cudaSuccess) e = launch_tree_batched(P->d_table, (const int*)(sdev + jb + js), count, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // host images must outlive the copies
+  // 4. publication (locked)
+  std::lock_guard<std::mutex> lock(P->mu);
   P->arena.release(scratch_off, scratch_bytes);
   if (e != cudaSuccess) {
     for (int j = 0; j < count; ++j) P->arena.release(out_off[j], S[j].out_bytes);
     P->arena.release(in_off, in_total);
+    for (int id : ids) P->surf[id].reserved = false;
     return pfail(NURBS_E_CUDA, "pool conversion: %s", cudaGetErrorString(e));
   }
   o = 0;
   for (int k = 0; k < count; ++k) {
     PoolSurface& ps = P->surf[ids[k]];
     ps.live = true;
+    ps.reserved = false;
     // the batch's input region is released piecewise: each surface owns its slice
     ps.in_off = in_off + o;
     ps.in_bytes = S[k].in_bytes;

@@ -246,6 +246,52 @@ int nurbs_graph_launch(nurbs_graph_t graph, void* stream);
  * NURBS_E_STATE); nurbs_graph_destroy must still be called once to free the handle. */
 int nurbs_graph_destroy(nurbs_graph_t graph);
 
+/* ------------------------------------------------------------------ serving */
+/* A continuous-batching request loop over a pool.  No counterpart in the reference.
+ * Requests are submitted from any host thread; a scheduler thread keeps up to `slots` batches
+ * in flight (one CUDA stream each), forms every new batch from the requests that arrived while
+ * the GPU was busy, and copies each request's results back to its host buffers.  Uploads are
+ * converted on their own stream; when the budget is full, the least recently used surfaces
+ * that no queued request references are evicted.  Host buffers passed to a submit call must
+ * stay valid until the request completes. */
+typedef struct nurbs_server_s* nurbs_server_t;
+typedef struct {
+    int slots;                   /* batches in flight (1..16) */
+    int64_t max_batch_queries;   /* queries per batch; also the largest request accepted */
+    int max_batch_requests;      /* requests per batch */
+    int precision;               /* NURBS_PREC_MIXED or NURBS_PREC_FP64 */
+} nurbs_server_config;
+typedef struct {
+    int64_t completed, batches, batch_queries;
+    int in_flight;
+} nurbs_server_stats_t;
+
+int nurbs_server_create(nurbs_pool_t pool, const nurbs_server_config* cfg, nurbs_server_t* out);
+/* Stops the threads; batches in flight finish, requests not started complete with NURBS_E_STATE. */
+int nurbs_server_destroy(nurbs_server_t server);
+int nurbs_server_submit_invert(nurbs_server_t server, int surf_id, const double* P_host, int64_t n,
+                               double* uv_host, int* status_host, double* residual_host,
+                               double* latency_us_out, uint64_t* ticket);
+int nurbs_server_submit_upload(nurbs_server_t server, const nurbs_surface_desc* desc, int* surf_id_out,
+                               double* latency_us_out, uint64_t* ticket);
+/* Bounded wait for one request (NURBS_E_TIMEOUT after timeout_ms); releases the ticket. */
+int nurbs_server_wait(nurbs_server_t server, uint64_t ticket, int timeout_ms, int* result);
+/* Completed requests since the last poll (tickets released). */
+int nurbs_server_poll(nurbs_server_t server, uint64_t* tickets, int* results, int max, int* count);
+/* Bounded wait until no request is queued or in flight. */
+int nurbs_server_drain(nurbs_server_t server, int timeout_ms);
+/* Holds (1) or resumes (0) the dispatch of new batches; batches in flight finish. */
+int nurbs_server_pause(nurbs_server_t server, int paused);
+int nurbs_server_stats(nurbs_server_t server, nurbs_server_stats_t* stats);
+/* Native load generator: submits request i at arrival_us[i] after the start, then drains.
+ * kind[i] 0 = inversion of queries [qoff[i], qoff[i+1]) of P against surf[i] (outputs at the
+ * same offsets); 1 = upload of uploads[upload_index[i]] (its id written to upload_ids[...]).
+ * latency_us[i] counts from the scheduled arrival; results[i] is the request's status. */
+int nurbs_server_replay(nurbs_server_t server, int nreq, const double* arrival_us, const int* kind,
+                        const int* surf, const int64_t* qoff, const double* P, double* uv, int* status,
+                        double* residual, const nurbs_surface_desc* uploads, const int* upload_index,
+                        int* upload_ids, double* latency_us, int* results, int timeout_ms);
+
 /* ------------------------------------------------------------------ diagnostics */
 /* Measured FMA throughput of the current GPU in TFLOP/s (bits = 64 or 32): independent FMA
  * chains over 8 CTAs per SM, timed with CUDA events.  No reference counterpart; used as the
