@@ -411,6 +411,114 @@ def run_batched(a):
     print(json.dumps(line))
 
 
+def run_serving(a):
+    """Serving: a pool of 10^4 surfaces (generated as the batched workload) under a 20 GB budget;
+    Poisson request arrivals swept over rates; each request targets a surface drawn Zipf(1.1)
+    with 1..4096 queries (log-uniform), 10% of requests upload a new surface.  Requests are
+    replayed by the library's native load generator against the continuous-batching server;
+    latency counts from the scheduled arrival.  The headline is p99 at half of the peak rate."""
+    import torch
+    gn = load_pkg()
+    from gpu_nurbs_gb300 import synth
+    t_start = time.perf_counter()
+
+    def phase(msg):
+        print(f"[serving] {time.perf_counter() - t_start:8.2f}s {msg}", file=sys.stderr, flush=True)
+
+    npool = a.surfaces if a.surfaces != 4096 else 10000
+    surfs, _ = synth.batched_surfaces(npool, seed=synth.SEED_BASE + 4)
+    pool = gn.Pool(20 << 30, max_surfaces=npool + 200000)
+    ids = pool.add(surfs)
+    pool.set_config(a.serve_chunk, 4)
+    phase(f"pool of {npool} surfaces, {pool.info().used_bytes / 2**30:.2f} GiB")
+    r = synth.Rng(synth.SEED_BASE + 4 + 1)
+    # Zipf(1.1) over the pool (ranks shuffled so popularity is not tied to generation order)
+    ranks = np.arange(1, npool + 1, dtype=np.float64)
+    pz = ranks ** -1.1
+    pz /= pz.sum()
+    perm = r.g.permutation(npool)
+    upload_bank = synth.batched_surfaces(2000, seed=synth.SEED_BASE + 4 + 2)[0]
+    rates = [float(x) for x in a.rates.split(",")]
+
+    def trace(rate, nreq, precision_server):
+        kind = (r.uniform(nreq) < a.upload_frac).astype(np.int32)
+        sizes = np.where(kind == 0, np.exp(r.uniform(nreq, 0.0, np.log(4096.0))).astype(np.int64), 0)
+        sizes = np.maximum(sizes, kind == 0)
+        which = perm[r.g.choice(npool, size=nreq, p=pz)]
+        qoff = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+        nq = int(qoff[-1])
+        # queries S(u,v) + N(0,1e-3) n on each request's surface, formed on the GPU
+        uvq = torch.as_tensor(np.stack([r.uniform(nq), r.uniform(nq)], 1), device="cuda")
+        req_ids = ids[which].astype(np.int32)
+        # upload requests own empty query ranges
+        E = pool.eval(gn.Batch(req_ids, qoff), uvq, gn.S | gn.SU | gn.SV)
+        nrm = torch.linalg.cross(E[3:6].T, E[6:9].T, dim=1)
+        nrm = nrm / nrm.norm(dim=1, keepdim=True)
+        off = torch.as_tensor(r.normal(nq, 1e-3), device="cuda")
+        P = (E[0:3].T + off[:, None] * nrm).cpu().numpy()
+        arrival = np.cumsum(r.g.exponential(1e6 / rate, nreq))
+        uidx = np.cumsum(kind) - 1
+        uidx = np.where(kind == 1, uidx % len(upload_bank), 0).astype(np.int32)
+        return arrival, kind, req_ids, qoff, P, uidx, sizes
+
+    def serve(rate, nreq, precision):
+        arrival, kind, req_ids, qoff, P, uidx, sizes = trace(rate, nreq, precision)
+        srv = gn.Server(pool, slots=a.slots, max_batch_queries=1 << 16, max_batch_requests=4096, precision=precision)
+        uv, st, res, lat, results, uids = srv.replay(arrival, kind, req_ids, qoff, P, upload_bank, uidx,
+                                                     timeout_ms=600000)
+        stats = srv.stats()
+        srv.close()
+        # uploaded surfaces are released again so every rate starts from the same pool
+        for u in np.unique(uids[uids >= 0]):
+            pool.remove(int(u))
+        inv = kind == 0
+        ok = results == 0
+        done = arrival + lat
+        # inversion throughput over the inversion requests' own span (uploads are reported apart)
+        span_s = (done[inv].max() - arrival[inv].min()) / 1e6
+        li = lat[inv & ok] / 1e3
+        lu = lat[(kind == 1) & ok] / 1e3
+        return {"rate_req_s": rate, "requests": int(nreq), "queries": int(sizes.sum()),
+                "ok_frac": float(ok.mean()), "achieved_req_s": int(inv.sum()) / span_s,
+                "achieved_queries_s": float(sizes.sum()) / span_s,
+                "p50_ms": float(np.percentile(li, 50)), "p99_ms": float(np.percentile(li, 99)),
+                "upload_p50_ms": float(np.percentile(lu, 50)) if lu.size else None,
+                "upload_p99_ms": float(np.percentile(lu, 99)) if lu.size else None,
+                "batches": int(stats.batches), "mean_batch_queries": stats.batch_queries / max(1, stats.batches),
+                "gpu_ms_per_batch": stats.gpu_ms / max(1, stats.batches),
+                "dispatch_us_per_batch": stats.dispatch_us / max(1, stats.batches),
+                "retire_us_per_batch": stats.retire_us / max(1, stats.batches),
+                "found_frac": float((st[np.repeat(inv, sizes)] == 0).mean()) if sizes.sum() else None}
+
+    sweep = []
+    for rate in rates:
+        nreq = int(min(max(rate * a.serve_seconds, 2000), a.max_requests))
+        sweep.append(serve(rate, nreq, gn.PREC_MIXED))
+        phase(f"rate {rate:.0f}: p50 {sweep[-1]['p50_ms']:.3f} ms p99 {sweep[-1]['p99_ms']:.3f} ms, "
+              f"{sweep[-1]['achieved_queries_s'] / 1e6:.1f} M queries/s")
+    peak = max(sweep, key=lambda d: d["achieved_req_s"])
+    half_rate = peak["achieved_req_s"] / 2
+    half = serve(half_rate, int(min(max(half_rate * a.serve_seconds, 2000), a.max_requests)), gn.PREC_MIXED)
+    phase(f"half peak {half_rate:.0f} req/s: p99 {half['p99_ms']:.3f} ms")
+    fp64_peak = serve(rates[-1], int(min(max(rates[-1] * a.serve_seconds, 2000), a.max_requests) // 4), gn.PREC_FP64)
+    phase("fp64 peak measured")
+    line = {
+        "metric": "serve p99 latency at half of peak throughput (mixed)", "value": half["p99_ms"], "unit": "ms",
+        "n_gpus": 1, "steps": len(rates) + 2, "warmup": 0, "ms_per_step": None, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "fp32+fp64 (mixed)", "data": "synthetic (seeded)",
+        "config": {"workload": f"serving: pool of {npool} surfaces (batched-workload distribution), 20 GB budget, "
+                               "Poisson arrivals, Zipf(1.1) surfaces, 1..4096 queries/request log-uniform, "
+                               "10% uploads", "slots": a.slots, "max_batch_queries": 1 << 16,
+                   "queries_per_warp_chunk": a.serve_chunk},
+        "peak": {"req_s": peak["achieved_req_s"], "queries_s": peak["achieved_queries_s"]},
+        "half_peak": half, "sweep": sweep,
+        "fp64_server_at_top_rate": fp64_peak,
+        "mixed_vs_fp64_peak_queries_s": peak["achieved_queries_s"] / fp64_peak["achieved_queries_s"],
+        "gpu_launches": None,
+    }
+    print(json.dumps(line))
+
+
 def run_eval(a):
     """Batched evaluation throughput: 'eval-small' = 2^20 (u,v) on the 8x8 bicubic surface with
     S, Su, Sv; 'eval-large' = 2^26 (u,v) on the 64x64 bicubic surface with S..Svv.  FP64 and FP32."""
@@ -542,7 +650,13 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="large",
-                    choices=["large", "small", "quintic", "batched", "eval-small", "eval-large"])
+                    choices=["large", "small", "quintic", "batched", "eval-small", "eval-large", "serving"])
+    ap.add_argument("--rates", default="1000,10000,30000,100000,300000,1000000")
+    ap.add_argument("--serve-seconds", type=float, default=1.0)
+    ap.add_argument("--max-requests", type=int, default=40000)
+    ap.add_argument("--slots", type=int, default=4)
+    ap.add_argument("--upload-frac", type=float, default=0.10)
+    ap.add_argument("--serve-chunk", type=int, default=16, help="queries per warp chunk when serving")
     ap.add_argument("--surfaces", type=int, default=4096)
     ap.add_argument("--tune-queries", type=int, default=4 << 20)
     ap.add_argument("--queries", type=int, default=1 << 20)
@@ -555,6 +669,8 @@ def main():
         run_batched(a)
     elif a.workload.startswith("eval"):
         run_eval(a)
+    elif a.workload == "serving":
+        run_serving(a)
     else:
         run_ours(a)
 

@@ -474,7 +474,8 @@ class ServerConfig(C.Structure):
 
 
 class ServerStats(C.Structure):
-    _fields_ = [("completed", C.c_int64), ("batches", C.c_int64), ("batch_queries", C.c_int64), ("in_flight", C.c_int)]
+    _fields_ = [("completed", C.c_int64), ("batches", C.c_int64), ("batch_queries", C.c_int64), ("in_flight", C.c_int),
+                ("gpu_ms", C.c_double), ("dispatch_us", C.c_double), ("retire_us", C.c_double)]
 
 
 class Server:

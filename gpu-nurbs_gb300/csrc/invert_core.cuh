@@ -209,38 +209,46 @@ __device__ __forceinline__ int finish_status(const double* us, const double* vs,
   return 0;
 }
 
-template <int MODE>
-struct InvSmem {
+// One surface staged in shared memory: tree boxes (FP32 outward-rounded and exact FP64), seed
+// centres, domain, and breakpoint tables when the surface has at most KS spans per direction.
+template <int KS>
+struct Staged {
   float box32[kTreeNodes][6];
   double box64[kTreeNodes][6];
   double ctr[kTreeNodes][2];
   float ctr32[kTreeNodes][2];
   float dom32[4];
   int nb;
-  unsigned long long smask0[kWarps][32];
-  unsigned char smask1[kWarps][32];
-  unsigned srmask[kWarps][kTreeNodes];
-  int srpref[kWarps][kTreeNodes + 1];
-  int slpref[kWarps][32];
-  typename std::conditional<MODE == kModeMixed, Rec32, Rec64>::type rec[kWarps][32];
-  float sp32[kWarps][32][3];
-  double sp64[kWarps][32][3];
-  float sb32[2][kSmemSpans + 1], si32[2][kSmemSpans];
-  double sb64[2][kSmemSpans + 1], si64[2][kSmemSpans];
+  float sb32[2][KS + 1], si32[2][KS];
+  double sb64[2][KS + 1], si64[2][KS];
 };
 
-// CTA-cooperative: stages one surface's tree boxes, seeds and (when they fit) breakpoint tables
-// in shared memory and fills the context.  The caller synchronises the CTA before and after.
+// Per-warp bookkeeping of the task scheduler: candidate masks, task-order tables, per-query
+// records and query coordinates of the warp's (up to) 32 queries.
 template <int MODE>
-__device__ __forceinline__ void stage_surface(const SurfDev& s, InvSmem<MODE>& sm, Ctx& cx) {
-  const bool smem_tables = s.ns_u <= kSmemSpans && s.ns_v <= kSmemSpans;
+struct WarpWork {
+  unsigned long long smask0[32];
+  unsigned char smask1[32];
+  unsigned srmask[kTreeNodes];
+  int srpref[kTreeNodes + 1];
+  int slpref[32];
+  typename std::conditional<MODE == kModeMixed, Rec32, Rec64>::type rec[32];
+  float sp32[32][3];
+  double sp64[32][3];
+};
+
+// Cooperative over `nthreads` threads (index tid): stages one surface and fills the context.
+// The callers synchronise the participating threads before and after.
+template <int KS>
+__device__ __forceinline__ void stage_surface(const SurfDev& s, Staged<KS>& sm, Ctx& cx, int tid, int nthreads) {
+  const bool smem_tables = s.ns_u <= KS && s.ns_v <= KS;
   if (smem_tables) {
-    for (int k = threadIdx.x; k <= s.ns_u; k += blockDim.x) {
+    for (int k = tid; k <= s.ns_u; k += nthreads) {
       sm.sb32[0][k] = s.bu32[k];
       sm.sb64[0][k] = s.bu[k];
       if (k < s.ns_u) { sm.si32[0][k] = s.inv_du32[k]; sm.si64[0][k] = s.inv_du[k]; }
     }
-    for (int k = threadIdx.x; k <= s.ns_v; k += blockDim.x) {
+    for (int k = tid; k <= s.ns_v; k += nthreads) {
       sm.sb32[1][k] = s.bv32[k];
       sm.sb64[1][k] = s.bv[k];
       if (k < s.ns_v) { sm.si32[1][k] = s.inv_dv32[k]; sm.si64[1][k] = s.inv_dv[k]; }
@@ -260,7 +268,7 @@ __device__ __forceinline__ void stage_surface(const SurfDev& s, InvSmem<MODE>& s
   // built nodes are the root alone, or the root and all 64 children (the children of the
   // 2-level tree are built together when the root is divided), so node k keeps index k
   const int nb = s.built[1] ? kTreeNodes : (s.built[0] ? 1 : 0);
-  for (int k = threadIdx.x; k < nb; k += blockDim.x) {
+  for (int k = tid; k < nb; k += nthreads) {
     const TreeNodeDev& T = s.tree[k];
     for (int j = 0; j < 3; ++j) {
       sm.box64[k][j] = T.lb[j];
@@ -273,7 +281,7 @@ __device__ __forceinline__ void stage_surface(const SurfDev& s, InvSmem<MODE>& s
     sm.ctr32[k][0] = (float)sm.ctr[k][0];
     sm.ctr32[k][1] = (float)sm.ctr[k][1];
   }
-  if (threadIdx.x == 0) {
+  if (tid == 0) {
     sm.nb = nb;
     const float slack = 1e-4f;  // FP32 domain test is a prefilter; the FP64 phase decides
     sm.dom32[0] = (float)s.dom_u0 - slack;
@@ -284,11 +292,12 @@ __device__ __forceinline__ void stage_surface(const SurfDev& s, InvSmem<MODE>& s
 }
 
 // One warp inverts the queries [q0, min(q0+32, qend)) of the staged surface.
-template <int P, int Q, int MODE>
-__device__ __forceinline__ void invert_chunk(InvSmem<MODE>& sm, const Ctx& cx, const double* __restrict__ Pq,
+template <int P, int Q, int MODE, int KS>
+__device__ __forceinline__ void invert_chunk(Staged<KS>& sm, WarpWork<MODE>& ww, const Ctx& cx,
+                                             const double* __restrict__ Pq,
                                              int64_t q0, int64_t qend, double* __restrict__ uv_out,
                                              int* __restrict__ st_out, double* __restrict__ res_out) {
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int lane = threadIdx.x & 31;
   const unsigned FULL = 0xffffffffu;
   const unsigned lt_mask = (1u << lane) - 1u;
   const int nbl = sm.nb;
@@ -326,12 +335,12 @@ __device__ __forceinline__ void invert_chunk(InvSmem<MODE>& sm, const Ctx& cx, c
     for (int r = 0; r < maxc; ++r) {
       unsigned m = __ballot_sync(FULL, cnt > r);
       if (lane == 0) {
-        sm.srmask[warp][r] = m;
-        sm.srpref[warp][r] = total;
+        ww.srmask[r] = m;
+        ww.srpref[r] = total;
       }
       total += __popc(m);
     }
-    if (lane == 0) sm.srpref[warp][maxc] = total;
+    if (lane == 0) ww.srpref[maxc] = total;
     if constexpr (MODE == kModeMixed) {
       int incl = cnt;
 #pragma unroll
@@ -339,23 +348,23 @@ __device__ __forceinline__ void invert_chunk(InvSmem<MODE>& sm, const Ctx& cx, c
         int t = __shfl_up_sync(FULL, incl, o);
         if (lane >= o) incl += t;
       }
-      sm.slpref[warp][lane] = incl - cnt;
+      ww.slpref[lane] = incl - cnt;
     }
-    sm.sp32[warp][lane][0] = fx;
-    sm.sp32[warp][lane][1] = fy;
-    sm.sp32[warp][lane][2] = fz;
-    sm.sp64[warp][lane][0] = px;
-    sm.sp64[warp][lane][1] = py;
-    sm.sp64[warp][lane][2] = pz;
-    sm.smask0[warp][lane] = m0;
-    sm.smask1[warp][lane] = (unsigned char)m1;
+    ww.sp32[lane][0] = fx;
+    ww.sp32[lane][1] = fy;
+    ww.sp32[lane][2] = fz;
+    ww.sp64[lane][0] = px;
+    ww.sp64[lane][1] = py;
+    ww.sp64[lane][2] = pz;
+    ww.smask0[lane] = m0;
+    ww.smask1[lane] = (unsigned char)m1;
     if constexpr (MODE == kModeMixed) {
-      Rec32& R = sm.rec[warp][lane];
+      Rec32& R = ww.rec[lane];
       R.d1 = INFINITY;
       R.d2 = INFINITY;
       R.u1 = R.v1 = R.u2 = R.v2 = 0.f;
     } else {
-      sm.rec[warp][lane].n = 0;
+      ww.rec[lane].n = 0;
     }
     __syncwarp();
 
@@ -367,10 +376,10 @@ __device__ __forceinline__ void invert_chunk(InvSmem<MODE>& sm, const Ctx& cx, c
         int lo = 0;
 #pragma unroll
         for (int step = 16; step > 0; step >>= 1)
-          if (sm.slpref[warp][lo + step] <= t) lo += step;
+          if (ww.slpref[lo + step] <= t) lo += step;
         ql = lo;
-        uint64_t mm = sm.smask0[warp][ql];
-        int k = t - sm.slpref[warp][lo];
+        uint64_t mm = ww.smask0[ql];
+        int k = t - ww.slpref[lo];
         if (k < __popcll(mm)) {
           for (int i = 0; i < k; ++i) mm &= mm - 1;
           node = __ffsll((long long)mm) - 1;
@@ -383,16 +392,16 @@ __device__ __forceinline__ void invert_chunk(InvSmem<MODE>& sm, const Ctx& cx, c
       int r = 0;
 #pragma unroll
       for (int step = 64; step > 0; step >>= 1)
-        if (r + step < maxc && sm.srpref[warp][r + step] <= t) r += step;
+        if (r + step < maxc && ww.srpref[r + step] <= t) r += step;
       // lane: the (t - rpref[r])-th set bit of rmask[r]
-      const unsigned m = sm.srmask[warp][r];
-      int i = t - sm.srpref[warp][r], pos = 0;
+      const unsigned m = ww.srmask[r];
+      int i = t - ww.srpref[r], pos = 0;
 #pragma unroll
       for (int w = 16; w > 0; w >>= 1)
         if (__popc(m & ((1u << (pos + w)) - 1u)) <= i) pos += w;
       ql = pos;
       int k = r;  // seed r of that query: its r-th candidate node in ascending order
-      uint64_t mm = sm.smask0[warp][ql];
+      uint64_t mm = ww.smask0[ql];
       int c0 = __popcll(mm);
       if (k < c0) {
         for (int i = 0; i < k; ++i) mm &= mm - 1;
@@ -412,9 +421,9 @@ __device__ __forceinline__ void invert_chunk(InvSmem<MODE>& sm, const Ctx& cx, c
       float tx = 0, ty = 0, tz = 0;
       auto start = [&]() {
         decode(task, ql, node);
-        tx = sm.sp32[warp][ql][0];
-        ty = sm.sp32[warp][ql][1];
-        tz = sm.sp32[warp][ql][2];
+        tx = ww.sp32[ql][0];
+        ty = ww.sp32[ql][1];
+        tz = ww.sp32[ql][2];
         sd.u = sm.ctr32[node][0];
         sd.v = sm.ctr32[node][1];
         sd.prev = INFINITY;
@@ -429,7 +438,7 @@ __device__ __forceinline__ void invert_chunk(InvSmem<MODE>& sm, const Ctx& cx, c
         if (active) {
           res = iterate32<P, Q>(cx, tx, ty, tz, sd, dist);
           if (kJoinSeeds && res == kContinue && sd.newton) {
-            const Rec32& R = sm.rec[warp][ql];
+            const Rec32& R = ww.rec[ql];
             if ((R.d1 < INFINITY && fabsf(sd.u - R.u1) <= kJoin && fabsf(sd.v - R.v1) <= kJoin) ||
                 (R.d2 < INFINITY && fabsf(sd.u - R.u2) <= kJoin && fabsf(sd.v - R.v2) <= kJoin))
               res = kFailed;  // joins a minimum already found: nothing new
@@ -442,7 +451,7 @@ __device__ __forceinline__ void invert_chunk(InvSmem<MODE>& sm, const Ctx& cx, c
         unsigned fm = __ballot_sync(FULL, done && keep);
         while (fm) {
           int j = __ffs(fm) - 1;
-          if (lane == j) merge32(sm.rec[warp][ql], sd.u, sd.v, dist);
+          if (lane == j) merge32(ww.rec[ql], sd.u, sd.v, dist);
           __syncwarp();
           fm &= fm - 1;
         }
@@ -459,9 +468,9 @@ __device__ __forceinline__ void invert_chunk(InvSmem<MODE>& sm, const Ctx& cx, c
       double tx = 0, ty = 0, tz = 0;
       auto start = [&]() {
         decode(task, ql, node);
-        tx = sm.sp64[warp][ql][0];
-        ty = sm.sp64[warp][ql][1];
-        tz = sm.sp64[warp][ql][2];
+        tx = ww.sp64[ql][0];
+        ty = ww.sp64[ql][1];
+        tz = ww.sp64[ql][2];
         sd.u = sm.ctr[node][0];
         sd.v = sm.ctr[node][1];
         sd.prev = INFINITY;
@@ -478,7 +487,7 @@ __device__ __forceinline__ void invert_chunk(InvSmem<MODE>& sm, const Ctx& cx, c
         if (active) {
           res = iterate64<P, Q>(cx, tx, ty, tz, sd);
           if (kJoinSeeds && res == kContinue && sd.newton) {
-            const Rec64& R = sm.rec[warp][ql];
+            const Rec64& R = ww.rec[ql];
             for (int k = 0; k < R.n; ++k)
               if (fabs(sd.u - R.u[k]) <= kJoin && fabs(sd.v - R.v[k]) <= kJoin) res = kFailed;
           }
@@ -489,7 +498,7 @@ __device__ __forceinline__ void invert_chunk(InvSmem<MODE>& sm, const Ctx& cx, c
         unsigned fm = __ballot_sync(FULL, done && keep);
         while (fm) {
           int j = __ffs(fm) - 1;
-          if (lane == j) merge64(sm.rec[warp][ql], sd.u, sd.v, rr);
+          if (lane == j) merge64(ww.rec[ql], sd.u, sd.v, rr);
           __syncwarp();
           fm &= fm - 1;
         }
@@ -510,7 +519,7 @@ __device__ __forceinline__ void invert_chunk(InvSmem<MODE>& sm, const Ctx& cx, c
     if (cnt == 0) {
       status = 2;  // NURBS_INV_NO_CANDIDATE
     } else if constexpr (MODE == kModeMixed) {
-      const Rec32 R = sm.rec[warp][lane];
+      const Rec32 R = ww.rec[lane];
       double us[2], vs[2], rs[2];
       int ns = 0;
       if (R.d1 < INFINITY) {
@@ -531,7 +540,7 @@ __device__ __forceinline__ void invert_chunk(InvSmem<MODE>& sm, const Ctx& cx, c
       }
       status = ns == 0 ? 3 : finish_status(us, vs, rs, ns, ou, ov, orr);
     } else {
-      const Rec64& R = sm.rec[warp][lane];
+      const Rec64& R = ww.rec[lane];
       status = R.n == 0 ? 3 : finish_status(R.u, R.v, R.r, R.n, ou, ov, orr);
     }
     if (valid) {

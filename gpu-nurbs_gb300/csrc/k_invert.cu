@@ -39,14 +39,15 @@ template <int P, int Q, int MODE>
 __global__ void __launch_bounds__(kThreads, MODE == kModeMixed ? kMinBlocksMixed : 4)
     k_invert(SurfDev s, const double* __restrict__ Pq, int64_t n, double* __restrict__ uv_out,
              int* __restrict__ st_out, double* __restrict__ res_out) {
-  __shared__ InvSmem<MODE> sm;
+  __shared__ Staged<kSmemSpans> sm;           // one surface for the whole CTA
+  __shared__ WarpWork<MODE> ww[kWarps];
   Ctx cx;
-  stage_surface<MODE>(s, sm, cx);
+  stage_surface<kSmemSpans>(s, sm, cx, threadIdx.x, blockDim.x);
   __syncthreads();
   const int warp = threadIdx.x >> 5;
   const int64_t chunks = (n + 31) / 32;
   for (int64_t ch = (int64_t)blockIdx.x * kWarps + warp; ch < chunks; ch += (int64_t)gridDim.x * kWarps)
-    invert_chunk<P, Q, MODE>(sm, cx, Pq, ch * 32, n, uv_out, st_out, res_out);
+    invert_chunk<P, Q, MODE, kSmemSpans>(sm, ww[warp], cx, Pq, ch * 32, n, uv_out, st_out, res_out);
 }
 
 template <int P, int Q>

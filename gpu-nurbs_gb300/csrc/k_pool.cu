@@ -1,13 +1,15 @@
 // Batched inversion over a pool of many surfaces of uneven degree, net size and query count,
 // in one persistent launch.
 //
-// The batch is cut on the host into tiles (surface, query range of at most tile_q queries);
-// persistent CTAs (a fixed number per SM) take tiles from a global atomic counter.  A CTA
-// stages the tile's surface (tree boxes, seeds, breakpoint tables) in shared memory when it
-// differs from the previous tile's, then its warps invert 32-query chunks of the tile with the
-// same per-warp task scheduler as the single-surface kernel (invert_core.cuh), dispatching on
-// the surface's degrees: (p,q) in {2,3,5}^2 run degree-specialised code, other degrees a
-// run-time-degree path.  Tile size and CTAs per SM are chosen by the pool's autotuner.
+// The batch is cut on the host into chunks (surface, query range of at most 32 queries, fewer
+// when the pool is configured for latency); every warp of the persistent CTAs takes chunks from
+// a global atomic counter on its own, stages the chunk's surface (tree boxes, seeds, breakpoint
+// tables for up to 64 spans per direction) in its own shared-memory area when it differs from
+// its previous chunk's, and inverts the chunk with the same task scheduler as the
+// single-surface kernel (invert_core.cuh).  Warps never wait for one another, so a batch of a
+// few thousand queries spreads over all SMs.  Degree dispatch: (p,q) in {2,3,5}^2 run
+// degree-specialised code, other degrees a run-time-degree path.  Chunk size and CTAs per SM
+// are chosen by the pool's autotuner.
 #include "invert_core.cuh"
 
 namespace gnurbs {
@@ -17,20 +19,23 @@ using namespace inv;
 
 // Each degree variant is its own (not inlined) function, so that it keeps its own register
 // allocation instead of the kernel taking the union of all variants' live ranges.
+constexpr int kPoolSpans = 64;  // breakpoint tables staged per warp up to this many spans
+
 template <int P, int Q, int MODE>
-__device__ __noinline__ void chunk_variant(InvSmem<MODE>& sm, const Ctx& cx, const double* __restrict__ P_,
-                                           int64_t q0, int64_t qend, double* __restrict__ uv, int* __restrict__ st,
-                                           double* __restrict__ res) {
-  invert_chunk<P, Q, MODE>(sm, cx, P_, q0, qend, uv, st, res);
+__device__ __noinline__ void chunk_variant(Staged<kPoolSpans>& sm, WarpWork<MODE>& ww, const Ctx& cx,
+                                           const double* __restrict__ P_, int64_t q0, int64_t qend,
+                                           double* __restrict__ uv, int* __restrict__ st, double* __restrict__ res) {
+  invert_chunk<P, Q, MODE, kPoolSpans>(sm, ww, cx, P_, q0, qend, uv, st, res);
 }
 
 template <int MODE>
-__device__ __forceinline__ void dispatch_chunk(InvSmem<MODE>& sm, const Ctx& cx, const double* __restrict__ P,
+__device__ __forceinline__ void dispatch_chunk(Staged<kPoolSpans>& sm, WarpWork<MODE>& ww, const Ctx& cx,
+                                               const double* __restrict__ P,
                                                int64_t q0, int64_t qend, double* __restrict__ uv, int* __restrict__ st,
                                                double* __restrict__ res) {
 #define GN_CASE(A, B)                                                 \
   if (cx.p == A && cx.q == B) {                                       \
-    chunk_variant<A, B, MODE>(sm, cx, P, q0, qend, uv, st, res);      \
+    chunk_variant<A, B, MODE>(sm, ww, cx, P, q0, qend, uv, st, res);  \
     return;                                                           \
   }
   GN_CASE(3, 3)
@@ -43,7 +48,7 @@ __device__ __forceinline__ void dispatch_chunk(InvSmem<MODE>& sm, const Ctx& cx,
   GN_CASE(3, 5)
   GN_CASE(5, 3)
 #undef GN_CASE
-  chunk_variant<0, 0, MODE>(sm, cx, P, q0, qend, uv, st, res);
+  chunk_variant<0, 0, MODE>(sm, ww, cx, P, q0, qend, uv, st, res);
 }
 
 template <int MODE>
@@ -51,28 +56,32 @@ __global__ void __launch_bounds__(kThreads, 4) k_invert_pool(const SurfDev* __re
                                                           const InvTile* __restrict__ tiles, int ntiles,
                                                           int* __restrict__ counter, const double* __restrict__ P,
                                                           double* __restrict__ uv, int* __restrict__ st,
-                                                          double* __restrict__ res) {
-  __shared__ InvSmem<MODE> sm;
-  __shared__ int s_tile;
+                                                          double* __restrict__ res, int group) {
+  __shared__ Staged<kPoolSpans> sm[kWarps];
+  __shared__ WarpWork<MODE> ww[kWarps];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   Ctx cx;
   int cur = -1;
-  const int warp = threadIdx.x >> 5;
   for (;;) {
-    if (threadIdx.x == 0) s_tile = atomicAdd(counter, 1);
-    __syncthreads();
-    const int t = s_tile;
-    if (t >= ntiles) break;
-    const InvTile T = tiles[t];
-    if (T.surf != cur) {
-      const SurfDev s = table[T.surf];
-      stage_surface<MODE>(s, sm, cx);
-      cur = T.surf;
-      __syncthreads();
+    // a group of consecutive chunks (mostly of one surface: chunks are listed surface by
+    // surface) per grab, so a warp restages rarely
+    int t0 = 0;
+    if (lane == 0) t0 = atomicAdd(counter, group);
+    t0 = __shfl_sync(0xffffffffu, t0, 0);
+    if (t0 >= ntiles) break;
+    const int t1 = min(t0 + group, ntiles);
+    for (int t = t0; t < t1; ++t) {
+      const InvTile T = tiles[t];
+      if (T.surf != cur) {
+        __syncwarp();
+        const SurfDev s = table[T.surf];
+        stage_surface<kPoolSpans>(s, sm[warp], cx, lane, 32);
+        cur = T.surf;
+        __syncwarp();
+      }
+      dispatch_chunk<MODE>(sm[warp], ww[warp], cx, P, T.begin, T.begin + T.count, uv, st, res);
+      __syncwarp();
     }
-    const int nch = (T.count + 31) >> 5;
-    for (int c = warp; c < nch; c += kWarps)
-      dispatch_chunk<MODE>(sm, cx, P, T.begin + 32 * (int64_t)c, T.begin + T.count, uv, st, res);
-    __syncthreads();
   }
 }
 
@@ -108,6 +117,73 @@ __global__ void __launch_bounds__(128) k_eval_pool(const SurfDev* __restrict__ t
   }
 }
 
+// CTA-granular schedule for large batches: a CTA takes a tile of up to 32*kWarps*k queries of
+// one surface, stages the surface once for its four warps, and the warps split the tile's
+// 32-query chunks.
+constexpr int kCtaSpans = 256;
+
+template <int P, int Q, int MODE>
+__device__ __noinline__ void chunk_variant_cta(Staged<kCtaSpans>& sm, WarpWork<MODE>& ww, const Ctx& cx,
+                                               const double* __restrict__ P_, int64_t q0, int64_t qend,
+                                               double* __restrict__ uv, int* __restrict__ st,
+                                               double* __restrict__ res) {
+  invert_chunk<P, Q, MODE, kCtaSpans>(sm, ww, cx, P_, q0, qend, uv, st, res);
+}
+
+template <int MODE>
+__device__ __forceinline__ void dispatch_chunk_cta(Staged<kCtaSpans>& sm, WarpWork<MODE>& ww, const Ctx& cx,
+                                                   const double* __restrict__ P, int64_t q0, int64_t qend,
+                                                   double* __restrict__ uv, int* __restrict__ st,
+                                                   double* __restrict__ res) {
+#define GN_CASE(A, B)                                                     \
+  if (cx.p == A && cx.q == B) {                                           \
+    chunk_variant_cta<A, B, MODE>(sm, ww, cx, P, q0, qend, uv, st, res);  \
+    return;                                                               \
+  }
+  GN_CASE(3, 3)
+  GN_CASE(2, 2)
+  GN_CASE(5, 5)
+  GN_CASE(2, 3)
+  GN_CASE(3, 2)
+  GN_CASE(2, 5)
+  GN_CASE(5, 2)
+  GN_CASE(3, 5)
+  GN_CASE(5, 3)
+#undef GN_CASE
+  chunk_variant_cta<0, 0, MODE>(sm, ww, cx, P, q0, qend, uv, st, res);
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(kThreads, 4) k_invert_pool_cta(const SurfDev* __restrict__ table,
+                                                              const InvTile* __restrict__ tiles, int ntiles,
+                                                              int* __restrict__ counter, const double* __restrict__ P,
+                                                              double* __restrict__ uv, int* __restrict__ st,
+                                                              double* __restrict__ res) {
+  __shared__ Staged<kCtaSpans> sm;
+  __shared__ WarpWork<MODE> ww[kWarps];
+  __shared__ int s_tile;
+  Ctx cx;
+  int cur = -1;
+  const int warp = threadIdx.x >> 5;
+  for (;;) {
+    if (threadIdx.x == 0) s_tile = atomicAdd(counter, 1);
+    __syncthreads();
+    const int t = s_tile;
+    if (t >= ntiles) break;
+    const InvTile T = tiles[t];
+    if (T.surf != cur) {
+      const SurfDev s = table[T.surf];
+      stage_surface<kCtaSpans>(s, sm, cx, threadIdx.x, blockDim.x);
+      cur = T.surf;
+      __syncthreads();
+    }
+    const int nch = (T.count + 31) >> 5;
+    for (int c = warp; c < nch; c += kWarps)
+      dispatch_chunk_cta<MODE>(sm, ww[warp], cx, P, T.begin + 32 * (int64_t)c, T.begin + T.count, uv, st, res);
+    __syncthreads();
+  }
+}
+
 }  // namespace
 
 cudaError_t launch_eval_pool(const SurfDev* table, const InvTile* tiles, int ntiles, const double* uv, int64_t n,
@@ -121,16 +197,31 @@ cudaError_t launch_eval_pool(const SurfDev* table, const InvTile* tiles, int nti
 }
 
 cudaError_t launch_invert_pool(const SurfDev* table, const InvTile* tiles, int ntiles, int* counter, const double* P,
-                               double* uv, int* status, double* residual, int precision, int ctas, int /*unused*/,
+                               double* uv, int* status, double* residual, int precision, int ctas, int tile_queries,
                                cudaStream_t st) {
   if (ntiles <= 0) return cudaSuccess;
   cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(int), st);
   if (e != cudaSuccess) return e;
-  if (ctas > ntiles) ctas = ntiles;
+  if (tile_queries > 32) {  // CTA tiles
+    if (ctas > ntiles) ctas = ntiles;
+    if (precision == 1)
+      k_invert_pool_cta<kModeMixed><<<ctas, kThreads, 0, st>>>(table, tiles, ntiles, counter, P, uv, status, residual);
+    else
+      k_invert_pool_cta<kModeFP64><<<ctas, kThreads, 0, st>>>(table, tiles, ntiles, counter, P, uv, status, residual);
+    return cudaGetLastError();
+  }
+  const int warps_needed = ntiles;
+  if (ctas * kWarps > warps_needed) ctas = (warps_needed + kWarps - 1) / kWarps;
+  // chunks per grab: large batches take up to 8 at a time, while every warp still gets about
+  // eight grabs so the tail stays short
+  int group = ntiles / (ctas * kWarps * 8);
+  group = group < 1 ? 1 : (group > 8 ? 8 : group);
   if (precision == 1)
-    k_invert_pool<kModeMixed><<<ctas, kThreads, 0, st>>>(table, tiles, ntiles, counter, P, uv, status, residual);
+    k_invert_pool<kModeMixed><<<ctas, kThreads, 0, st>>>(table, tiles, ntiles, counter, P, uv, status, residual,
+                                                          group);
   else
-    k_invert_pool<kModeFP64><<<ctas, kThreads, 0, st>>>(table, tiles, ntiles, counter, P, uv, status, residual);
+    k_invert_pool<kModeFP64><<<ctas, kThreads, 0, st>>>(table, tiles, ntiles, counter, P, uv, status, residual,
+                                                         group);
   return cudaGetLastError();
 }
 

@@ -100,7 +100,7 @@ cudaError_t launch_eval_pool(const SurfDev* table, const InvTile* tiles, int nti
                              unsigned mask, double* out, cudaStream_t st);
 cudaError_t launch_invert_pool(const SurfDev* table, const InvTile* tiles, int ntiles, int* counter,
                                const double* P, double* uv, int* status, double* residual, int precision,
-                               int ctas, int tile_warp_chunks, cudaStream_t st);
+                               int ctas, int tile_queries, cudaStream_t st);
 
 // stage d
 cudaError_t launch_invert(const SurfDev& s, const double* P, int64_t n, double* uv, int* status,

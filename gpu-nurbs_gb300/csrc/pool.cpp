@@ -118,7 +118,7 @@ struct nurbs_pool_s {
   int max_surfaces = 0;
   std::vector<PoolSurface> surf;
   SurfDev* d_table = nullptr;  // device table of max_surfaces records (outside the arena)
-  int tile_queries = 256;
+  int tile_queries = 128;
   int ctas_per_sm = 4;
   int sms = 152;
   std::map<cudaStream_t, Workspace> ws;
@@ -192,7 +192,7 @@ int workspace_for(nurbs_pool_t P, cudaStream_t st, size_t ntiles, Workspace*& ou
 }
 
 int run_tiles(nurbs_pool_t P, const std::vector<InvTile>& tiles, const double* Pd, double* uv, int* st_out,
-              double* res, int precision, cudaStream_t st, int ctas_per_sm) {
+              double* res, int precision, cudaStream_t st, int ctas_per_sm, int tile_q) {
   if (tiles.empty()) return NURBS_OK;
   Workspace* w = nullptr;
   int rc = workspace_for(P, st, tiles.size(), w);
@@ -204,7 +204,7 @@ int run_tiles(nurbs_pool_t P, const std::vector<InvTile>& tiles, const double* P
   if (e == cudaSuccess) e = cudaEventRecord(w->ev, st);
   if (e == cudaSuccess)
     e = launch_invert_pool(P->d_table, (const InvTile*)(dev + 256), (int)tiles.size(), (int*)dev, Pd, uv, st_out, res,
-                           precision, P->sms * ctas_per_sm, 0, st);
+                           precision, P->sms * ctas_per_sm, tile_q, st);
   if (e != cudaSuccess) return pfail(NURBS_E_CUDA, "pool inversion: %s", cudaGetErrorString(e));
   return NURBS_OK;
 }
@@ -472,8 +472,9 @@ int nurbs_pool_surface_bytes(int p, int q, int nu, int nv, const double* ku, con
 }
 
 int nurbs_pool_set_config(nurbs_pool_t P, int tile_queries, int ctas_per_sm) {
-  if (!P || tile_queries < 32 || tile_queries % 32 || ctas_per_sm < 1 || ctas_per_sm > 16)
-    return pfail(NURBS_E_INVALID, "tile_queries must be a positive multiple of 32, ctas_per_sm in 1..16");
+  if (!P || tile_queries < 1 || (tile_queries > 32 && tile_queries % 32) || ctas_per_sm < 1 || ctas_per_sm > 16)
+    return pfail(NURBS_E_INVALID, "tile_queries must be 1..32 (warp chunks) or a multiple of 32 (CTA tiles), "
+                                  "ctas_per_sm in 1..16");
   std::lock_guard<std::mutex> lock(P->mu);
   P->tile_queries = tile_queries;
   P->ctas_per_sm = ctas_per_sm;
@@ -487,7 +488,7 @@ int nurbs_pool_invert(nurbs_pool_t P, int nbatch, const int* ids, const int64_t*
   std::lock_guard<std::mutex> lock(P->mu);
   std::vector<InvTile> tiles;
   if ((rc = make_tiles(P, nbatch, ids, offsets, P->tile_queries, tiles))) return rc;
-  return run_tiles(P, tiles, Pd, uv, st_out, res, precision, (cudaStream_t)stream, P->ctas_per_sm);
+  return run_tiles(P, tiles, Pd, uv, st_out, res, precision, (cudaStream_t)stream, P->ctas_per_sm, P->tile_queries);
 }
 
 int nurbs_pool_eval(nurbs_pool_t P, int nbatch, const int* ids, const int64_t* offsets, const double* uv, int64_t n,
@@ -498,7 +499,7 @@ int nurbs_pool_eval(nurbs_pool_t P, int nbatch, const int* ids, const int64_t* o
   if (nbatch > 0 && offsets[nbatch] > n) return pfail(NURBS_E_INVALID, "offsets exceed n");
   std::lock_guard<std::mutex> lock(P->mu);
   std::vector<InvTile> tiles;
-  int rc = make_tiles(P, nbatch, ids, offsets, 1024, tiles);
+  int rc = make_tiles(P, nbatch, ids, offsets, 1024, tiles);  // evaluation tiles: one CTA each
   if (rc) return rc;
   if (tiles.empty()) return NURBS_OK;
   cudaStream_t st = (cudaStream_t)stream;
@@ -546,7 +547,8 @@ int nurbs_pool_autotune(nurbs_pool_t P, int nbatch, const int* ids, const int64_
         return NURBS_OK;
       }
   }
-  const int tile_opts[] = {128, 256, 512, 1024};
+  // above 32: CTA tiles (throughput); 32 and below: warp chunks (latency, small batches)
+  const int tile_opts[] = {128, 256, 32, 16};
   const int cta_opts[] = {2, 3, 4};
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
@@ -565,7 +567,7 @@ int nurbs_pool_autotune(nurbs_pool_t P, int nbatch, const int* ids, const int64_
         cudaEventRecord(e0, st);
         {
           std::lock_guard<std::mutex> lock(P->mu);
-          rc = run_tiles(P, tiles, Pd, uv, st_out, res, precision, st, c);
+          rc = run_tiles(P, tiles, Pd, uv, st_out, res, precision, st, c, t);
         }
         cudaEventRecord(e1, st);
         cudaEventSynchronize(e1);
@@ -619,7 +621,7 @@ int nurbs_pool_graph_create(nurbs_pool_t P, int nbatch, const int* ids, const in
   if (e == cudaSuccess) e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
   if (e == cudaSuccess) {
     cudaError_t le = launch_invert_pool(P->d_table, (const InvTile*)(dev + 256), (int)tiles.size(), (int*)dev, Pd, uv,
-                                        st_out, res, precision, P->sms * P->ctas_per_sm, 0, cs);
+                                        st_out, res, precision, P->sms * P->ctas_per_sm, P->tile_queries, cs);
     e = cudaStreamEndCapture(cs, &G->graph);
     if (le != cudaSuccess) e = le;
   }

@@ -9,9 +9,10 @@
 //    arrived meanwhile (FIFO, up to max_batch_queries), grouped by surface, then
 //    H2D copy -> nurbs_pool_invert -> D2H copies -> event, all on the slot's stream.  Requests
 //    arriving while batches run are admitted as soon as a slot frees: batches overlap on the GPU.
-//  * uploader — converts uploaded surfaces into the pool on its own stream (nurbs_pool_add keeps
-//    the pool lock only to reserve and publish, so inversions continue meanwhile).  When the
-//    budget is full it evicts least-recently-used surfaces that no queued request references.
+//  * uploader — converts uploaded surfaces into the pool on its own stream, all uploads queued
+//    at that moment in one batch (nurbs_pool_add keeps the pool lock only to reserve and
+//    publish, so inversions continue meanwhile).  When the budget is full it evicts
+//    least-recently-used surfaces that no queued request references.
 // Every wait is bounded; nothing spins on the GPU.
 #include <cuda_runtime.h>
 
@@ -59,6 +60,7 @@ struct Request {
 struct Slot {
   cudaStream_t stream = nullptr;
   cudaEvent_t done = nullptr;
+  cudaEvent_t begin = nullptr;  // timing: batch start on the slot's stream
   size_t off = 0, bytes = 0;
   char* dev = nullptr;
   double* hP = nullptr;
@@ -92,6 +94,7 @@ struct nurbs_server_s {
   uint64_t next_ticket = 1;
   int64_t n_batches = 0, n_batch_queries = 0, n_completed = 0;
   int in_flight_requests = 0;
+  double gpu_ms = 0, dispatch_us = 0, retire_us = 0;
 };
 
 namespace {
@@ -113,6 +116,9 @@ void complete(nurbs_server_s* S, Request* r, int result) {
 }
 
 void retire(nurbs_server_s* S, Slot& sl, int result) {
+  const Clock::time_point t0 = Clock::now();
+  float ms = 0;
+  if (result == NURBS_OK) cudaEventElapsedTime(&ms, sl.begin, sl.done);
   int64_t o = 0;
   for (size_t k = 0; k < sl.reqs.size(); ++k) {
     Request* r = sl.reqs[k];
@@ -128,11 +134,14 @@ void retire(nurbs_server_s* S, Slot& sl, int result) {
   sl.reqs.clear();
   sl.req_off.clear();
   sl.busy = false;
+  S->gpu_ms += ms;
+  S->retire_us += std::chrono::duration<double, std::micro>(Clock::now() - t0).count();
   S->cv_done.notify_all();
 }
 
 // Fills a free slot from the pending queue; returns true if a batch was launched.
 bool dispatch(nurbs_server_s* S, Slot& sl, std::deque<Request*>& pending) {
+  const Clock::time_point t0 = Clock::now();
   const int64_t cap = S->cfg.max_batch_queries;
   int64_t total = 0;
   while (!pending.empty() && total + pending.front()->n <= cap &&
@@ -164,7 +173,8 @@ bool dispatch(nurbs_server_s* S, Slot& sl, std::deque<Request*>& pending) {
   double* duv = (double*)(sl.dev + align256(cap3 * 24));
   int* dst = (int*)(sl.dev + align256(cap3 * 24) + align256(cap3 * 16));
   double* dres = (double*)(sl.dev + align256(cap3 * 24) + align256(cap3 * 16) + align256(cap3 * 4));
-  cudaError_t e = cudaMemcpyAsync(dP, sl.hP, o * 24, cudaMemcpyHostToDevice, sl.stream);
+  cudaError_t e = cudaEventRecord(sl.begin, sl.stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dP, sl.hP, o * 24, cudaMemcpyHostToDevice, sl.stream);
   int rc = e == cudaSuccess ? NURBS_OK : NURBS_E_CUDA;
   if (rc == NURBS_OK)
     rc = nurbs_pool_invert(S->pool, (int)ids.size(), ids.data(), offs.data(), dP, duv, dst, dres, S->cfg.precision,
@@ -186,6 +196,7 @@ bool dispatch(nurbs_server_s* S, Slot& sl, std::deque<Request*>& pending) {
     std::lock_guard<std::mutex> lock(S->mu);
     S->n_batches++;
     S->n_batch_queries += o;
+    S->dispatch_us += std::chrono::duration<double, std::micro>(Clock::now() - t0).count();
   }
   return true;
 }
@@ -234,41 +245,63 @@ void scheduler_main(nurbs_server_s* S) {
   S->cv_done.notify_all();
 }
 
+// One upload with LRU eviction when the budget is full.
+int upload_one(nurbs_server_s* S, Request* r, int* id) {
+  int rc = nurbs_pool_add(S->pool, 1, &r->desc, S->up_stream, id);
+  while (rc == NURBS_E_BUDGET) {
+    // evict the least recently used surface no queued request references
+    int victim = -1;
+    {
+      std::lock_guard<std::mutex> lock(S->mu);
+      Clock::time_point oldest = Clock::time_point::max();
+      for (auto& kv : S->last_use)
+        if (!S->refs.count(kv.first) && kv.second < oldest) {
+          oldest = kv.second;
+          victim = kv.first;
+        }
+      if (victim >= 0) S->last_use.erase(victim);
+    }
+    if (victim < 0 || pool_release_surface(S->pool, victim) != NURBS_OK) break;
+    rc = nurbs_pool_add(S->pool, 1, &r->desc, S->up_stream, id);
+  }
+  return rc;
+}
+
 void uploader_main(nurbs_server_s* S) {
+  constexpr int kMaxBatch = 64;  // uploads converted together (one copy, one launch per stage)
+  std::vector<Request*> batch;
+  std::vector<nurbs_surface_desc> descs;
+  std::vector<int> ids;
   while (!S->stop.load()) {
-    Request* r = nullptr;
+    batch.clear();
     {
       std::unique_lock<std::mutex> lock(S->mu);
       S->cv_work.wait_for(lock, std::chrono::milliseconds(2), [&] { return !S->uploads.empty() || S->stop.load(); });
-      if (S->uploads.empty()) continue;
-      r = S->uploads.front();
-      S->uploads.pop_front();
-    }
-    int id = -1;
-    int rc = nurbs_pool_add(S->pool, 1, &r->desc, S->up_stream, &id);
-    while (rc == NURBS_E_BUDGET) {
-      // evict the least recently used surface no queued request references
-      int victim = -1;
-      {
-        std::lock_guard<std::mutex> lock(S->mu);
-        Clock::time_point oldest = Clock::time_point::max();
-        for (auto& kv : S->last_use)
-          if (!S->refs.count(kv.first) && kv.second < oldest) {
-            oldest = kv.second;
-            victim = kv.first;
-          }
-        if (victim >= 0) S->last_use.erase(victim);
+      while (!S->uploads.empty() && (int)batch.size() < kMaxBatch) {
+        batch.push_back(S->uploads.front());
+        S->uploads.pop_front();
       }
-      if (victim < 0 || pool_release_surface(S->pool, victim) != NURBS_OK) break;
-      rc = nurbs_pool_add(S->pool, 1, &r->desc, S->up_stream, &id);
+    }
+    if (batch.empty()) continue;
+    descs.resize(batch.size());
+    ids.assign(batch.size(), -1);
+    for (size_t k = 0; k < batch.size(); ++k) descs[k] = batch[k]->desc;
+    std::vector<int> rcs(batch.size(), NURBS_OK);
+    int rc = nurbs_pool_add(S->pool, (int)batch.size(), descs.data(), S->up_stream, ids.data());
+    if (rc != NURBS_OK) {
+      // a refusal of the whole batch (budget, or one invalid surface): one at a time, evicting
+      for (size_t k = 0; k < batch.size(); ++k) rcs[k] = upload_one(S, batch[k], &ids[k]);
     }
     std::lock_guard<std::mutex> lock(S->mu);
-    if (rc == NURBS_OK) {
-      r->surf = id;
-      if (r->id_out) *r->id_out = id;
-      S->last_use[id] = Clock::now();
+    for (size_t k = 0; k < batch.size(); ++k) {
+      Request* r = batch[k];
+      if (rcs[k] == NURBS_OK) {
+        r->surf = ids[k];
+        if (r->id_out) *r->id_out = ids[k];
+        S->last_use[ids[k]] = Clock::now();
+      }
+      complete(S, r, rcs[k]);
     }
-    complete(S, r, rc);
     S->cv_done.notify_all();
   }
   std::lock_guard<std::mutex> lock(S->mu);
@@ -299,6 +332,7 @@ void free_slots(nurbs_server_s* S) {
   for (auto& sl : S->slots) {
     if (sl.stream) cudaStreamDestroy(sl.stream);
     if (sl.done) cudaEventDestroy(sl.done);
+    if (sl.begin) cudaEventDestroy(sl.begin);
     if (sl.hP) cudaFreeHost(sl.hP);
     if (sl.huv) cudaFreeHost(sl.huv);
     if (sl.hst) cudaFreeHost(sl.hst);
@@ -333,7 +367,7 @@ int nurbs_server_create(nurbs_pool_t pool, const nurbs_server_config* cfg, nurbs
       break;
     }
     if (cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreate(&sl.done) != cudaSuccess || cudaEventCreate(&sl.begin) != cudaSuccess ||
         cudaMallocHost((void**)&sl.hP, cap * 24) != cudaSuccess ||
         cudaMallocHost((void**)&sl.huv, cap * 16) != cudaSuccess ||
         cudaMallocHost((void**)&sl.hst, cap * 4) != cudaSuccess ||
@@ -500,6 +534,9 @@ int nurbs_server_stats(nurbs_server_t S, nurbs_server_stats_t* st) {
   st->batches = S->n_batches;
   st->batch_queries = S->n_batch_queries;
   st->in_flight = S->in_flight_requests;
+  st->gpu_ms = S->gpu_ms;
+  st->dispatch_us = S->dispatch_us;
+  st->retire_us = S->retire_us;
   return NURBS_OK;
 }
 

@@ -217,7 +217,10 @@ int nurbs_pool_info(nurbs_pool_t pool, nurbs_pool_info_t* info);
 int nurbs_pool_surface_bytes(int degree_u, int degree_v, int cp_u, int cp_v, const double* knots_u,
                              const double* knots_v, int64_t* bytes);
 const char* nurbs_pool_last_error(void);
-/* Launch configuration: queries per tile (multiple of 32) and persistent CTAs per SM. */
+/* Launch configuration and persistent CTAs per SM.  tile_queries > 32 (a multiple of 32): each
+ * CTA takes tiles of that many queries of one surface (throughput on large batches);
+ * tile_queries <= 32: each warp takes chunks of that many queries on its own (small batches
+ * spread over all SMs; fewer queries per warp lowers latency). */
 int nurbs_pool_set_config(nurbs_pool_t pool, int tile_queries, int ctas_per_sm);
 /* Batched inversion.  Queries are grouped by surface: surface ids_host[k] owns the queries
  * [offsets_host[k], offsets_host[k+1]) of P_dev (3 doubles each); outputs are indexed like P.
@@ -264,6 +267,9 @@ typedef struct {
 typedef struct {
     int64_t completed, batches, batch_queries;
     int in_flight;
+    double gpu_ms;        /* sum over batches of stream time from H2D start to D2H end */
+    double dispatch_us;   /* scheduler host time forming and enqueuing batches */
+    double retire_us;     /* scheduler host time copying results back */
 } nurbs_server_stats_t;
 
 int nurbs_server_create(nurbs_pool_t pool, const nurbs_server_config* cfg, nurbs_server_t* out);
