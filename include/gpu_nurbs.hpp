@@ -8,6 +8,8 @@
 //   nurbs::Surface  a device-resident surface in matrix form with its subdivision tree:
 //                   matrix_n() = GetMatrixN layout, eval() = batched S..Svv,
 //                   candidates() = the NewInverse scan, invert() = NewInverse + GaussNewton
+//   nurbs::Pool     many surfaces under a device budget, batched invert/eval, autotune, graphs
+//   nurbs::Server   the continuous-batching request loop over a pool (submit / wait / drain)
 //   nurbs::Error    thrown for any non-zero status (message from nurbs_last_error)
 #pragma once
 #include <cstdint>
@@ -133,6 +135,139 @@ class Surface {
     h_ = nullptr;
   }
   nurbs_surface_t h_ = nullptr;
+};
+
+inline nurbs_surface_desc view(const SurfaceDesc& s) {
+  return {s.degree_u, s.degree_v, s.cp_u, s.cp_v, s.knots_u.data(), s.knots_v.data(), s.cps.data(), s.weights.data()};
+}
+
+// One batch layout: surface ids[k] owns queries [offsets[k], offsets[k+1]).
+struct Batch {
+  std::vector<int> ids;
+  std::vector<int64_t> offsets;
+  int size() const { return (int)ids.size(); }
+};
+
+// A captured batched inversion (nurbs_pool_graph_create); replays on new query values.
+class Graph {
+ public:
+  explicit Graph(nurbs_graph_t g) : g_(g) {}
+  Graph(const Graph&) = delete;
+  Graph& operator=(const Graph&) = delete;
+  Graph(Graph&& o) noexcept : g_(std::exchange(o.g_, nullptr)) {}
+  ~Graph() {
+    if (g_) nurbs_graph_destroy(g_);
+  }
+  void launch(void* stream = nullptr) const { check(nurbs_graph_launch(g_, stream), "nurbs_graph_launch"); }
+
+ private:
+  nurbs_graph_t g_ = nullptr;
+};
+
+// Many surfaces under one device-memory budget, inverted and evaluated in one launch.
+class Pool {
+ public:
+  explicit Pool(int64_t budget_bytes, int max_surfaces = 65536) {
+    check(nurbs_pool_create(budget_bytes, max_surfaces, &h_), "nurbs_pool_create");
+  }
+  Pool(const Pool&) = delete;
+  Pool& operator=(const Pool&) = delete;
+  ~Pool() {
+    if (h_) nurbs_pool_destroy(h_);
+  }
+  nurbs_pool_t handle() const { return h_; }
+
+  std::vector<int> add(const std::vector<SurfaceDesc>& surfaces, void* stream = nullptr) {
+    std::vector<nurbs_surface_desc> d;
+    for (const SurfaceDesc& s : surfaces) d.push_back(view(s));
+    std::vector<int> ids(d.size());
+    check(nurbs_pool_add(h_, (int)d.size(), d.data(), stream, ids.data()), "nurbs_pool_add");
+    return ids;
+  }
+  void remove(int id, void* stream = nullptr) { check(nurbs_pool_remove(h_, id, stream), "nurbs_pool_remove"); }
+  nurbs_pool_info_t info() const {
+    nurbs_pool_info_t i{};
+    check(nurbs_pool_info(h_, &i), "nurbs_pool_info");
+    return i;
+  }
+  void set_config(int tile_queries, int ctas_per_sm) {
+    check(nurbs_pool_set_config(h_, tile_queries, ctas_per_sm), "nurbs_pool_set_config");
+  }
+  void invert(const Batch& b, const double* P_dev, double* uv_dev, int* status_dev, double* residual_dev,
+              int precision = NURBS_PREC_MIXED, void* stream = nullptr) const {
+    check(nurbs_pool_invert(h_, b.size(), b.ids.data(), b.offsets.data(), P_dev, uv_dev, status_dev, residual_dev,
+                            precision, stream),
+          "nurbs_pool_invert");
+  }
+  void eval(const Batch& b, const double* uv_dev, unsigned mask, double* out_dev, void* stream = nullptr) const {
+    check(nurbs_pool_eval(h_, b.size(), b.ids.data(), b.offsets.data(), uv_dev, b.offsets.back(), mask, out_dev,
+                          stream),
+          "nurbs_pool_eval");
+  }
+  // Times the launch configurations on the batch and keeps the fastest; returns {tile, ctas}.
+  std::pair<int, int> autotune(const Batch& b, const double* P_dev, double* uv_dev, int* status_dev,
+                               double* residual_dev, int precision = NURBS_PREC_MIXED, int64_t max_queries = 0,
+                               const char* cache_path = nullptr, void* stream = nullptr) {
+    int tile = 0, ctas = 0;
+    float ms = 0;
+    check(nurbs_pool_autotune(h_, b.size(), b.ids.data(), b.offsets.data(), P_dev, uv_dev, status_dev, residual_dev,
+                              precision, max_queries, cache_path, stream, &tile, &ctas, &ms),
+          "nurbs_pool_autotune");
+    return {tile, ctas};
+  }
+  Graph graph(const Batch& b, const double* P_dev, double* uv_dev, int* status_dev, double* residual_dev,
+              int precision = NURBS_PREC_MIXED) const {
+    nurbs_graph_t g = nullptr;
+    check(nurbs_pool_graph_create(h_, b.size(), b.ids.data(), b.offsets.data(), P_dev, uv_dev, status_dev,
+                                  residual_dev, precision, &g),
+          "nurbs_pool_graph_create");
+    return Graph(g);
+  }
+
+ private:
+  nurbs_pool_t h_ = nullptr;
+};
+
+// The continuous-batching request loop over a pool (the pool must outlive it).
+class Server {
+ public:
+  Server(Pool& pool, const nurbs_server_config& cfg) { check(nurbs_server_create(pool.handle(), &cfg, &h_), "nurbs_server_create"); }
+  Server(const Server&) = delete;
+  Server& operator=(const Server&) = delete;
+  ~Server() {
+    if (h_) nurbs_server_destroy(h_);
+  }
+  nurbs_server_t handle() const { return h_; }
+  // Host buffers stay owned by the caller and must live until the request completes.
+  uint64_t submit_invert(int surf_id, const double* P, int64_t n, double* uv, int* status, double* residual,
+                         double* latency_us = nullptr) {
+    uint64_t t = 0;
+    check(nurbs_server_submit_invert(h_, surf_id, P, n, uv, status, residual, latency_us, &t),
+          "nurbs_server_submit_invert");
+    return t;
+  }
+  uint64_t submit_upload(const SurfaceDesc& s, int* surf_id_out, double* latency_us = nullptr) {
+    nurbs_surface_desc d = view(s);
+    uint64_t t = 0;
+    check(nurbs_server_submit_upload(h_, &d, surf_id_out, latency_us, &t), "nurbs_server_submit_upload");
+    return t;
+  }
+  // The request's own status (NURBS_OK or its error); throws on a timeout or a bad ticket.
+  int wait(uint64_t ticket, int timeout_ms = 10000) {
+    int result = 0;
+    check(nurbs_server_wait(h_, ticket, timeout_ms, &result), "nurbs_server_wait");
+    return result;
+  }
+  void drain(int timeout_ms = 60000) { check(nurbs_server_drain(h_, timeout_ms), "nurbs_server_drain"); }
+  void pause(bool paused) { check(nurbs_server_pause(h_, paused ? 1 : 0), "nurbs_server_pause"); }
+  nurbs_server_stats_t stats() const {
+    nurbs_server_stats_t s{};
+    check(nurbs_server_stats(h_, &s), "nurbs_server_stats");
+    return s;
+  }
+
+ private:
+  nurbs_server_t h_ = nullptr;
 };
 
 }  // namespace nurbs
