@@ -3,7 +3,9 @@
 Each translation unit is compiled by nvcc in parallel, then linked into one shared library
 next to this file.  Translation units whose results must be bit-identical to the
 reference's unfused FP64 arithmetic (span conversion, subdivision tree, legacy drop-in
-kernels) are compiled with --fmad=false.
+kernels) are compiled with --fmad=false.  So are the evaluation and inversion kernels: their
+arithmetic writes each fused multiply-add explicitly, and without compiler contraction a
+point's result is the same in every kernel that computes it (single surface, pool, graph).
 """
 from __future__ import annotations
 
@@ -23,6 +25,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-I" + INCLUDE, "-I" + CSRC,
           "--expt-relaxed-constexpr", "-Wno-deprecated-gpu-targets"]
 EXACT_TUS = {"k_convert.cu", "k_tree.cu", "k_legacy.cu"}
+EXPLICIT_FMA_TUS = {"k_eval.cu", "k_invert.cu", "k_pool.cu"}
 SOURCES = ["k_convert.cu", "k_tree.cu", "k_legacy.cu", "k_eval.cu", "k_invert.cu", "api.cpp", "nu_io.cpp", "k_probe.cu", "k_static.cu", "k_pool.cu", "pool.cpp", "server.cpp"]
 
 
@@ -41,7 +44,7 @@ def _compile(src: str, verbose: bool) -> str:
     if os.path.exists(obj) and os.path.getmtime(obj) >= max(os.path.getmtime(d) for d in deps):
         return obj
     cmd = [nvcc()] + ARCH + COMMON
-    if src in EXACT_TUS:
+    if src in EXACT_TUS or src in EXPLICIT_FMA_TUS:
         cmd.append("--fmad=false")
     if src.endswith(".cpp"):
         cmd += ["-x", "cu"]

@@ -37,33 +37,44 @@ constexpr bool kJoinSeeds = false;
 constexpr int kSols = 4;                // FP64 mode: distinct minima kept per query
 constexpr int kSmemSpans = 256;         // breakpoint tables staged in shared memory up to this
 
+// Arithmetic below writes every product that feeds a sum as an explicit FMA (the translation
+// units are compiled with --fmad=false), so a seed's trajectory is the same bit for bit in
+// every kernel that runs it: results do not depend on the kernel, the batch or the schedule.
 template <typename T>
 __device__ __forceinline__ T dot3(const v3<T>& a, const v3<T>& b) {
-  return a.x * b.x + a.y * b.y + a.z * b.z;
+  return fast::mad(a.z, b.z, fast::mad(a.y, b.y, a.x * b.x));
+}
+template <typename T, typename TH>
+__device__ __forceinline__ T dot3c(const v3<T>& a, const v3<TH>& b) {  // b converted to T
+  return fast::mad(a.z, (T)b.z, fast::mad(a.y, (T)b.y, a.x * (T)b.x));
+}
+template <typename T>
+__device__ __forceinline__ T det2(T h00, T h01, T h11) {
+  return fast::mad(h00, h11, -(h01 * h01));
 }
 
 // One (Gauss-)Newton step from the derivatives at C.  Returns false when the system is
-// singular.  Newton uses H = J^T J + r.d2S when that H is positive definite.
-template <typename T, typename TH>
+// singular.  Newton uses H = J^T J + r.d2S when that H is positive definite, else the
+// Gauss-Newton matrix J^T J (the reference's update, kernel.cu:195-243).  FAST: FP32
+// reciprocal by the hardware approximation.
+template <typename T, typename TH, bool FAST>
 __device__ __forceinline__ bool solve_step(const v3<T>& r, const v3<T>& Su, const v3<T>& Sv, const v3<TH>& Suu,
                                            const v3<TH>& Suv, const v3<TH>& Svv, bool newton, T& du, T& dv) {
-  T a00 = dot3(Su, Su), a01 = dot3(Su, Sv), a11 = dot3(Sv, Sv);
-  T g0 = dot3(Su, r), g1 = dot3(Sv, r);
+  T h00 = dot3(Su, Su), h01 = dot3(Su, Sv), h11 = dot3(Sv, Sv);
+  const T g0 = dot3(Su, r), g1 = dot3(Sv, r);
   if (newton) {
-    T h00 = a00 + (T)(r.x * (T)Suu.x + r.y * (T)Suu.y + r.z * (T)Suu.z);
-    T h01 = a01 + (T)(r.x * (T)Suv.x + r.y * (T)Suv.y + r.z * (T)Suv.z);
-    T h11 = a11 + (T)(r.x * (T)Svv.x + r.y * (T)Svv.y + r.z * (T)Svv.z);
-    T det = h00 * h11 - h01 * h01;
-    if (h00 > T(0) && det > T(0)) {
-      du = (h11 * g0 - h01 * g1) / det;
-      dv = (h00 * g1 - h01 * g0) / det;
-      return true;
+    const T n00 = h00 + dot3c(r, Suu), n01 = h01 + dot3c(r, Suv), n11 = h11 + dot3c(r, Svv);
+    if (n00 > T(0) && det2(n00, n01, n11) > T(0)) {
+      h00 = n00;
+      h01 = n01;
+      h11 = n11;
     }
   }
-  T det = a00 * a11 - a01 * a01;
+  const T det = det2(h00, h01, h11);
   if (!(det > T(0))) return false;
-  du = (a11 * g0 - a01 * g1) / det;
-  dv = (a00 * g1 - a01 * g0) / det;
+  const T inv = fast::rcp<FAST>(det);
+  du = fast::mad(h11, g0, -(h01 * g1)) * inv;
+  dv = fast::mad(h00, g1, -(h01 * g0)) * inv;
   return true;
 }
 
@@ -88,22 +99,23 @@ struct Seed {
 enum StepResult { kContinue = 0, kConverged = 1, kFailed = 2 };
 
 // One FP32 iteration of a seed.  Convergence: the step is at the FP32 resolution of the
-// parameters (rounding of S mapped through the shorter tangent), or Newton steps stop shrinking.
+// parameters (rounding of S mapped through the shorter tangent: step * |S_t|min <= 8 ulp(|S|)),
+// or Newton steps stop shrinking.  dist2 = |S - P|^2 before the step.
 template <int P, int Q>
-__device__ __forceinline__ int iterate32(const Ctx& c, float px, float py, float pz, Seed<float>& st, float& dist) {
-  fast::SDer<float> d = fast::eval_at<float, P, Q, 2>(c.L32, c.m32, c.p, c.q, st.u, st.v, st.hu, st.hv);
+__device__ __forceinline__ int iterate32(const Ctx& c, float px, float py, float pz, Seed<float>& st, float& dist2) {
+  fast::SDer<float> d = fast::eval_at<float, P, Q, 2, true>(c.L32, c.m32, c.p, c.q, st.u, st.v, st.hu, st.hv);
   v3<float> r = {d.S.x - px, d.S.y - py, d.S.z - pz};
   float du, dv;
-  if (!solve_step<float, float>(r, d.Su, d.Sv, d.Suu, d.Suv, d.Svv, st.newton, du, dv)) return kFailed;
+  if (!solve_step<float, float, true>(r, d.Su, d.Sv, d.Suu, d.Suv, d.Svv, st.newton, du, dv)) return kFailed;
   if (!(isfinite(du) && isfinite(dv))) return kFailed;
   st.u -= du;
   st.v -= dv;
   float step = fmaxf(fabsf(du), fabsf(dv));
-  dist = sqrtf(dot3(r, r));
+  dist2 = dot3(r, r);
   float smag = fmaxf(fmaxf(fabsf(d.S.x), fabsf(d.S.y)), fmaxf(fabsf(d.S.z), 1.0f));
-  float tmin = sqrtf(fminf(dot3(d.Su, d.Su), dot3(d.Sv, d.Sv)));
-  float floor32 = 8.0f * 5.96e-8f * smag / fmaxf(tmin, 1e-30f);
-  if (step <= fmaxf(kTol32, floor32)) return kConverged;
+  float tmin2 = fminf(dot3(d.Su, d.Su), dot3(d.Sv, d.Sv));
+  float fl = 8.0f * 5.96e-8f * smag;
+  if (step <= kTol32 || step * step * tmin2 <= fl * fl) return kConverged;
   if (st.newton && step < 1e-4f && step > 0.5f * st.prev) return kConverged;
   st.prev = step;
   st.newton = step < (float)kNewtonSwitch;
@@ -117,7 +129,7 @@ __device__ __forceinline__ int iterate64(const Ctx& c, double px, double py, dou
   fast::SDer<double> d = fast::eval_at<double, P, Q, 2>(c.L64, c.m64, c.p, c.q, st.u, st.v, st.hu, st.hv);
   v3<double> r = {d.S.x - px, d.S.y - py, d.S.z - pz};
   double du, dv;
-  if (!solve_step<double, double>(r, d.Su, d.Sv, d.Suu, d.Suv, d.Svv, st.newton, du, dv)) return kFailed;
+  if (!solve_step<double, double, false>(r, d.Su, d.Sv, d.Suu, d.Suv, d.Svv, st.newton, du, dv)) return kFailed;
   if (!(isfinite(du) && isfinite(dv))) return kFailed;
   st.u -= du;
   st.v -= dv;
@@ -145,10 +157,10 @@ __device__ bool final64(const Ctx& c, double px, double py, double pz, double& u
   int hu = 0, hv = 0, hu32 = 0, hv32 = 0;
   for (int it = 0; it < kMaxFinal64; ++it) {
     fast::SDer<double> d = fast::eval_at<double, P, Q, 1>(c.L64, c.m64, c.p, c.q, u, v, hu, hv);
-    fast::SDer<float> e = fast::eval_at<float, P, Q, 2>(c.L32, c.m32, c.p, c.q, (float)u, (float)v, hu32, hv32);
+    fast::SDer<float> e = fast::eval_at<float, P, Q, 2, true>(c.L32, c.m32, c.p, c.q, (float)u, (float)v, hu32, hv32);
     v3<double> r = {d.S.x - px, d.S.y - py, d.S.z - pz};
     double du, dv;
-    if (!solve_step<double, float>(r, d.Su, d.Sv, e.Suu, e.Suv, e.Svv, true, du, dv)) return false;
+    if (!solve_step<double, float, false>(r, d.Su, d.Sv, e.Suu, e.Suv, e.Svv, true, du, dv)) return false;
     if (!(isfinite(du) && isfinite(dv))) return false;
     u -= du;
     v -= dv;
@@ -157,9 +169,16 @@ __device__ bool final64(const Ctx& c, double px, double py, double pz, double& u
   return false;
 }
 
-struct Rec32 {  // per-query FP32 record: best and best distinct runner-up
+struct Rec32 {  // per-query FP32 record: best and best distinct runner-up (squared distances)
   float u1, v1, d1, u2, v2, d2;
 };
+
+// Total order on results (distance, then u, then v): the minimum of a set does not depend on
+// the order in which its members arrive, so per-query records are schedule independent.
+template <typename T>
+__device__ __forceinline__ bool before(T d, T u, T v, T d0, T u0, T v0) {
+  return d < d0 || (d == d0 && (u < u0 || (u == u0 && v < v0)));
+}
 struct Rec64 {  // per-query FP64 record: distinct minima
   double u[kSols], v[kSols], r[kSols];
   int n;
@@ -168,11 +187,11 @@ struct Rec64 {  // per-query FP64 record: distinct minima
 __device__ __forceinline__ void merge32(Rec32& R, float u, float v, float d) {
   bool same1 = R.d1 < INFINITY && fabsf(u - R.u1) <= kDistinct32 && fabsf(v - R.v1) <= kDistinct32;
   if (same1) {
-    if (d < R.d1) { R.u1 = u; R.v1 = v; R.d1 = d; }
-  } else if (d < R.d1) {
+    if (before(d, u, v, R.d1, R.u1, R.v1)) { R.u1 = u; R.v1 = v; R.d1 = d; }
+  } else if (before(d, u, v, R.d1, R.u1, R.v1)) {
     R.u2 = R.u1; R.v2 = R.v1; R.d2 = R.d1;
     R.u1 = u; R.v1 = v; R.d1 = d;
-  } else if (d < R.d2) {
+  } else if (before(d, u, v, R.d2, R.u2, R.v2)) {
     R.u2 = u; R.v2 = v; R.d2 = d;
   }
 }
@@ -180,15 +199,15 @@ __device__ __forceinline__ void merge32(Rec32& R, float u, float v, float d) {
 __device__ __forceinline__ void merge64(Rec64& R, double u, double v, double r) {
   for (int k = 0; k < R.n; ++k)
     if (fabs(R.u[k] - u) <= kDistinct && fabs(R.v[k] - v) <= kDistinct) {
-      if (r < R.r[k]) { R.u[k] = u; R.v[k] = v; R.r[k] = r; }
+      if (before(r, u, v, R.r[k], R.u[k], R.v[k])) { R.u[k] = u; R.v[k] = v; R.r[k] = r; }
       return;
     }
   int slot = R.n;
   if (R.n >= kSols) {
     slot = 0;
     for (int k = 1; k < kSols; ++k)
-      if (R.r[k] > R.r[slot]) slot = k;
-    if (!(r < R.r[slot])) return;
+      if (before(R.r[slot], R.u[slot], R.v[slot], R.r[k], R.u[k], R.v[k])) slot = k;
+    if (!before(r, u, v, R.r[slot], R.u[slot], R.v[slot])) return;
   } else {
     ++R.n;
   }
@@ -200,7 +219,7 @@ __device__ __forceinline__ int finish_status(const double* us, const double* vs,
                                              double& v, double& r) {
   int bi = 0;
   for (int k = 1; k < n; ++k)
-    if (rs[k] < rs[bi]) bi = k;
+    if (before(rs[k], us[k], vs[k], rs[bi], us[bi], vs[bi])) bi = k;
   u = us[bi];
   v = vs[bi];
   r = rs[bi];
@@ -213,7 +232,8 @@ __device__ __forceinline__ int finish_status(const double* us, const double* vs,
 // centres, domain, and breakpoint tables when the surface has at most KS spans per direction.
 template <int KS>
 struct Staged {
-  float box32[kTreeNodes][6];
+  float box32[kTreeNodes][6];   // rounded outward: a point outside is outside the exact box
+  float box32i[kTreeNodes][6];  // rounded inward: a point strictly inside is inside the exact box
   double box64[kTreeNodes][6];
   double ctr[kTreeNodes][2];
   float ctr32[kTreeNodes][2];
@@ -275,6 +295,8 @@ __device__ __forceinline__ void stage_surface(const SurfDev& s, Staged<KS>& sm, 
       sm.box64[k][3 + j] = T.rt[j];
       sm.box32[k][j] = __double2float_rd(T.lb[j]);
       sm.box32[k][3 + j] = __double2float_ru(T.rt[j]);
+      sm.box32i[k][j] = __double2float_ru(T.lb[j]);
+      sm.box32i[k][3 + j] = __double2float_rd(T.rt[j]);
     }
     sm.ctr[k][0] = (T.uv_lb[0] + T.uv_rt[0]) / 2;  // kernel.cu:154
     sm.ctr[k][1] = (T.uv_lb[1] + T.uv_rt[1]) / 2;
@@ -311,15 +333,19 @@ __device__ __forceinline__ void invert_chunk(Staged<KS>& sm, WarpWork<MODE>& ww,
       pz = Pq[3 * q + 2];
     }
     const float fx = (float)px, fy = (float)py, fz = (float)pz;
-    // ---- cull (exact candidate set, ascending node order)
+    // ---- cull (exact candidate set, ascending node order).  With f = fl(x) rounded to nearest,
+    // f < rd(lb) implies x < lb and f > ru(lb) implies x > lb (rounding is monotone), so the
+    // FP64 comparison only runs for coordinates within an FP32 ulp of a box face.
     uint64_t m0 = 0;
     unsigned m1 = 0;
     if (valid) {
       for (int k = 0; k < nbl; ++k) {
         if (fx >= sm.box32[k][0] && fy >= sm.box32[k][1] && fz >= sm.box32[k][2] && fx <= sm.box32[k][3] &&
             fy <= sm.box32[k][4] && fz <= sm.box32[k][5]) {
-          if (px >= sm.box64[k][0] && py >= sm.box64[k][1] && pz >= sm.box64[k][2] && px <= sm.box64[k][3] &&
-              py <= sm.box64[k][4] && pz <= sm.box64[k][5]) {
+          const bool surely = fx > sm.box32i[k][0] && fy > sm.box32i[k][1] && fz > sm.box32i[k][2] &&
+                              fx < sm.box32i[k][3] && fy < sm.box32i[k][4] && fz < sm.box32i[k][5];
+          if (surely || (px >= sm.box64[k][0] && py >= sm.box64[k][1] && pz >= sm.box64[k][2] &&
+                         px <= sm.box64[k][3] && py <= sm.box64[k][4] && pz <= sm.box64[k][5])) {
             if (k < 64) m0 |= 1ull << k;
             else m1 = 1u;
           }
@@ -526,7 +552,8 @@ __device__ __forceinline__ void invert_chunk(Staged<KS>& sm, WarpWork<MODE>& ww,
         double u = R.u1, v = R.v1, r;
         bool ok1 = final64<P, Q>(cx, px, py, pz, u, v, r);
         if (ok1) { us[ns] = u; vs[ns] = v; rs[ns] = r; ++ns; }
-        if (R.d2 < INFINITY && (!ok1 || R.d2 <= R.d1 * 1.001f + 1e-5f)) {
+        const float e1 = sqrtf(R.d1) * 1.001f + 1e-5f;
+        if (R.d2 < INFINITY && (!ok1 || R.d2 <= e1 * e1)) {
           double u2 = R.u2, v2 = R.v2, r2;
           if (final64<P, Q>(cx, px, py, pz, u2, v2, r2)) {
             bool same = ns == 1 && fabs(u2 - us[0]) <= kDistinct && fabs(v2 - vs[0]) <= kDistinct;

@@ -325,30 +325,43 @@ GN_HD v3<T> xyz(const v4<T>& a) {
 // (a - s*b) * f, componentwise, s scalar
 template <typename T>
 GN_HD v3<T> sub_scaled(const v3<T>& a, T s, const v3<T>& b, T f) {
-  return {(a.x - s * b.x) * f, (a.y - s * b.y) * f, (a.z - s * b.z) * f};
+  return {mad(-s, b.x, a.x) * f, mad(-s, b.y, a.y) * f, mad(-s, b.z, a.z) * f};
+}
+
+// 1/x: IEEE in FP64; in FP32 either IEEE or the hardware approximation (about 1 ulp), which the
+// FP32 exploration of the inversion uses since its results are refined in FP64 anyway.
+template <bool FAST>
+__device__ __forceinline__ float rcp(float x) {
+  if constexpr (FAST) return __fdividef(1.0f, x);
+  else return 1.0f / x;
+}
+template <bool FAST>
+__device__ __forceinline__ double rcp(double x) {
+  return 1.0 / x;
 }
 
 // Quotient rule S = R.xyz / h and its derivatives (h = R.w), mapped to global parameters
-// by su = d(local u)/du and sv.
-template <typename T, int ORDER>
-GN_HD SDer<T> quotient(const RDer<T>& d, T su, T sv) {
+// by su = d(local u)/du and sv.  Every product that feeds a sum is an explicit FMA, so the
+// results do not depend on how the compiler contracts the surrounding code.
+template <typename T, int ORDER, bool FAST = false>
+__device__ __forceinline__ SDer<T> quotient(const RDer<T>& d, T su, T sv) {
   SDer<T> o;
-  T ih = T(1) / d.R.w;
+  T ih = rcp<FAST>(d.R.w);
   o.S = {d.R.x * ih, d.R.y * ih, d.R.z * ih};
   if (ORDER >= 1) {
     v3<T> Au = sub_scaled(xyz(d.Ru), d.Ru.w, o.S, ih);  // local dS/du
     v3<T> Av = sub_scaled(xyz(d.Rv), d.Rv.w, o.S, ih);
     if (ORDER >= 2) {
-      T hu = d.Ru.w, hv = d.Rv.w;
-      v3<T> Auu = {(d.Ruu.x - T(2) * hu * Au.x - d.Ruu.w * o.S.x) * ih,
-                   (d.Ruu.y - T(2) * hu * Au.y - d.Ruu.w * o.S.y) * ih,
-                   (d.Ruu.z - T(2) * hu * Au.z - d.Ruu.w * o.S.z) * ih};
-      v3<T> Auv = {(d.Ruv.x - hu * Av.x - hv * Au.x - d.Ruv.w * o.S.x) * ih,
-                   (d.Ruv.y - hu * Av.y - hv * Au.y - d.Ruv.w * o.S.y) * ih,
-                   (d.Ruv.z - hu * Av.z - hv * Au.z - d.Ruv.w * o.S.z) * ih};
-      v3<T> Avv = {(d.Rvv.x - T(2) * hv * Av.x - d.Rvv.w * o.S.x) * ih,
-                   (d.Rvv.y - T(2) * hv * Av.y - d.Rvv.w * o.S.y) * ih,
-                   (d.Rvv.z - T(2) * hv * Av.z - d.Rvv.w * o.S.z) * ih};
+      T hu2 = T(2) * d.Ru.w, hv2 = T(2) * d.Rv.w, hu = d.Ru.w, hv = d.Rv.w;
+      v3<T> Auu = {mad(-d.Ruu.w, o.S.x, mad(-hu2, Au.x, d.Ruu.x)) * ih,
+                   mad(-d.Ruu.w, o.S.y, mad(-hu2, Au.y, d.Ruu.y)) * ih,
+                   mad(-d.Ruu.w, o.S.z, mad(-hu2, Au.z, d.Ruu.z)) * ih};
+      v3<T> Auv = {mad(-d.Ruv.w, o.S.x, mad(-hv, Au.x, mad(-hu, Av.x, d.Ruv.x))) * ih,
+                   mad(-d.Ruv.w, o.S.y, mad(-hv, Au.y, mad(-hu, Av.y, d.Ruv.y))) * ih,
+                   mad(-d.Ruv.w, o.S.z, mad(-hv, Au.z, mad(-hu, Av.z, d.Ruv.z))) * ih};
+      v3<T> Avv = {mad(-d.Rvv.w, o.S.x, mad(-hv2, Av.x, d.Rvv.x)) * ih,
+                   mad(-d.Rvv.w, o.S.y, mad(-hv2, Av.y, d.Rvv.y)) * ih,
+                   mad(-d.Rvv.w, o.S.z, mad(-hv2, Av.z, d.Rvv.z)) * ih};
       T suu = su * su, suv = su * sv, svv = sv * sv;
       o.Suu = {Auu.x * suu, Auu.y * suu, Auu.z * suu};
       o.Suv = {Auv.x * suv, Auv.y * suv, Auv.z * suv};
@@ -452,7 +465,7 @@ __device__ __forceinline__ int find_seg_hint(const T* b, int ns, T x, int hint) 
 }
 
 // eval_point with explicit breakpoint tables and span hints (updated in place).
-template <typename T, int P, int Q, int ORDER>
+template <typename T, int P, int Q, int ORDER, bool FAST = false>
 __device__ __forceinline__ SDer<T> eval_at(const Locator<T>& L, const T* __restrict__ m, int p, int q, T u, T v,
                                            int& hu, int& hv) {
   hu = find_seg_hint(L.bu, L.ns_u, u, hu);
@@ -463,7 +476,7 @@ __device__ __forceinline__ SDer<T> eval_at(const Locator<T>& L, const T* __restr
   const int k12 = (p + 1) * (q + 1);
   const T* span = m + (size_t)(hu * L.ns_v + hv) * k12 * 4;
   RDer<T> d = span_contract<T, P, Q, ORDER>(span, p, q, lu, lv);
-  return quotient<T, ORDER>(d, L.ru * idu, L.rv * idv);
+  return quotient<T, ORDER, FAST>(d, L.ru * idu, L.rv * idv);
 }
 
 }  // namespace fast

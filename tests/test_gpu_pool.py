@@ -63,19 +63,46 @@ def test_pool_inversion_matches_single_surface(nurbs, pool_setup, precision, til
     pool.set_config(tile, 4)
     uv, st, res = (x.cpu().numpy() for x in pool.invert(batch, T(P), precision))
     per = batch.offsets[1] - batch.offsets[0]
-    differ = 0
     for k, sf in enumerate(surfs):
         s = nurbs.Surface(sf)
         sl = slice(k * per, (k + 1) * per)
         u1, s1, r1 = (x.cpu().numpy() for x in s.invert(T(P[sl]), precision))
-        # Same algorithm and code.  FP64 results are identical; the separately compiled pooled
-        # kernel may fuse FP32 operations differently, and a seed's FP32 trajectory from far
-        # away can then end in another minimum, so a rare mixed-precision query may differ.
-        same = (s1 == st[sl]) & ((np.abs(u1 - uv[sl]).max(1) <= 1e-12) | (np.isnan(u1).all(1) & np.isnan(uv[sl]).all(1)))
-        if precision == 0:
-            assert same.all(), k
-        differ += int((~same).sum())
-    assert differ <= 0.002 * len(P), differ
+        # Same seeds, same arithmetic (explicit FMAs, no compiler contraction) and per-query
+        # records whose minimum does not depend on the order seeds finish: identical results.
+        assert np.array_equal(s1, st[sl]), k
+        assert np.array_equal(u1, uv[sl], equal_nan=True), k
+        assert np.array_equal(r1, res[sl], equal_nan=True), k
+
+
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "mixed"])
+def test_result_does_not_depend_on_batch(nurbs, pool_setup, precision):
+    """A query's result is the same alone, in its own batch, and shuffled into any batch."""
+    surfs, pool, ids, batch, P, _ = pool_setup
+    pool.set_config(128, 4)
+    uv, st, res = (x.cpu().numpy() for x in pool.invert(batch, T(P), precision))
+    per = batch.offsets[1] - batch.offsets[0]
+    rng = np.random.default_rng(17)
+    # regroup: every surface's queries split into two parts, the surfaces in random order
+    order = rng.permutation(len(surfs))
+    ids2, offs, idx = [], [0], []
+    for k in order:
+        cut = int(rng.integers(1, per))
+        for a, b in ((0, cut), (cut, per)):
+            ids2.append(int(ids[k]))
+            idx.append(np.arange(k * per + a, k * per + b))
+            offs.append(offs[-1] + b - a)
+    idx = np.concatenate(idx)
+    for tile in (128, 16):
+        pool.set_config(tile, 4)
+        u2, s2, r2 = (x.cpu().numpy() for x in pool.invert(nurbs.Batch(ids2, offs), T(P[idx]), precision))
+        assert np.array_equal(s2, st[idx])
+        assert np.array_equal(u2, uv[idx], equal_nan=True)
+        assert np.array_equal(r2, res[idx], equal_nan=True)
+    # one query alone
+    for q in rng.choice(len(P), 8, replace=False):
+        k = q // per
+        u3, s3, r3 = (x.cpu().numpy() for x in pool.invert(nurbs.Batch([int(ids[k])], [0, 1]), T(P[q:q + 1]), precision))
+        assert s3[0] == st[q] and np.array_equal(u3[0], uv[q], equal_nan=True)
 
 
 def test_pool_inversion_parity_with_oracle(nurbs, pool_setup):
