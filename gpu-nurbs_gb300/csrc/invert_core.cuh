@@ -17,8 +17,6 @@ constexpr int kModeMixed = 1;
 constexpr int kWarps = 4;          // warps per CTA
 constexpr int kThreads = 32 * kWarps;
 constexpr int kMinBlocksMixed = 4;  // CTAs per SM the mixed kernel is register-budgeted for
-  // CTAs per SM the mixed kernel is register-budgeted for
-  // CTAs per SM the mixed kernel is register-budgeted for
 constexpr int kMaxIter32 = 24;     // FP32 iterations per seed
 constexpr int kMaxIter64 = 40;     // FP64-mode iterations per seed
 constexpr int kMaxFinal64 = 6;     // MIXED: FP64 steps (2 normally)
@@ -26,8 +24,8 @@ constexpr double kNewtonSwitch = 1e-2;  // GN while the step is larger, Newton b
 constexpr float kTol32 = 3e-7f;
 constexpr double kTolNewton64 = 1e-10;  // a Newton step this small leaves < 1e-19 error
 constexpr double kTolAny64 = 1e-14;
-constexpr double kDistinct = 1e-7;      // two FP64 solutions are the same minimum within this
-constexpr float kDistinct32 = 1e-4f;    // ... two FP32 solutions
+constexpr double kDistinct = 1e-7;      // FP64 minima: grid cell size, times the domain's extent
+constexpr float kDistinct32 = 1e-4f;    // FP32 minima: the same
 constexpr float kJoin = 1e-3f;          // a Newton iterate this close to a known minimum joins it
 // Stopping a seed once it nears a minimum its query already found saves ~15-20 % of the
 // iterations, but whether the other seed has finished first depends on the other queries that
@@ -171,6 +169,7 @@ __device__ bool final64(const Ctx& c, double px, double py, double pz, double& u
 
 struct Rec32 {  // per-query FP32 record: best and best distinct runner-up (squared distances)
   float u1, v1, d1, u2, v2, d2;
+  int cu1, cv1;  // grid cell of the best
 };
 
 // Total order on results (distance, then u, then v): the minimum of a set does not depend on
@@ -179,26 +178,49 @@ template <typename T>
 __device__ __forceinline__ bool before(T d, T u, T v, T d0, T u0, T v0) {
   return d < d0 || (d == d0 && (u < u0 || (u == u0 && v < v0)));
 }
-struct Rec64 {  // per-query FP64 record: distinct minima
+struct Rec64 {  // per-query FP64 record: distinct minima and their grid cells
   double u[kSols], v[kSols], r[kSols];
+  int cu[kSols], cv[kSols];
   int n;
 };
 
-__device__ __forceinline__ void merge32(Rec32& R, float u, float v, float d) {
-  bool same1 = R.d1 < INFINITY && fabsf(u - R.u1) <= kDistinct32 && fabsf(v - R.v1) <= kDistinct32;
-  if (same1) {
+// Results are grouped into minima by a fixed grid over the parameter domain (cells of
+// kDistinct32 / kDistinct times the domain's extent): a grouping that depends on each result
+// alone, unlike "within a distance of the current representative", so the records below hold
+// the same values whatever order the seeds finish in.
+template <typename T>
+struct Cells {
+  T u0, v0, iu, iv;  // domain origin, cells per parameter unit
+};
+// cell indices of an in-domain result (rounded down; saturating)
+__device__ __forceinline__ int cell_index(float x) { return __float2int_rd(x); }
+__device__ __forceinline__ int cell_index(double x) { return __double2int_rd(x); }
+template <typename T>
+__device__ __forceinline__ void cell_of(const Cells<T>& g, T u, T v, int& cu, int& cv) {
+  cu = cell_index((u - g.u0) * g.iu);
+  cv = cell_index((v - g.v0) * g.iv);
+}
+
+// R.1 = the minimum of all results (total order); R.2 = the minimum of the results outside
+// R.1's cell.  Exact for any arrival order: a new overall minimum in another cell makes the
+// old minimum (smaller than everything else seen) the runner-up.
+__device__ __forceinline__ void merge32(Rec32& R, int cu, int cv, float u, float v, float d) {
+  if (R.d1 < INFINITY && cu == R.cu1 && cv == R.cv1) {
     if (before(d, u, v, R.d1, R.u1, R.v1)) { R.u1 = u; R.v1 = v; R.d1 = d; }
   } else if (before(d, u, v, R.d1, R.u1, R.v1)) {
     R.u2 = R.u1; R.v2 = R.v1; R.d2 = R.d1;
-    R.u1 = u; R.v1 = v; R.d1 = d;
+    R.u1 = u; R.v1 = v; R.d1 = d; R.cu1 = cu; R.cv1 = cv;
   } else if (before(d, u, v, R.d2, R.u2, R.v2)) {
     R.u2 = u; R.v2 = v; R.d2 = d;
   }
 }
 
-__device__ __forceinline__ void merge64(Rec64& R, double u, double v, double r) {
+// The kSols cells with the smallest minima, each with its minimum.  A cell evicted earlier can
+// only come back with a smaller value than the one it was evicted with, so the kept values are
+// exact cell minima whatever the arrival order.
+__device__ __forceinline__ void merge64(Rec64& R, int cu, int cv, double u, double v, double r) {
   for (int k = 0; k < R.n; ++k)
-    if (fabs(R.u[k] - u) <= kDistinct && fabs(R.v[k] - v) <= kDistinct) {
+    if (cu == R.cu[k] && cv == R.cv[k]) {
       if (before(r, u, v, R.r[k], R.u[k], R.v[k])) { R.u[k] = u; R.v[k] = v; R.r[k] = r; }
       return;
     }
@@ -211,7 +233,7 @@ __device__ __forceinline__ void merge64(Rec64& R, double u, double v, double r) 
   } else {
     ++R.n;
   }
-  R.u[slot] = u; R.v[slot] = v; R.r[slot] = r;
+  R.u[slot] = u; R.v[slot] = v; R.r[slot] = r; R.cu[slot] = cu; R.cv[slot] = cv;
 }
 
 // best minimum and status (FOUND / AMBIGUOUS), as the oracle decides them
@@ -238,6 +260,8 @@ struct Staged {
   double ctr[kTreeNodes][2];
   float ctr32[kTreeNodes][2];
   float dom32[4];
+  Cells<float> cell32;
+  Cells<double> cell64;
   int nb;
   float sb32[2][KS + 1], si32[2][KS];
   double sb64[2][KS + 1], si64[2][KS];
@@ -310,6 +334,10 @@ __device__ __forceinline__ void stage_surface(const SurfDev& s, Staged<KS>& sm, 
     sm.dom32[1] = (float)s.dom_u1 + slack;
     sm.dom32[2] = (float)s.dom_v0 - slack;
     sm.dom32[3] = (float)s.dom_v1 + slack;
+    const double eu = s.dom_u1 - s.dom_u0, ev = s.dom_v1 - s.dom_v0;
+    sm.cell32 = {(float)s.dom_u0, (float)s.dom_v0, (float)(1.0 / ((double)kDistinct32 * eu)),
+                 (float)(1.0 / ((double)kDistinct32 * ev))};
+    sm.cell64 = {s.dom_u0, s.dom_v0, 1.0 / (kDistinct * eu), 1.0 / (kDistinct * ev)};
   }
 }
 
@@ -389,6 +417,7 @@ __device__ __forceinline__ void invert_chunk(Staged<KS>& sm, WarpWork<MODE>& ww,
       R.d1 = INFINITY;
       R.d2 = INFINITY;
       R.u1 = R.v1 = R.u2 = R.v2 = 0.f;
+      R.cu1 = R.cv1 = 0;
     } else {
       ww.rec[lane].n = 0;
     }
@@ -474,10 +503,12 @@ __device__ __forceinline__ void invert_chunk(Staged<KS>& sm, WarpWork<MODE>& ww,
         const bool keep = res == kConverged && sd.u >= sm.dom32[0] && sd.u <= sm.dom32[1] && sd.v >= sm.dom32[2] &&
                           sd.v <= sm.dom32[3];
         __syncwarp();
+        int cu = 0, cv = 0;
+        if (done && keep) cell_of(sm.cell32, sd.u, sd.v, cu, cv);
         unsigned fm = __ballot_sync(FULL, done && keep);
         while (fm) {
           int j = __ffs(fm) - 1;
-          if (lane == j) merge32(ww.rec[ql], sd.u, sd.v, dist);
+          if (lane == j) merge32(ww.rec[ql], cu, cv, sd.u, sd.v, dist);
           __syncwarp();
           fm &= fm - 1;
         }
@@ -521,10 +552,12 @@ __device__ __forceinline__ void invert_chunk(Staged<KS>& sm, WarpWork<MODE>& ww,
         }
         const bool done = active && res != kContinue;
         __syncwarp();
+        int cu = 0, cv = 0;
+        if (done && keep) cell_of(sm.cell64, sd.u, sd.v, cu, cv);
         unsigned fm = __ballot_sync(FULL, done && keep);
         while (fm) {
           int j = __ffs(fm) - 1;
-          if (lane == j) merge64(ww.rec[ql], sd.u, sd.v, rr);
+          if (lane == j) merge64(ww.rec[ql], cu, cv, sd.u, sd.v, rr);
           __syncwarp();
           fm &= fm - 1;
         }
@@ -545,15 +578,19 @@ __device__ __forceinline__ void invert_chunk(Staged<KS>& sm, WarpWork<MODE>& ww,
     if (cnt == 0) {
       status = 2;  // NURBS_INV_NO_CANDIDATE
     } else if constexpr (MODE == kModeMixed) {
-      const Rec32 R = ww.rec[lane];
       double us[2], vs[2], rs[2];
       int ns = 0;
+      const Rec32& R = ww.rec[lane];
       if (R.d1 < INFINITY) {
-        double u = R.u1, v = R.v1, r;
-        bool ok1 = final64<P, Q>(cx, px, py, pz, u, v, r);
-        if (ok1) { us[ns] = u; vs[ns] = v; rs[ns] = r; ++ns; }
+        // the runner-up also takes the FP64 steps when the best fails there, or when it is within
+        // 0.1 % of the best; one next to the best is the same minimum split by a cell boundary
         const float e1 = sqrtf(R.d1) * 1.001f + 1e-5f;
-        if (R.d2 < INFINITY && (!ok1 || R.d2 <= e1 * e1)) {
+        const bool second = R.d2 < INFINITY && !(fabsf(R.u2 - R.u1) <= kDistinct32 && fabsf(R.v2 - R.v1) <= kDistinct32);
+        const bool tie = second && R.d2 <= e1 * e1;
+        double u = R.u1, v = R.v1, r;
+        const bool ok1 = final64<P, Q>(cx, px, py, pz, u, v, r);
+        if (ok1) { us[ns] = u; vs[ns] = v; rs[ns] = r; ++ns; }
+        if (ok1 ? tie : second) {
           double u2 = R.u2, v2 = R.v2, r2;
           if (final64<P, Q>(cx, px, py, pz, u2, v2, r2)) {
             bool same = ns == 1 && fabs(u2 - us[0]) <= kDistinct && fabs(v2 - vs[0]) <= kDistinct;
