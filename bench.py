@@ -94,6 +94,29 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+# DRAM bytes (read + write) per launch of the dominant kernel, from one ncu capture each
+# (profiles/k_invert_large.md, profiles/k_eval_large.md), per unit of work so that they scale
+# to the launch size: traffic grows with the number of queries or points.
+TRAFFIC_PER_UNIT = {
+    "large": (29.04e6 + 0.45e6) / (1 << 20),   # mixed k_invert, bytes per query (2^20-query capture)
+    "eval-large": 346.3e9 * 1.7665e-3 / (1 << 22),  # FP64 k_eval S..Svv, bytes per point (2^22 points)
+}
+
+
+def mean_step_ms_over_ranks(ts, world, device):
+    """Per-step time of the slowest rank: each rank's total over its timed steps, the maximum
+    taken over ranks (an all-reduce of one number; nothing else crosses ranks), divided by the
+    step count."""
+    tot = sum(ts)
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([tot], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        tot = float(t.item())
+    return tot / len(ts)
+
+
 def make_workload(gn, torch, name, n, seed):
     from gpu_nurbs_gb300 import synth
     if name == "large":
@@ -210,13 +233,7 @@ def run_ours(a):
         t_e2e.append((time.perf_counter() - t0) * 1e3)
     barrier()
 
-    def agg(ts):
-        tot = sum(ts)
-        if world > 1:
-            t = torch.tensor([tot], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            tot = float(t.item())
-        return tot / len(ts)
+    agg = lambda ts: mean_step_ms_over_ranks(ts, world, "cuda")
 
     ms_mixed, ms_fp64, ms_e2e = agg(t_mixed), agg(t_fp64), agg(t_e2e)
     if rank != 0:
@@ -257,7 +274,9 @@ def run_ours(a):
         "e2e": {"value": n * world / (ms_e2e / 1e3), "unit": "inversions/s", "h2d_bytes_per_step": n * 24,
                 "d2h_bytes_per_step": n * (16 + 4 + 8), "ms_per_step": ms_e2e},
         "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak64, "unit": "TFLOP/s",
-                     "frac": (achieved / peak64) if peak64 else None, "traffic": None,
+                     "frac": (achieved / peak64) if peak64 else None,
+                     "traffic": TRAFFIC_PER_UNIT[a.workload] * n if a.workload in TRAFFIC_PER_UNIT else None,
+                     "traffic_unit": "bytes per launch",
                      "peak_source": "FP64 FMA probe kernel run in this process",
                      "fp32_peak": peak32, "flop_per_query_nominal": flop_q},
         "clocks": clk,
@@ -579,7 +598,9 @@ def run_eval(a):
                    "l2": "flushed (512 MB write) before each step"},
         "fp32_value": n / (ms32 / 1e3), "fp32_ms_per_step": ms32,
         "roofline": {"bound": "fp64", "achieved": ach64, "peak": peak64, "unit": "TFLOP/s",
-                     "frac": ach64 / peak64 if peak64 else None, "traffic": None,
+                     "frac": ach64 / peak64 if peak64 else None,
+                     "traffic": TRAFFIC_PER_UNIT[a.workload] * n if a.workload in TRAFFIC_PER_UNIT else None,
+                     "traffic_unit": "bytes per launch",
                      "flop_per_point": flop, "bytes_per_point_fp64": bytes64,
                      "hbm_achieved_gbs": bytes64 * n / (ms64 / 1e3) / 1e9,
                      "fp32_hbm_achieved_gbs": (8 + 12 * nout) * n / (ms32 / 1e3) / 1e9,
