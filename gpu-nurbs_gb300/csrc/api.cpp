@@ -75,6 +75,11 @@ int fetch(const double* src, size_t n, int kind, std::vector<double>& dst, cudaS
 
 }  // namespace
 
+// Inversion launches take their chunk counter from a ring of device words.  A slot is reused
+// only after the launch that used it before has finished on the GPU (an event per slot), so
+// calls on several streams at once never share a counter.
+constexpr int kCounterRing = 16;
+
 struct nurbs_surface_s {
   SurfDev dev{};
   void* arena = nullptr;
@@ -83,7 +88,43 @@ struct nurbs_surface_s {
   double* basis_v = nullptr;
   int device = 0;
   bool tree_built = false;
+  unsigned* counters = nullptr;  // kCounterRing device words
+  cudaEvent_t done[kCounterRing] = {};
+  unsigned next_slot = 0;
+  std::mutex mu;
 };
+
+// Enqueues one inversion on `st`: waits for the previous user of the counter slot, zeroes the
+// counter, launches, marks the slot.  Inside a stream capture the slot is used without the
+// event handshake (capture cannot wait on work recorded outside it).
+static cudaError_t invert_on(nurbs_surface_s* s, const double* P, int64_t n, double* uv, int* status, double* res,
+                             int precision, cudaStream_t st) {
+  std::lock_guard<std::mutex> lk(s->mu);
+  const int slot = (int)(s->next_slot++ % kCounterRing);
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  cudaError_t e = cudaStreamIsCapturing(st, &cap);
+  if (e != cudaSuccess) return e;
+  const bool capturing = cap != cudaStreamCaptureStatusNone;
+  if (!capturing) {
+    if (!s->done[slot]) {
+      e = cudaEventCreateWithFlags(&s->done[slot], cudaEventDisableTiming);
+      if (e != cudaSuccess) return e;
+    } else {
+      e = cudaStreamWaitEvent(st, s->done[slot], 0);
+      if (e != cudaSuccess) return e;
+    }
+  }
+  e = cudaMemsetAsync(s->counters + slot, 0, sizeof(unsigned), st);
+  if (e == cudaSuccess) e = launch_invert(s->dev, P, n, uv, status, res, precision, s->counters + slot, st);
+  if (e == cudaSuccess && !capturing) e = cudaEventRecord(s->done[slot], st);
+  return e;
+}
+
+static void release_surface(nurbs_surface_s* s) {
+  for (cudaEvent_t& ev : s->done)
+    if (ev) cudaEventDestroy(ev);
+  if (s->counters) cudaFree(s->counters);
+}
 
 extern "C" {
 
@@ -165,12 +206,20 @@ int nurbs_surface_create(int p, int q, int nu, int nv, const double* knots_u, co
     return cuda_fail(e, "matrix-form conversion");
   }
   s->tree_built = true;
+  e = cudaMalloc((void**)&s->counters, sizeof(unsigned) * kCounterRing);
+  if (e != cudaSuccess) {
+    cudaFree(s->arena);
+    delete s;
+    cudaGetLastError();
+    return fail(NURBS_E_NOMEM, "device allocation of the launch counters failed: %s", cudaGetErrorString(e));
+  }
   *out = s;
   return NURBS_OK;
 }
 
 int nurbs_surface_destroy(nurbs_surface_t s) {
   if (!s) return NURBS_OK;
+  release_surface(s);
   cudaError_t e = cudaFree(s->arena);
   delete s;
   if (e != cudaSuccess) return cuda_fail(e, "cudaFree");
@@ -309,7 +358,7 @@ int nurbs_invert(nurbs_surface_t s, const double* P_dev, int64_t n, double* uv_d
     return fail(NURBS_E_INVALID, "precision %d is not FP64 or MIXED", precision);
   if (n == 0) return NURBS_OK;
   if (!P_dev || !uv_dev || !status_dev || !residual_dev) return fail(NURBS_E_INVALID, "NULL buffer");
-  CUDA_TRY(launch_invert(s->dev, P_dev, n, uv_dev, status_dev, residual_dev, precision, (cudaStream_t)stream),
+  CUDA_TRY(invert_on(s, P_dev, n, uv_dev, status_dev, residual_dev, precision, (cudaStream_t)stream),
            "invert launch");
   return NURBS_OK;
 }
@@ -319,6 +368,8 @@ int nurbs_invert_host(nurbs_surface_t s, const double* P_host, int64_t n, double
   if (!s) return fail(NURBS_E_INVALID, "NULL surface");
   if (n < 0) return fail(NURBS_E_INVALID, "negative count");
   if (n == 0) return NURBS_OK;
+  if (precision != NURBS_PREC_FP64 && precision != NURBS_PREC_MIXED)
+    return fail(NURBS_E_INVALID, "precision %d is not FP64 or MIXED", precision);
   if (!P_host || !uv_host || !status_host || !residual_host) return fail(NURBS_E_INVALID, "NULL buffer");
   cudaStream_t st = (cudaStream_t)stream;
   size_t bP = (size_t)n * 24, bUV = (size_t)n * 16, bS = (size_t)n * 4, bR = (size_t)n * 8;
@@ -327,8 +378,8 @@ int nurbs_invert_host(nurbs_surface_t s, const double* P_host, int64_t n, double
   CUDA_TRY(cudaMallocAsync((void**)&buf, total, st), "device buffers");
   cudaError_t e = cudaMemcpyAsync(buf, P_host, bP, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess)
-    e = launch_invert(s->dev, (const double*)buf, n, (double*)(buf + oUV), (int*)(buf + oS), (double*)(buf + oR),
-                      precision, st);
+    e = invert_on(s, (const double*)buf, n, (double*)(buf + oUV), (int*)(buf + oS), (double*)(buf + oR),
+                  precision, st);
   if (e == cudaSuccess) e = cudaMemcpyAsync(uv_host, buf + oUV, bUV, cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaMemcpyAsync(status_host, buf + oS, bS, cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaMemcpyAsync(residual_host, buf + oR, bR, cudaMemcpyDeviceToHost, st);

@@ -10,9 +10,11 @@
 //      fixed point is the same stationary point but which converge quadratically;
 //   3. results inside the knot domain are kept; the closest wins.
 //
-// Work distribution.  A query has anywhere from 0 to 65 candidate seeds and a seed needs from
-// 2 to 24 iterations, so one thread per query leaves most lanes of a warp idle.  Each warp
-// owns 32 queries, flattens their (query, seed) pairs into a task list (warp prefix sum over
+// Work distribution.  The grid is persistent (as many CTAs as fit on the GPU at once) and each
+// warp takes chunks of 32 consecutive queries from a global counter until none are left, so
+// warps that drew expensive queries do not hold up the end of the launch.  A query has anywhere
+// from 0 to 65 candidate seeds and a seed needs from 2 to 24 iterations, so one thread per query
+// leaves most lanes of a warp idle.  Each warp owns 32 queries, flattens their (query, seed) pairs into a task list (warp prefix sum over
 // the candidate counts) and every lane pulls the next task as soon as its seed converges or
 // fails, so all 32 lanes iterate until the warp's list is exhausted.  Finished seeds are merged
 // into per-query records in shared memory, one lane at a time.  Every seed runs to its own end
@@ -38,7 +40,7 @@ using namespace inv;
 template <int P, int Q, int MODE>
 __global__ void __launch_bounds__(kThreads, MODE == kModeMixed ? kMinBlocksMixed : 4)
     k_invert(SurfDev s, const double* __restrict__ Pq, int64_t n, double* __restrict__ uv_out,
-             int* __restrict__ st_out, double* __restrict__ res_out) {
+             int* __restrict__ st_out, double* __restrict__ res_out, unsigned* __restrict__ counter) {
   __shared__ Staged<kSmemSpans> sm;           // one surface for the whole CTA
   __shared__ WarpWork<MODE> ww[kWarps];
   Ctx cx;
@@ -46,33 +48,59 @@ __global__ void __launch_bounds__(kThreads, MODE == kModeMixed ? kMinBlocksMixed
   __syncthreads();
   const int warp = threadIdx.x >> 5;
   const int64_t chunks = (n + 31) / 32;
-  for (int64_t ch = (int64_t)blockIdx.x * kWarps + warp; ch < chunks; ch += (int64_t)gridDim.x * kWarps)
-    invert_chunk<P, Q, MODE, kSmemSpans>(sm, ww[warp], cx, Pq, ch * 32, n, uv_out, st_out, res_out);
+  for (;;) {
+    unsigned ch = 0;
+    if ((threadIdx.x & 31) == 0) ch = atomicAdd(counter, 1u);
+    ch = __shfl_sync(0xffffffffu, ch, 0);
+    if ((int64_t)ch >= chunks) break;
+    invert_chunk<P, Q, MODE, kSmemSpans>(sm, ww[warp], cx, Pq, (int64_t)ch * 32, n, uv_out, st_out, res_out);
+  }
+}
+
+// CTAs of a kernel that fit on the current GPU at once (queried once per kernel and device).
+template <class K>
+int64_t resident_ctas(K kernel) {
+  static int cached[64] = {0};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) dev = 0;
+  if (!cached[dev]) {
+    int sms = 0, per_sm = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kThreads, 0);
+    cached[dev] = (sms > 0 ? sms : 1) * (per_sm > 0 ? per_sm : 1);
+  }
+  return cached[dev];
+}
+
+template <int P, int Q, int MODE>
+cudaError_t launch_mode(const SurfDev& s, const double* P_, int64_t n, double* uv, int* st_, double* res,
+                        unsigned* counter, cudaStream_t st) {
+  const int64_t chunks = (n + 31) / 32;
+  if (chunks > 0x7fffffffLL) return cudaErrorInvalidValue;  // chunk ids are 32-bit
+  int64_t blocks = (chunks + kWarps - 1) / kWarps;
+  const int64_t cap = resident_ctas(k_invert<P, Q, MODE>);
+  if (blocks > cap) blocks = cap;
+  k_invert<P, Q, MODE><<<(unsigned)blocks, kThreads, 0, st>>>(s, P_, n, uv, st_, res, counter);
+  return cudaGetLastError();
 }
 
 template <int P, int Q>
 cudaError_t launch_pq(const SurfDev& s, const double* P_, int64_t n, double* uv, int* st_, double* res, int prec,
-                      cudaStream_t st) {
-  int64_t chunks = (n + 31) / 32;
-  int64_t blocks = (chunks + kWarps - 1) / kWarps;
-  const int64_t cap = 152 * 16;
-  if (blocks > cap) blocks = cap;
-  if (prec == 1)
-    k_invert<P, Q, kModeMixed><<<(unsigned)blocks, kThreads, 0, st>>>(s, P_, n, uv, st_, res);
-  else
-    k_invert<P, Q, kModeFP64><<<(unsigned)blocks, kThreads, 0, st>>>(s, P_, n, uv, st_, res);
-  return cudaGetLastError();
+                      unsigned* counter, cudaStream_t st) {
+  if (prec == 1) return launch_mode<P, Q, kModeMixed>(s, P_, n, uv, st_, res, counter, st);
+  return launch_mode<P, Q, kModeFP64>(s, P_, n, uv, st_, res, counter, st);
 }
 
 }  // namespace
 
 cudaError_t launch_invert(const SurfDev& s, const double* P, int64_t n, double* uv, int* status, double* residual,
-                          int precision, cudaStream_t st) {
+                          int precision, unsigned* counter, cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
-  if (s.p == 3 && s.q == 3) return launch_pq<3, 3>(s, P, n, uv, status, residual, precision, st);
-  if (s.p == 5 && s.q == 5) return launch_pq<5, 5>(s, P, n, uv, status, residual, precision, st);
-  if (s.p == 2 && s.q == 2) return launch_pq<2, 2>(s, P, n, uv, status, residual, precision, st);
-  return launch_pq<0, 0>(s, P, n, uv, status, residual, precision, st);
+  if (s.p == 3 && s.q == 3) return launch_pq<3, 3>(s, P, n, uv, status, residual, precision, counter, st);
+  if (s.p == 5 && s.q == 5) return launch_pq<5, 5>(s, P, n, uv, status, residual, precision, counter, st);
+  if (s.p == 2 && s.q == 2) return launch_pq<2, 2>(s, P, n, uv, status, residual, precision, counter, st);
+  return launch_pq<0, 0>(s, P, n, uv, status, residual, precision, counter, st);
 }
 
 }  // namespace gnurbs

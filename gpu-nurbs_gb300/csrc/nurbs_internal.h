@@ -102,8 +102,8 @@ cudaError_t launch_invert_pool(const SurfDev* table, const InvTile* tiles, int n
                                const double* P, double* uv, int* status, double* residual, int precision,
                                int ctas, int tile_queries, cudaStream_t st);
 
-// stage d
+// stage d.  counter: one device word, zero when the launch starts (the kernel's chunk counter).
 cudaError_t launch_invert(const SurfDev& s, const double* P, int64_t n, double* uv, int* status,
-                          double* residual, int precision, cudaStream_t st);
+                          double* residual, int precision, unsigned* counter, cudaStream_t st);
 
 }  // namespace gnurbs
