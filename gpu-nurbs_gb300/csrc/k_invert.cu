@@ -11,8 +11,10 @@
 //   3. results inside the knot domain are kept; the closest wins.
 //
 // Work distribution.  The grid is persistent (as many CTAs as fit on the GPU at once) and each
-// warp takes chunks of 32 consecutive queries from a global counter until none are left, so
-// warps that drew expensive queries do not hold up the end of the launch.  A query has anywhere
+// warp takes chunks of consecutive queries from a global counter until none are left, so
+// warps that drew expensive queries do not hold up the end of the launch.  Chunks hold 32
+// queries; on large launches the last two rounds hold 8, which shortens the tail in which the
+// last warps finish while the others idle.  A query has anywhere
 // from 0 to 65 candidate seeds and a seed needs from 2 to 24 iterations, so one thread per query
 // leaves most lanes of a warp idle.  Each warp owns 32 queries, flattens their (query, seed) pairs into a task list (warp prefix sum over
 // the candidate counts) and every lane pulls the next task as soon as its seed converges or
@@ -40,20 +42,24 @@ using namespace inv;
 template <int P, int Q, int MODE>
 __global__ void __launch_bounds__(kThreads, MODE == kModeMixed ? kMinBlocksMixed : 4)
     k_invert(SurfDev s, const double* __restrict__ Pq, int64_t n, double* __restrict__ uv_out,
-             int* __restrict__ st_out, double* __restrict__ res_out, unsigned* __restrict__ counter) {
+             int* __restrict__ st_out, double* __restrict__ res_out, unsigned* __restrict__ counter,
+             int64_t n_big) {
   __shared__ Staged<kSmemSpans> sm;           // one surface for the whole CTA
   __shared__ WarpWork<MODE> ww[kWarps];
   Ctx cx;
   stage_surface<kSmemSpans>(s, sm, cx, threadIdx.x, blockDim.x);
   __syncthreads();
   const int warp = threadIdx.x >> 5;
-  const int64_t chunks = (n + 31) / 32;
+  // queries [0, n_big) in chunks of 32, then [n_big, n) in chunks of 8
+  const int64_t big = n_big / 32, units = big + (n - n_big + 7) / 8;
   for (;;) {
     unsigned ch = 0;
     if ((threadIdx.x & 31) == 0) ch = atomicAdd(counter, 1u);
     ch = __shfl_sync(0xffffffffu, ch, 0);
-    if ((int64_t)ch >= chunks) break;
-    invert_chunk<P, Q, MODE, kSmemSpans>(sm, ww[warp], cx, Pq, (int64_t)ch * 32, n, uv_out, st_out, res_out);
+    if ((int64_t)ch >= units) break;
+    const int64_t q0 = (int64_t)ch < big ? (int64_t)ch * 32 : n_big + ((int64_t)ch - big) * 8;
+    const int64_t q1 = (int64_t)ch < big ? q0 + 32 : min(q0 + 8, n);
+    invert_chunk<P, Q, MODE, kSmemSpans>(sm, ww[warp], cx, Pq, q0, q1, uv_out, st_out, res_out);
   }
 }
 
@@ -77,11 +83,14 @@ template <int P, int Q, int MODE>
 cudaError_t launch_mode(const SurfDev& s, const double* P_, int64_t n, double* uv, int* st_, double* res,
                         unsigned* counter, cudaStream_t st) {
   const int64_t chunks = (n + 31) / 32;
-  if (chunks > 0x7fffffffLL) return cudaErrorInvalidValue;  // chunk ids are 32-bit
+  if (chunks > 0x3fffffffLL) return cudaErrorInvalidValue;  // chunk ids are 32-bit
   int64_t blocks = (chunks + kWarps - 1) / kWarps;
   const int64_t cap = resident_ctas(k_invert<P, Q, MODE>);
   if (blocks > cap) blocks = cap;
-  k_invert<P, Q, MODE><<<(unsigned)blocks, kThreads, 0, st>>>(s, P_, n, uv, st_, res, counter);
+  // small chunks for the last two rounds of warps, when there are at least four rounds
+  const int64_t warps = cap * kWarps, tail = 2 * warps * 8;
+  const int64_t n_big = ((n >= 4 * warps * 32 ? n - tail : n) / 32) * 32;  // a multiple of 32
+  k_invert<P, Q, MODE><<<(unsigned)blocks, kThreads, 0, st>>>(s, P_, n, uv, st_, res, counter, n_big);
   return cudaGetLastError();
 }
 
