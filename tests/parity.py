@@ -32,12 +32,15 @@ def eval_errors(ev, ref):
     return out
 
 
-def classify_inversion(uv, st, res, ouv, ost, ores, P):
+def classify_inversion(uv, st, res, ouv, ost, ores, P, res_abs=1e-14):
+    """res_abs: absolute residual slack per unit of max(1, |P|_inf); 1e-14 unless the surface's
+    FP64 evaluation itself is less accurate than that (high degrees), in which case the caller
+    passes the measured relative difference of S between the two evaluations."""
     uv = np.asarray(uv).reshape(-1, 2)
     ouv = np.asarray(ouv).reshape(-1, 2)
     scale = np.maximum(np.abs(np.asarray(P).reshape(-1, 3)).max(1), 1.0)
     found = st <= 1
-    no_worse = res <= ores * (1 + 1e-12) + 1e-14 * scale
+    no_worse = res <= ores * (1 + 1e-12) + res_abs * scale
     same = found & (np.abs(uv - ouv).max(1) <= UV_TOL) & no_worse
     closer = found & (res < ores - 1e-12)
     uniq = ost == 0

@@ -13,6 +13,7 @@ import pytest
 
 import oracle as O
 from conftest import golden_files, load_golden, GOLDEN
+from parity import eval_errors
 
 MODEL_FILES = [f for f in golden_files() if os.path.basename(f).startswith(("model_", "synth_"))]
 
@@ -110,3 +111,15 @@ def test_oracle_inversion_small_recovers_truth():
     assert ok.mean() > 0.95
     assert np.abs(ruv[ok] - uv[ok]).max() < 1e-12
     assert np.allclose(res[ok], np.abs(off[ok]), rtol=1e-6, atol=1e-12)
+
+
+def test_oracle_high_degree_eval_against_40_digit_values():
+    """Pins the high-degree accuracy fixture: the oracle (the reference's FP64 formulation) is
+    within its conditioning-limited error of the 40-digit values."""
+    z = np.load(os.path.join(GOLDEN, "eval_truth.npz"))
+    for d in z["degrees"]:
+        tag = f"p{int(d[0])}q{int(d[1])}_"
+        sf = {k: z[tag + k] for k in ("knots_u", "knots_v", "cps", "weights")}
+        sf.update({k: int(z[tag + k]) for k in ("p", "q", "nu", "nv")})
+        errs = eval_errors(O.OracleSurface(sf).eval(z[tag + "uv"], 63), z[tag + "truth"])
+        assert max(errs) < 1e-9, (tag, errs)
