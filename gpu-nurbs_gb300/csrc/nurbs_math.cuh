@@ -225,14 +225,30 @@ GN_HD v4<T> vmad(const v4<T>& a, T s, const v4<T>& c) {
   return {mad(a.x, s, c.x), mad(a.y, s, c.y), mad(a.z, s, c.z), mad(a.w, s, c.w)};
 }
 
+// Coefficient loads through the read-only path.  An FP64 coefficient (32 bytes, 32-byte
+// aligned) is one 256-bit load; two adjacent FP32 coefficients starting at an even index of a
+// 32-byte aligned table are one 256-bit load too, halving the load instructions and the L1
+// wavefronts of the gathers, which bound the FP32 evaluation.
 __device__ __forceinline__ v4<double> load_coef(const double* m, int idx) {
-  const double2* p = reinterpret_cast<const double2*>(m + 4 * idx);
-  double2 lo = __ldg(p), hi = __ldg(p + 1);
-  return {lo.x, lo.y, hi.x, hi.y};
+  v4<double> c;
+  asm("ld.global.nc.v4.f64 {%0, %1, %2, %3}, [%4];"
+      : "=d"(c.x), "=d"(c.y), "=d"(c.z), "=d"(c.w)
+      : "l"(m + 4 * idx));
+  return c;
 }
 __device__ __forceinline__ v4<float> load_coef(const float* m, int idx) {
   float4 f = __ldg(reinterpret_cast<const float4*>(m + 4 * idx));
   return {f.x, f.y, f.z, f.w};
+}
+// coefficients idx (lo) and idx + 1 (hi); idx even, table 32-byte aligned
+__device__ __forceinline__ void load_coef_pair(const float* m, int idx, v4<float>& lo, v4<float>& hi) {
+  asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+      : "=f"(lo.x), "=f"(lo.y), "=f"(lo.z), "=f"(lo.w), "=f"(hi.x), "=f"(hi.y), "=f"(hi.z), "=f"(hi.w)
+      : "l"(m + 4 * idx));
+}
+__device__ __forceinline__ void load_coef_pair(const double* m, int idx, v4<double>& lo, v4<double>& hi) {
+  lo = load_coef(m, idx);
+  hi = load_coef(m, idx + 1);
 }
 
 // Horner accumulator tracking value and D derivatives (D <= 2).  Coefficients are pushed from
@@ -289,10 +305,21 @@ __device__ __forceinline__ RDer<T> span_contract(const T* __restrict__ m, int p_
   for (int a = (P > 0 ? P : kMaxDegree); a >= 0; --a) {
     if (P == 0 && a > pp) continue;
     Horner<T, ORDER> row;
+    if constexpr (Q > 0 && (Q & 1)) {
+      // (q+1) even: coefficients (a, b-1) and (a, b) for odd b share one aligned 256-bit load
 #pragma unroll
-    for (int b = (Q > 0 ? Q : kMaxDegree); b >= 0; --b) {
-      if (Q == 0 && b > qq) continue;
-      row.push(load_coef(m, a * k2 + b), v);
+      for (int b = Q; b >= 1; b -= 2) {
+        v4<T> lo, hi;
+        load_coef_pair(m, a * k2 + b - 1, lo, hi);
+        row.push(hi, v);
+        row.push(lo, v);
+      }
+    } else {
+#pragma unroll
+      for (int b = (Q > 0 ? Q : kMaxDegree); b >= 0; --b) {
+        if (Q == 0 && b > qq) continue;
+        row.push(load_coef(m, a * k2 + b), v);
+      }
     }
     colR.push(row.p, u);
     if (ORDER >= 1) colV.push(row.dp, u);
