@@ -361,7 +361,7 @@ def run_batched(a):
     t_mixed = timed(g_mixed.launch, a.steps)
     phase("mixed timed")
     t_e2e = []
-    for k in range(max(3, a.steps // 2)):
+    for k in range(1 + max(3, a.steps // 2)):   # the first pass (untimed) maps the pinned buffers
         flush.fill_(float(k))
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -370,7 +370,8 @@ def run_batched(a):
         for h, d in zip(hout, out):
             h.copy_(d, non_blocking=True)
         torch.cuda.synchronize()
-        t_e2e.append((time.perf_counter() - t0) * 1e3)
+        if k > 0:
+            t_e2e.append((time.perf_counter() - t0) * 1e3)
     phase("e2e timed")
     clk = clocks.stop()
     phase("clocks read")

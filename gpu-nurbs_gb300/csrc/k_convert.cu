@@ -115,9 +115,8 @@ __device__ void span_component(const SurfDev& s, const double* __restrict__ basi
         size_t pos = (((size_t)i * (q + s.nv) + j) * 4 + c) * (size_t)(k1 * k2) + a * k2 + l;
         ref_out[pos] = acc;
       } else {
-        size_t o = ((size_t)span * k1 * k2 + a * k2 + l) * 4 + c;
-        m64[o] = acc;
-        m32[o] = (float)acc;
+        m64[((size_t)span * k1 * k2 + a * k2 + l) * 4 + c] = acc;
+        m32[((size_t)span * span_coefs32(p, q) + a * k2 + l) * 4 + c] = (float)acc;
       }
     }
 }

@@ -7,6 +7,13 @@ namespace gnurbs {
 
 constexpr int kMaxDegree = 7;     // p, q <= 7 (reference MAX_DEGREE 8 = p+1)
 constexpr int kTreeNodes = 65;    // root + 8x8 children
+
+// Coefficients per span in the FP32 span table: (p+1)(q+1) rounded up to even, so every span
+// starts 32-byte aligned and coefficient pairs can be read with one 256-bit load.
+__host__ __device__ inline int span_coefs32(int p, int q) {
+  const int k = (p + 1) * (q + 1);
+  return k + (k & 1);
+}
 constexpr int kGap = 8;           // GapPerEdge (src/kernel/kernel.cuh:17)
 constexpr int kPts = kGap + 1;    // PointsPerEdge
 

@@ -305,15 +305,23 @@ __device__ __forceinline__ RDer<T> span_contract(const T* __restrict__ m, int p_
   for (int a = (P > 0 ? P : kMaxDegree); a >= 0; --a) {
     if (P == 0 && a > pp) continue;
     Horner<T, ORDER> row;
-    if constexpr (Q > 0 && (Q & 1)) {
-      // (q+1) even: coefficients (a, b-1) and (a, b) for odd b share one aligned 256-bit load
+    if constexpr (P > 0 && Q > 0) {
+      // Spans start at an even coefficient index, so coefficients (a, b-1) and (a, b) share
+      // one aligned 256-bit load when a*(q+1) + b - 1 is even; a coefficient left over at
+      // either end of the row is loaded alone.
+      int b = Q;
+      if (((a * k2 + b - 1) & 1) && b >= 0) {  // row starts on an unpaired coefficient
+        row.push(load_coef(m, a * k2 + b), v);
+        --b;
+      }
 #pragma unroll
-      for (int b = Q; b >= 1; b -= 2) {
+      for (; b >= 1; b -= 2) {
         v4<T> lo, hi;
         load_coef_pair(m, a * k2 + b - 1, lo, hi);
         row.push(hi, v);
         row.push(lo, v);
       }
+      if (b == 0) row.push(load_coef(m, a * k2), v);
     } else {
 #pragma unroll
       for (int b = (Q > 0 ? Q : kMaxDegree); b >= 0; --b) {
@@ -438,7 +446,7 @@ __device__ __forceinline__ SDer<T> eval_point(const SurfDev& s, T u, T v) {
   T idu = __ldg(iu + su), idv = __ldg(iv + sv);
   T lu = (u - __ldg(bu + su)) * idu;
   T lv = (v - __ldg(bv + sv)) * idv;
-  const int k12 = (s.p + 1) * (s.q + 1);
+  const int k12 = sizeof(T) == 4 ? span_coefs32(s.p, s.q) : (s.p + 1) * (s.q + 1);
   const T* span = m + (size_t)(su * s.ns_v + sv) * k12 * 4;
   RDer<T> d = span_contract<T, P, Q, ORDER>(span, s.p, s.q, lu, lv);
   T ru, rv;
@@ -500,7 +508,7 @@ __device__ __forceinline__ SDer<T> eval_at(const Locator<T>& L, const T* __restr
   T idu = L.iu[hu], idv = L.iv[hv];
   T lu = (u - L.bu[hu]) * idu;
   T lv = (v - L.bv[hv]) * idv;
-  const int k12 = (p + 1) * (q + 1);
+  const int k12 = sizeof(T) == 4 ? span_coefs32(p, q) : (p + 1) * (q + 1);
   const T* span = m + (size_t)(hu * L.ns_v + hv) * k12 * 4;
   RDer<T> d = span_contract<T, P, Q, ORDER>(span, p, q, lu, lv);
   return quotient<T, ORDER, FAST>(d, L.ru * idu, L.rv * idv);

@@ -109,7 +109,7 @@ inline int prepare_surface(int p, int q, int nu, int nv, const double* ku, const
   off = 0;
   const size_t k12 = (size_t)(p + 1) * (q + 1), nspan = (size_t)nsu * nsv;
   S.o_m64 = take(nspan * k12 * 4 * 8);
-  S.o_m32 = take(nspan * k12 * 4 * 4);
+  S.o_m32 = take(nspan * (size_t)span_coefs32(p, q) * 4 * 4);
   S.o_bas_u = take((size_t)nsu * (p + 1) * (p + 1) * 8);
   S.o_bas_v = take((size_t)nsv * (q + 1) * (q + 1) * 8);
   S.out_bytes = off;
