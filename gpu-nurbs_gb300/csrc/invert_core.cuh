@@ -16,7 +16,7 @@ constexpr int kModeMixed = 1;
 
 constexpr int kWarps = 4;          // warps per CTA
 constexpr int kThreads = 32 * kWarps;
-constexpr int kMinBlocksMixed = 4;  // CTAs per SM the mixed kernel is register-budgeted for
+constexpr int kMinBlocksMixed = 6;  // CTAs per SM the mixed kernels are register-budgeted for (80 registers)
 constexpr int kMaxIter32 = 24;     // FP32 iterations per seed
 constexpr int kMaxIter64 = 40;     // FP64-mode iterations per seed
 constexpr int kMaxFinal64 = 6;     // MIXED: FP64 steps (2 normally)

@@ -154,7 +154,8 @@ __device__ __forceinline__ void dispatch_chunk_cta(Staged<kCtaSpans>& sm, WarpWo
 }
 
 template <int MODE>
-__global__ void __launch_bounds__(kThreads, 4) k_invert_pool_cta(const SurfDev* __restrict__ table,
+__global__ void __launch_bounds__(kThreads, MODE == kModeMixed ? kMinBlocksMixed : 4)
+    k_invert_pool_cta(const SurfDev* __restrict__ table,
                                                               const InvTile* __restrict__ tiles, int ntiles,
                                                               int* __restrict__ counter, const double* __restrict__ P,
                                                               double* __restrict__ uv, int* __restrict__ st,

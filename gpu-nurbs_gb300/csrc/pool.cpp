@@ -549,7 +549,7 @@ int nurbs_pool_autotune(nurbs_pool_t P, int nbatch, const int* ids, const int64_
   }
   // above 32: CTA tiles (throughput); 32 and below: warp chunks (latency, small batches)
   const int tile_opts[] = {128, 256, 32, 16};
-  const int cta_opts[] = {2, 3, 4};
+  const int cta_opts[] = {4, 5, 6};
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
