@@ -143,3 +143,20 @@ def test_high_degree_eval_no_worse_than_reference(nurbs, pq):
     ref = eval_errors(O.OracleSurface(sf).eval(uv, 63), truth)
     for b in range(6):
         assert mine[b] <= 2 * ref[b] + 1e-14, (b, mine, ref)
+
+
+def test_host_buffer_pipeline_matches_device_call(nurbs):
+    """Host-buffer inversion of a large batch equals the device-buffer call bit for bit, with
+    pinned and with pageable host memory."""
+    sf = surface(3, 3, 8, 8, 10)
+    s, o = nurbs.Surface(sf), O.OracleSurface(sf)
+    n = (1 << 19) + 77
+    P = queries(o, n, 6)
+    uv, st, res = (x.cpu().numpy() for x in s.invert(T(P), 1))
+    for pinned in (True, False):
+        Ph = torch.from_numpy(P).pin_memory().numpy() if pinned else P.copy()
+        out = tuple(torch.empty(sh, dtype=dt).pin_memory().numpy() if pinned else np.empty(sh, npdt)
+                    for sh, dt, npdt in (((n, 2), torch.float64, np.float64), (n, torch.int32, np.int32),
+                                         (n, torch.float64, np.float64)))
+        hu, hs, hr = s.invert_host(Ph, 1, out=out)
+        assert np.array_equal(hs, st) and np.array_equal(hu, uv, equal_nan=True) and np.array_equal(hr, res, equal_nan=True)
