@@ -252,11 +252,14 @@ __device__ __forceinline__ int finish_status(const double* us, const double* vs,
 
 // One surface staged in shared memory: tree boxes (FP32 outward-rounded and exact FP64), seed
 // centres, domain, and breakpoint tables when the surface has at most KS spans per direction.
-template <int KS>
+// FP64 breakpoint tables are staged only for the FP64 schedule: the mixed schedule reads them in
+// its few final FP64 steps from global memory, which leaves more of the SM's memory to L1.
+template <int KS, int MODE>
 struct Staged {
+  static constexpr int KS64 = MODE == kModeMixed ? 1 : KS;
   float box32[kTreeNodes][6];   // rounded outward: a point outside is outside the exact box
   float box32i[kTreeNodes][6];  // rounded inward: a point strictly inside is inside the exact box
-  double box64[kTreeNodes][6];
+  const TreeNodeDev* tree;     // exact FP64 boxes, read only near a face (global memory, L2)
   double ctr[kTreeNodes][2];
   float ctr32[kTreeNodes][2];
   float dom32[4];
@@ -264,7 +267,7 @@ struct Staged {
   Cells<double> cell64;
   int nb;
   float sb32[2][KS + 1], si32[2][KS];
-  double sb64[2][KS + 1], si64[2][KS];
+  double sb64[2][KS64 + 1], si64[2][KS64];
 };
 
 // Per-warp bookkeeping of the task scheduler: candidate masks, task-order tables, per-query
@@ -283,26 +286,36 @@ struct WarpWork {
 
 // Cooperative over `nthreads` threads (index tid): stages one surface and fills the context.
 // The callers synchronise the participating threads before and after.
-template <int KS>
-__device__ __forceinline__ void stage_surface(const SurfDev& s, Staged<KS>& sm, Ctx& cx, int tid, int nthreads) {
+template <int KS, int MODE>
+__device__ __forceinline__ void stage_surface(const SurfDev& s, Staged<KS, MODE>& sm, Ctx& cx, int tid, int nthreads) {
+  constexpr int KS64 = Staged<KS, MODE>::KS64;
   const bool smem_tables = s.ns_u <= KS && s.ns_v <= KS;
+  const bool smem_tables64 = s.ns_u <= KS64 && s.ns_v <= KS64;
   if (smem_tables) {
     for (int k = tid; k <= s.ns_u; k += nthreads) {
       sm.sb32[0][k] = s.bu32[k];
-      sm.sb64[0][k] = s.bu[k];
-      if (k < s.ns_u) { sm.si32[0][k] = s.inv_du32[k]; sm.si64[0][k] = s.inv_du[k]; }
+      if (smem_tables64) sm.sb64[0][k] = s.bu[k];
+      if (k < s.ns_u) {
+        sm.si32[0][k] = s.inv_du32[k];
+        if (smem_tables64) sm.si64[0][k] = s.inv_du[k];
+      }
     }
     for (int k = tid; k <= s.ns_v; k += nthreads) {
       sm.sb32[1][k] = s.bv32[k];
-      sm.sb64[1][k] = s.bv[k];
-      if (k < s.ns_v) { sm.si32[1][k] = s.inv_dv32[k]; sm.si64[1][k] = s.inv_dv[k]; }
+      if (smem_tables64) sm.sb64[1][k] = s.bv[k];
+      if (k < s.ns_v) {
+        sm.si32[1][k] = s.inv_dv32[k];
+        if (smem_tables64) sm.si64[1][k] = s.inv_dv[k];
+      }
     }
   }
   cx.L32 = fast::global_locator<float>(s);
   cx.L64 = fast::global_locator<double>(s);
   if (smem_tables) {
     cx.L32.bu = sm.sb32[0]; cx.L32.bv = sm.sb32[1]; cx.L32.iu = sm.si32[0]; cx.L32.iv = sm.si32[1];
-    cx.L64.bu = sm.sb64[0]; cx.L64.bv = sm.sb64[1]; cx.L64.iu = sm.si64[0]; cx.L64.iv = sm.si64[1];
+    if (smem_tables64) {
+      cx.L64.bu = sm.sb64[0]; cx.L64.bv = sm.sb64[1]; cx.L64.iu = sm.si64[0]; cx.L64.iv = sm.si64[1];
+    }
   }
   cx.m32 = s.m32;
   cx.m64 = s.m64;
@@ -315,8 +328,6 @@ __device__ __forceinline__ void stage_surface(const SurfDev& s, Staged<KS>& sm, 
   for (int k = tid; k < nb; k += nthreads) {
     const TreeNodeDev& T = s.tree[k];
     for (int j = 0; j < 3; ++j) {
-      sm.box64[k][j] = T.lb[j];
-      sm.box64[k][3 + j] = T.rt[j];
       sm.box32[k][j] = __double2float_rd(T.lb[j]);
       sm.box32[k][3 + j] = __double2float_ru(T.rt[j]);
       sm.box32i[k][j] = __double2float_ru(T.lb[j]);
@@ -329,6 +340,7 @@ __device__ __forceinline__ void stage_surface(const SurfDev& s, Staged<KS>& sm, 
   }
   if (tid == 0) {
     sm.nb = nb;
+    sm.tree = s.tree;
     const float slack = 1e-4f;  // FP32 domain test is a prefilter; the FP64 phase decides
     sm.dom32[0] = (float)s.dom_u0 - slack;
     sm.dom32[1] = (float)s.dom_u1 + slack;
@@ -343,7 +355,7 @@ __device__ __forceinline__ void stage_surface(const SurfDev& s, Staged<KS>& sm, 
 
 // One warp inverts the queries [q0, min(q0+32, qend)) of the staged surface.
 template <int P, int Q, int MODE, int KS>
-__device__ __forceinline__ void invert_chunk(Staged<KS>& sm, WarpWork<MODE>& ww, const Ctx& cx,
+__device__ __forceinline__ void invert_chunk(Staged<KS, MODE>& sm, WarpWork<MODE>& ww, const Ctx& cx,
                                              const double* __restrict__ Pq,
                                              int64_t q0, int64_t qend, double* __restrict__ uv_out,
                                              int* __restrict__ st_out, double* __restrict__ res_out) {
@@ -372,8 +384,9 @@ __device__ __forceinline__ void invert_chunk(Staged<KS>& sm, WarpWork<MODE>& ww,
             fy <= sm.box32[k][4] && fz <= sm.box32[k][5]) {
           const bool surely = fx > sm.box32i[k][0] && fy > sm.box32i[k][1] && fz > sm.box32i[k][2] &&
                               fx < sm.box32i[k][3] && fy < sm.box32i[k][4] && fz < sm.box32i[k][5];
-          if (surely || (px >= sm.box64[k][0] && py >= sm.box64[k][1] && pz >= sm.box64[k][2] &&
-                         px <= sm.box64[k][3] && py <= sm.box64[k][4] && pz <= sm.box64[k][5])) {
+          const TreeNodeDev* B = sm.tree + k;
+          if (surely || (px >= B->lb[0] && py >= B->lb[1] && pz >= B->lb[2] && px <= B->rt[0] && py <= B->rt[1] &&
+                         pz <= B->rt[2])) {
             if (k < 64) m0 |= 1ull << k;
             else m1 = 1u;
           }

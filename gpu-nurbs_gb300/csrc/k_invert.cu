@@ -44,7 +44,7 @@ __global__ void __launch_bounds__(kThreads, MODE == kModeMixed ? kMinBlocksMixed
     k_invert(SurfDev s, const double* __restrict__ Pq, int64_t n, double* __restrict__ uv_out,
              int* __restrict__ st_out, double* __restrict__ res_out, unsigned* __restrict__ counter,
              int64_t n_big) {
-  __shared__ Staged<kSmemSpans> sm;           // one surface for the whole CTA
+  __shared__ Staged<kSmemSpans, MODE> sm;           // one surface for the whole CTA
   __shared__ WarpWork<MODE> ww[kWarps];
   Ctx cx;
   stage_surface<kSmemSpans>(s, sm, cx, threadIdx.x, blockDim.x);

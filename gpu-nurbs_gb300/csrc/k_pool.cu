@@ -22,14 +22,14 @@ using namespace inv;
 constexpr int kPoolSpans = 64;  // breakpoint tables staged per warp up to this many spans
 
 template <int P, int Q, int MODE>
-__device__ __noinline__ void chunk_variant(Staged<kPoolSpans>& sm, WarpWork<MODE>& ww, const Ctx& cx,
+__device__ __noinline__ void chunk_variant(Staged<kPoolSpans, MODE>& sm, WarpWork<MODE>& ww, const Ctx& cx,
                                            const double* __restrict__ P_, int64_t q0, int64_t qend,
                                            double* __restrict__ uv, int* __restrict__ st, double* __restrict__ res) {
   invert_chunk<P, Q, MODE, kPoolSpans>(sm, ww, cx, P_, q0, qend, uv, st, res);
 }
 
 template <int MODE>
-__device__ __forceinline__ void dispatch_chunk(Staged<kPoolSpans>& sm, WarpWork<MODE>& ww, const Ctx& cx,
+__device__ __forceinline__ void dispatch_chunk(Staged<kPoolSpans, MODE>& sm, WarpWork<MODE>& ww, const Ctx& cx,
                                                const double* __restrict__ P,
                                                int64_t q0, int64_t qend, double* __restrict__ uv, int* __restrict__ st,
                                                double* __restrict__ res) {
@@ -57,7 +57,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_invert_pool(const SurfDev* __re
                                                           int* __restrict__ counter, const double* __restrict__ P,
                                                           double* __restrict__ uv, int* __restrict__ st,
                                                           double* __restrict__ res, int group) {
-  __shared__ Staged<kPoolSpans> sm[kWarps];
+  __shared__ Staged<kPoolSpans, MODE> sm[kWarps];
   __shared__ WarpWork<MODE> ww[kWarps];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   Ctx cx;
@@ -123,7 +123,7 @@ __global__ void __launch_bounds__(128) k_eval_pool(const SurfDev* __restrict__ t
 constexpr int kCtaSpans = 256;
 
 template <int P, int Q, int MODE>
-__device__ __noinline__ void chunk_variant_cta(Staged<kCtaSpans>& sm, WarpWork<MODE>& ww, const Ctx& cx,
+__device__ __noinline__ void chunk_variant_cta(Staged<kCtaSpans, MODE>& sm, WarpWork<MODE>& ww, const Ctx& cx,
                                                const double* __restrict__ P_, int64_t q0, int64_t qend,
                                                double* __restrict__ uv, int* __restrict__ st,
                                                double* __restrict__ res) {
@@ -131,7 +131,7 @@ __device__ __noinline__ void chunk_variant_cta(Staged<kCtaSpans>& sm, WarpWork<M
 }
 
 template <int MODE>
-__device__ __forceinline__ void dispatch_chunk_cta(Staged<kCtaSpans>& sm, WarpWork<MODE>& ww, const Ctx& cx,
+__device__ __forceinline__ void dispatch_chunk_cta(Staged<kCtaSpans, MODE>& sm, WarpWork<MODE>& ww, const Ctx& cx,
                                                    const double* __restrict__ P, int64_t q0, int64_t qend,
                                                    double* __restrict__ uv, int* __restrict__ st,
                                                    double* __restrict__ res) {
@@ -160,7 +160,7 @@ __global__ void __launch_bounds__(kThreads, MODE == kModeMixed ? kMinBlocksMixed
                                                               int* __restrict__ counter, const double* __restrict__ P,
                                                               double* __restrict__ uv, int* __restrict__ st,
                                                               double* __restrict__ res) {
-  __shared__ Staged<kCtaSpans> sm;
+  __shared__ Staged<kCtaSpans, MODE> sm;
   __shared__ WarpWork<MODE> ww[kWarps];
   __shared__ int s_tile;
   Ctx cx;
