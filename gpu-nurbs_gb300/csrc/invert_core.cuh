@@ -276,12 +276,13 @@ template <int MODE>
 struct WarpWork {
   unsigned long long smask0[32];
   unsigned char smask1[32];
-  unsigned srmask[kTreeNodes];
-  int srpref[kTreeNodes + 1];
+  // round-major task order and the queries' FP64 coordinates: FP64 schedule only
+  unsigned srmask[MODE == kModeMixed ? 1 : kTreeNodes];
+  int srpref[MODE == kModeMixed ? 1 : kTreeNodes + 1];
   int slpref[32];
   typename std::conditional<MODE == kModeMixed, Rec32, Rec64>::type rec[32];
   float sp32[32][3];
-  double sp64[32][3];
+  double sp64[MODE == kModeMixed ? 1 : 32][3];
 };
 
 // Cooperative over `nthreads` threads (index tid): stages one surface and fills the context.
@@ -401,13 +402,13 @@ __device__ __forceinline__ void invert_chunk(Staged<KS, MODE>& sm, WarpWork<MODE
     int total = 0;
     for (int r = 0; r < maxc; ++r) {
       unsigned m = __ballot_sync(FULL, cnt > r);
-      if (lane == 0) {
+      if (MODE != kModeMixed && lane == 0) {
         ww.srmask[r] = m;
         ww.srpref[r] = total;
       }
       total += __popc(m);
     }
-    if (lane == 0) ww.srpref[maxc] = total;
+    if (MODE != kModeMixed && lane == 0) ww.srpref[maxc] = total;
     if constexpr (MODE == kModeMixed) {
       int incl = cnt;
 #pragma unroll
@@ -420,9 +421,11 @@ __device__ __forceinline__ void invert_chunk(Staged<KS, MODE>& sm, WarpWork<MODE
     ww.sp32[lane][0] = fx;
     ww.sp32[lane][1] = fy;
     ww.sp32[lane][2] = fz;
-    ww.sp64[lane][0] = px;
-    ww.sp64[lane][1] = py;
-    ww.sp64[lane][2] = pz;
+    if constexpr (MODE != kModeMixed) {
+      ww.sp64[lane][0] = px;
+      ww.sp64[lane][1] = py;
+      ww.sp64[lane][2] = pz;
+    }
     ww.smask0[lane] = m0;
     ww.smask1[lane] = (unsigned char)m1;
     if constexpr (MODE == kModeMixed) {
@@ -591,6 +594,10 @@ __device__ __forceinline__ void invert_chunk(Staged<KS, MODE>& sm, WarpWork<MODE
     if (cnt == 0) {
       status = 2;  // NURBS_INV_NO_CANDIDATE
     } else if constexpr (MODE == kModeMixed) {
+      // the query's FP64 coordinates again (not kept in registers through the seed loop)
+      px = Pq[3 * q];
+      py = Pq[3 * q + 1];
+      pz = Pq[3 * q + 2];
       double us[2], vs[2], rs[2];
       int ns = 0;
       const Rec32& R = ww.rec[lane];
