@@ -1,9 +1,10 @@
 // Stage d: candidate culling + Gauss-Newton point inversion (K4 invert), one fused kernel.
 //
 // Replaces NewInverse + GaussNewton (src/kernel/kernel.cu:433-469, 151-249).  Per query:
-//   1. cull: the built tree nodes sit in shared memory twice — as FP32 boxes rounded outward
-//      (a necessary test that never rejects a true hit) and as the exact FP64 boxes that decide
-//      it — so the candidate set equals the reference's NewBoundingBoxCheck scan bit for bit;
+//   1. cull: the built tree nodes sit in shared memory as FP32 boxes rounded outward (a point
+//      outside is outside the exact box) and inward (a point strictly inside is inside it); only
+//      coordinates within an FP32 ulp of a face are decided by the exact FP64 box, so the
+//      candidate set equals the reference's NewBoundingBoxCheck scan bit for bit;
 //   2. each candidate is seeded at its node's uv-centre (kernel.cu:154) and iterated with the
 //      reference's Gauss-Newton update  C <- C - (J^T J)^-1 J^T (S(C) - P)  (kernel.cu:195-243)
 //      until the step is small, then with Newton steps (Hessian J^T J + sum r_k d2S_k) whose
@@ -14,11 +15,11 @@
 // warp takes chunks of consecutive queries from a global counter until none are left, so
 // warps that drew expensive queries do not hold up the end of the launch.  Chunks hold 32
 // queries; on large launches the last two rounds hold 8, which shortens the tail in which the
-// last warps finish while the others idle.  A query has anywhere
-// from 0 to 65 candidate seeds and a seed needs from 2 to 24 iterations, so one thread per query
-// leaves most lanes of a warp idle.  Each warp owns 32 queries, flattens their (query, seed) pairs into a task list (warp prefix sum over
-// the candidate counts) and every lane pulls the next task as soon as its seed converges or
-// fails, so all 32 lanes iterate until the warp's list is exhausted.  Finished seeds are merged
+// last warps finish while the others idle.  A query has anywhere from 0 to 65 candidate seeds
+// and a seed needs from 2 to 24 iterations, so one thread per query leaves most lanes of a warp
+// idle.  Each warp flattens its chunk's (query, seed) pairs into a task list (warp prefix sum
+// over the candidate counts) and every lane pulls the next task as soon as its seed converges
+// or fails, so all 32 lanes iterate until the warp's list is exhausted.  Finished seeds are merged
 // into per-query records in shared memory, one lane at a time.  Every seed runs to its own end
 // (convergence, failure or the iteration cap), so a query's result does not depend on which
 // other queries share its warp: results are the same alone and in any batch.
