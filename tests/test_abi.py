@@ -114,3 +114,26 @@ def test_nu_comments_and_extra_values(nurbs):
     d = nurbs.parse_nu(text)
     assert np.array_equal(d["knots_u"], [0, 0, 1, 1])
     assert d["weights"][3] == 2.0
+
+
+def test_pool_surface_bytes_admission_size(nurbs):
+    """Host-only sizing used for budget admission: covers both span tables (FP64 and the FP32
+    table padded to an even coefficient count per span), grows with the net, rejects bad input."""
+    from gpu_nurbs_gb300 import synth
+    small, large = synth.surface_small(), synth.surface_large()
+    b_small, b_large = nurbs.surface_bytes(small), nurbs.surface_bytes(large)
+    spans = lambda k, p: len(np.unique(k[p:len(k) - p]))  - 1
+    for sf, b in ((small, b_small), (large, b_large)):
+        p, q = sf["p"], sf["q"]
+        ns = spans(sf["knots_u"], p) * spans(sf["knots_v"], q)
+        k12 = (p + 1) * (q + 1)
+        assert b >= ns * (k12 * 32 + (k12 + (k12 & 1)) * 16)
+        assert b % 256 == 0
+    assert b_large > b_small
+    # degree 2 x 2: 9 coefficients per span, FP32 spans padded to 10
+    d = dict(small, p=2, q=2, knots_u=synth.uniform_knots(2, small["nu"]), knots_v=synth.uniform_knots(2, small["nv"]))
+    ns = (small["nu"] - 2) * (small["nv"] - 2)
+    assert nurbs.surface_bytes(d) >= ns * (9 * 32 + 10 * 16)
+    bad = dict(small, knots_u=small["knots_u"][::-1].copy())
+    with pytest.raises(nurbs.NurbsError):
+        nurbs.surface_bytes(bad)
