@@ -26,12 +26,9 @@ constexpr double kTolNewton64 = 1e-10;  // a Newton step this small leaves < 1e-
 constexpr double kTolAny64 = 1e-14;
 constexpr double kDistinct = 1e-7;      // FP64 minima: grid cell size, times the domain's extent
 constexpr float kDistinct32 = 1e-4f;    // FP32 minima: the same
-constexpr float kJoin = 1e-3f;          // a Newton iterate this close to a known minimum joins it
-// Stopping a seed once it nears a minimum its query already found saves ~15-20 % of the
-// iterations, but whether the other seed has finished first depends on the other queries that
-// share the warp, so results would depend on how requests are batched.  Off: every seed runs
-// to its own end, and a query's result does not depend on its batch.
-constexpr bool kJoinSeeds = false;
+// Every seed runs to its own end.  Stopping a seed once it nears a minimum its query already
+// found saves ~15-20 % of the iterations, but whether that other seed has finished first
+// depends on the other queries sharing the warp, so results would depend on the batch.
 constexpr int kSols = 4;                // FP64 mode: distinct minima kept per query
 constexpr int kSmemSpans = 256;         // breakpoint tables staged in shared memory up to this
 
@@ -395,9 +392,10 @@ __device__ __forceinline__ void invert_chunk(Staged<KS, MODE>& sm, WarpWork<MODE
       }
     }
     const int cnt = __popcll(m0) + (int)m1;
-    // Task list in round-major order: round r holds seed r of every query that has more than
-    // r seeds, so each query's first seeds run first and its later seeds can join the minima
-    // those found.  rmask[r] = lanes with a seed in round r, rpref[r] = tasks before round r.
+    // Task lists.  FP64 schedule: round-major, round r holds seed r of every query with more
+    // than r seeds (rmask[r] = lanes with a seed in round r, rpref[r] = tasks before round r), so
+    // a warp's concurrent seeds come from different queries.  Mixed schedule: lane-major, a
+    // query's seeds consecutive (slpref = exclusive prefix of the candidate counts).
     const int maxc = __reduce_max_sync(FULL, (unsigned)cnt);
     int total = 0;
     for (int r = 0; r < maxc; ++r) {
@@ -508,12 +506,6 @@ __device__ __forceinline__ void invert_chunk(Staged<KS, MODE>& sm, WarpWork<MODE
         int res = kContinue;
         if (active) {
           res = iterate32<P, Q>(cx, tx, ty, tz, sd, dist);
-          if (kJoinSeeds && res == kContinue && sd.newton) {
-            const Rec32& R = ww.rec[ql];
-            if ((R.d1 < INFINITY && fabsf(sd.u - R.u1) <= kJoin && fabsf(sd.v - R.v1) <= kJoin) ||
-                (R.d2 < INFINITY && fabsf(sd.u - R.u2) <= kJoin && fabsf(sd.v - R.v2) <= kJoin))
-              res = kFailed;  // joins a minimum already found: nothing new
-          }
         }
         const bool done = active && res != kContinue;
         const bool keep = res == kConverged && sd.u >= sm.dom32[0] && sd.u <= sm.dom32[1] && sd.v >= sm.dom32[2] &&
@@ -559,11 +551,6 @@ __device__ __forceinline__ void invert_chunk(Staged<KS, MODE>& sm, WarpWork<MODE
         bool keep = false;
         if (active) {
           res = iterate64<P, Q>(cx, tx, ty, tz, sd);
-          if (kJoinSeeds && res == kContinue && sd.newton) {
-            const Rec64& R = ww.rec[ql];
-            for (int k = 0; k < R.n; ++k)
-              if (fabs(sd.u - R.u[k]) <= kJoin && fabs(sd.v - R.v[k]) <= kJoin) res = kFailed;
-          }
           if (res == kConverged) keep = finish64<P, Q>(cx, tx, ty, tz, sd.u, sd.v, sd.hu, sd.hv, rr);
         }
         const bool done = active && res != kContinue;
