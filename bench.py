@@ -103,6 +103,13 @@ TRAFFIC_PER_UNIT = {
 }
 
 
+def workload_label(name, n):
+    """The workload a bench line is about (the same string for this library and the reference arm)."""
+    return {"large": f"large: bicubic 64x64 net, 2^{int(np.log2(n))} queries, offsets |N(0,1e-2)|",
+            "small": f"small: bicubic 8x8 net, {n} queries, offsets N(0,1e-3)",
+            "quintic": f"quintic: degree 5x5 256x256 net, 2^{int(np.log2(n))} queries, offsets N(0,1e-3)"}[name]
+
+
 def mean_step_ms_over_ranks(ts, world, device):
     """Per-step time of the slowest rank: each rank's total over its timed steps, the maximum
     taken over ranks (an all-reduce of one number; nothing else crosses ranks), divided by the
@@ -262,9 +269,7 @@ def run_ours(a):
         "vs_baseline": None,
         "dtype": "fp32+fp64 (mixed)",
         "data": "synthetic (seeded)",
-        "config": {"workload": {"large": f"large: bicubic 64x64 net, 2^{int(np.log2(n))} queries, offsets |N(0,1e-2)|",
-                                "small": f"small: bicubic 8x8 net, {n} queries, offsets N(0,1e-3)",
-                                "quintic": f"quintic: degree 5x5 256x256 net, 2^{int(np.log2(n))} queries, offsets N(0,1e-3)"}[a.workload],
+        "config": {"workload": workload_label(a.workload, n),
                    "queries_per_step": n, "precision": "mixed", "l2": "flushed (512 MB write) before each step",
                    "parallelism": f"replicas x{world}"},
         "fp64_value": n * world / (ms_fp64 / 1e3),
@@ -640,7 +645,7 @@ def run_reference(a):
     load_pkg()
     from gpu_nurbs_gb300 import synth
     import oracle as O
-    surf = synth.surface_large() if a.workload == "large" else synth.surface_small()
+    surf = {"large": synth.surface_large, "quintic": synth.surface_quintic}.get(a.workload, synth.surface_small)()
     o = O.OracleSurface(surf)
     uv, off = synth.query_params(a.cpu_sample, 1000, "large" if a.workload == "large" else "small")
     E = o.eval(uv, 7)
@@ -661,8 +666,10 @@ def run_reference(a):
         "impl": "reference", "metric": METRIC, "value": v, "unit": "inversions/s", "n_gpus": world,
         "steps": a.steps, "warmup": a.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "fp64", "data": "synthetic (seeded)",
-        "config": {"workload": a.workload, "queries_per_step": len(P)},
-        "cpu_baseline": {"value": v, "unit": "inversions/s", "cores": cores, "kind": "port",
+        "config": {"workload": workload_label(a.workload if a.workload in ("large", "small", "quintic") else "small",
+                                              (1 << 24) if a.workload == "quintic" else a.queries),
+                   "queries_per_step": len(P), "note": "each step inverts a bounded sample of the workload"},
+        "cpu_baseline": {"value": v, "unit": "inversions/s", "cores": cores, "kind": kind,
                          "sample": f"{len(P)} queries per step (bounded sample of the workload), all host cores"},
         "e2e": {"value": v, "unit": "inversions/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }))

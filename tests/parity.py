@@ -55,4 +55,6 @@ def classify_inversion(uv, st, res, ouv, ost, ores, P, res_abs=1e-14):
                 no_candidate=int(nocand.sum()), fail_no_candidate=int(fail_nc.sum()),
                 oracle_not_converged=int(nconv.sum()), gpu_found_where_oracle_not=int((nconv & found).sum()),
                 max_uv_err_same=float(np.abs(uv - ouv).max(1)[uniq & same].max()) if (uniq & same).any() else 0.0,
+                p99_uv_err_same=float(np.percentile(np.abs(uv - ouv).max(1)[uniq & same], 99))
+                if (uniq & same).any() else 0.0,
                 fail_idx=np.nonzero(fail_u | fail_a | fail_nc)[0])
