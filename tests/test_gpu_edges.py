@@ -160,3 +160,38 @@ def test_host_buffer_pipeline_matches_device_call(nurbs):
                                          (n, torch.float64, np.float64)))
         hu, hs, hr = s.invert_host(Ph, 1, out=out)
         assert np.array_equal(hs, st) and np.array_equal(hu, uv, equal_nan=True) and np.array_equal(hr, res, equal_nan=True)
+
+
+def test_one_surface_from_many_streams_and_threads(nurbs):
+    """Inversions on one surface handle from four threads, each on its own stream, launched
+    repeatedly and overlapping on the GPU: every result equals the serial one."""
+    import threading
+    import ctypes as C
+    sf = surface(3, 3, 12, 12, 11)
+    s, o = nurbs.Surface(sf), O.OracleSurface(sf)
+    sets = [queries(o, 20000 + 37 * k, 20 + k) for k in range(4)]
+    ref = [[x.cpu().numpy() for x in s.invert(T(P), 1)] for P in sets]
+    streams = [torch.cuda.Stream() for _ in sets]
+    inputs = [T(P) for P in sets]
+    outs = [[None] * 6 for _ in sets]
+    errors = []
+
+    def work(k):
+        try:
+            h = C.c_void_p(streams[k].cuda_stream)
+            for rep in range(6):
+                outs[k][rep] = s.invert(inputs[k], 1, stream=h)
+        except Exception as e:  # reported below
+            errors.append(e)
+
+    threads = [threading.Thread(target=work, args=(k,)) for k in range(len(sets))]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    torch.cuda.synchronize()
+    assert not errors, errors
+    for k in range(len(sets)):
+        for rep in range(6):
+            uv, st, res = (x.cpu().numpy() for x in outs[k][rep])
+            assert np.array_equal(st, ref[k][1]) and np.array_equal(uv, ref[k][0], equal_nan=True), (k, rep)
