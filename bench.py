@@ -362,18 +362,24 @@ def run_batched(a):
     clocks = Clocks(0)
     t_mixed = timed(g_mixed.launch, a.steps)
     phase("mixed timed")
-    t_e2e = []
+    t_e2e, parts = [], []
     for k in range(1 + max(3, a.steps // 2)):   # the first pass (untimed) maps the pinned buffers
         flush.fill_(float(k))
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
         torch.cuda.synchronize()
         t0 = time.perf_counter()
+        ev[0].record(stream)
         Pd.copy_(Ph, non_blocking=True)
+        ev[1].record(stream)
         g_mixed.launch()
+        ev[2].record(stream)
         for h, d in zip(hout, out):
             h.copy_(d, non_blocking=True)
+        ev[3].record(stream)
         torch.cuda.synchronize()
         if k > 0:
             t_e2e.append((time.perf_counter() - t0) * 1e3)
+            parts.append([round(ev[i].elapsed_time(ev[i + 1]), 2) for i in range(3)])
     phase("e2e timed")
     clk = clocks.stop()
     phase("clocks read")
@@ -406,7 +412,7 @@ def run_batched(a):
                      "frac_found_within_1e9_of_truth": float((err[found] <= 1e-9).mean()) if found.any() else None},
         "e2e": {"value": n / (ms_e2e / 1e3), "unit": "inversions/s", "h2d_bytes_per_step": n * 24,
                 "d2h_bytes_per_step": n * 28, "ms_per_step": ms_e2e,
-                "step_ms": [round(t, 3) for t in t_e2e]},
+                "step_ms": [round(t, 3) for t in t_e2e], "h2d_kernel_d2h_ms": parts},
         "clocks": clk, "gpu_launches": a.steps,
     }
     if not a.no_cpu:
