@@ -512,8 +512,18 @@ __device__ __forceinline__ void invert_chunk(Staged<KS, MODE>& sm, WarpWork<MODE
                           sd.v <= sm.dom32[3];
         __syncwarp();
         int cu = 0, cv = 0;
-        if (done && keep) cell_of(sm.cell32, sd.u, sd.v, cu, cv);
-        unsigned fm = __ballot_sync(FULL, done && keep);
+        bool upd = done && keep;
+        if (upd) {
+          // Records only improve, so a result that cannot change its query's record now never
+          // will: only the others are merged, one lane at a time.
+          cell_of(sm.cell32, sd.u, sd.v, cu, cv);
+          const Rec32& R = ww.rec[ql];
+          if (R.d1 < INFINITY && cu == R.cu1 && cv == R.cv1)
+            upd = before(dist, sd.u, sd.v, R.d1, R.u1, R.v1);
+          else
+            upd = before(dist, sd.u, sd.v, R.d1, R.u1, R.v1) || before(dist, sd.u, sd.v, R.d2, R.u2, R.v2);
+        }
+        unsigned fm = __ballot_sync(FULL, upd);
         while (fm) {
           int j = __ffs(fm) - 1;
           if (lane == j) merge32(ww.rec[ql], cu, cv, sd.u, sd.v, dist);
