@@ -164,6 +164,26 @@ __device__ bool final64(const Ctx& c, double px, double py, double pz, double& u
   return false;
 }
 
+// Position of the k-th (0-based) set bit of m, which has more than k set bits: a fixed
+// five-step bisection on bit counts of the lower half of each window.
+__device__ __forceinline__ int select_bit(uint64_t m, int k) {
+  const unsigned lo = (unsigned)m;
+  const int clo = __popc(lo);
+  unsigned w32 = k < clo ? lo : (unsigned)(m >> 32);
+  int pos = k < clo ? 0 : 32;
+  if (k >= clo) k -= clo;
+#pragma unroll
+  for (int w = 16; w > 0; w >>= 1) {
+    const int c = __popc(w32 & ((1u << w) - 1u));
+    if (k >= c) {
+      k -= c;
+      w32 >>= w;
+      pos += w;
+    }
+  }
+  return pos;
+}
+
 struct Rec32 {  // per-query FP32 record: best and best distinct runner-up (squared distances)
   float u1, v1, d1, u2, v2, d2;
   int cu1, cv1;  // grid cell of the best
@@ -450,8 +470,7 @@ __device__ __forceinline__ void invert_chunk(Staged<KS, MODE>& sm, WarpWork<MODE
         uint64_t mm = ww.smask0[ql];
         int k = t - ww.slpref[lo];
         if (k < __popcll(mm)) {
-          for (int i = 0; i < k; ++i) mm &= mm - 1;
-          node = __ffsll((long long)mm) - 1;
+          node = select_bit(mm, k);
         } else {
           node = 64;
         }
@@ -473,8 +492,7 @@ __device__ __forceinline__ void invert_chunk(Staged<KS, MODE>& sm, WarpWork<MODE
       uint64_t mm = ww.smask0[ql];
       int c0 = __popcll(mm);
       if (k < c0) {
-        for (int i = 0; i < k; ++i) mm &= mm - 1;
-        node = __ffsll((long long)mm) - 1;
+        node = select_bit(mm, k);
       } else {
         node = 64;
       }
