@@ -159,7 +159,15 @@ __device__ bool final64(const Ctx& c, double px, double py, double pz, double& u
     if (!(isfinite(du) && isfinite(dv))) return false;
     u -= du;
     v -= dv;
-    if (fmax(fabs(du), fabs(dv)) <= kTolNewton64) return finish64<P, Q>(c, px, py, pz, u, v, hu, hv, res);
+    if (fmax(fabs(du), fabs(dv)) <= kTolNewton64) {
+      // Residual at the returned point from this step's FP64 S, Su, Sv: S(u - du, v - dv) =
+      // S - Su du - Sv dv + O(|S''| 1e-20), below the rounding of S itself.
+      const v3<double> r2 = {fast::mad(-d.Sv.x, dv, fast::mad(-d.Su.x, du, r.x)),
+                             fast::mad(-d.Sv.y, dv, fast::mad(-d.Su.y, du, r.y)),
+                             fast::mad(-d.Sv.z, dv, fast::mad(-d.Su.z, du, r.z))};
+      res = sqrt(dot3(r2, r2));
+      return (u >= c.dom_u0 && u <= c.dom_u1 && v >= c.dom_v0 && v <= c.dom_v1) && isfinite(res);
+    }
   }
   return false;
 }
