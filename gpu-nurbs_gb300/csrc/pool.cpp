@@ -119,7 +119,7 @@ struct nurbs_pool_s {
   std::vector<PoolSurface> surf;
   SurfDev* d_table = nullptr;  // device table of max_surfaces records (outside the arena)
   int tile_queries = 128;
-  int ctas_per_sm = 4;
+  int ctas_per_sm = 6;  // the CTA-tile kernel is budgeted for 6 (mixed)
   int sms = 152;
   std::map<cudaStream_t, Workspace> ws;
   std::set<struct nurbs_graph_s*> graphs;  // live graphs, detached if the pool goes first
