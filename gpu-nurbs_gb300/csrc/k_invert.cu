@@ -30,9 +30,10 @@
 //           minimum (plus a runner-up within 0.1 %) then takes the final two Newton steps in
 //           FP64: S, Su, Sv and the gradient J^T r in FP64, the Hessian's curvature term from
 //           FP32 second derivatives (it only sets the convergence rate), the 2x2 solve and the
-//           residual |S - P| at the returned point in FP64.  Extra FP64 steps (at most 4) run
-//           only when the second step is not yet below tolerance (near-singular or boundary
-//           cases).
+//           residual |S - P| at the returned point in FP64 (from the last step's S, Su, Sv and
+//           the step, a first-order update whose error is far below FP64 rounding).  Extra FP64
+//           steps (at most 4) run only when the second step is not yet below tolerance
+//           (near-singular or boundary cases).
 #include "invert_core.cuh"
 
 namespace gnurbs {
