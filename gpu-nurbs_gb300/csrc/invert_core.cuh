@@ -262,8 +262,10 @@ __device__ __forceinline__ void merge64(Rec64& R, int cu, int cv, double u, doub
 }
 
 // best minimum and status (FOUND / AMBIGUOUS), as the oracle decides them
-__device__ __forceinline__ int finish_status(const double* us, const double* vs, const double* rs, int n, double& u,
-                                             double& v, double& r) {
+// A minimum within (tu, tv) of the best is the same minimum: results that converged to one
+// point can fall on both sides of a grid-cell boundary (an exact parameter such as 0.5 is one).
+__device__ __forceinline__ int finish_status(const double* us, const double* vs, const double* rs, int n, double tu,
+                                             double tv, double& u, double& v, double& r) {
   int bi = 0;
   for (int k = 1; k < n; ++k)
     if (before(rs[k], us[k], vs[k], rs[bi], us[bi], vs[bi])) bi = k;
@@ -271,7 +273,8 @@ __device__ __forceinline__ int finish_status(const double* us, const double* vs,
   v = vs[bi];
   r = rs[bi];
   for (int k = 0; k < n; ++k)
-    if (k != bi && rs[k] <= r * (1 + 1e-6) + 1e-12) return 1;  // NURBS_INV_AMBIGUOUS
+    if (k != bi && rs[k] <= r * (1 + 1e-6) + 1e-12 && (fabs(us[k] - u) > tu || fabs(vs[k] - v) > tv))
+      return 1;  // NURBS_INV_AMBIGUOUS
   return 0;
 }
 
@@ -645,10 +648,10 @@ __device__ __forceinline__ void invert_chunk(Staged<KS, MODE>& sm, WarpWork<MODE
           }
         }
       }
-      status = ns == 0 ? 3 : finish_status(us, vs, rs, ns, ou, ov, orr);
+      status = ns == 0 ? 3 : finish_status(us, vs, rs, ns, kDistinct, kDistinct, ou, ov, orr);
     } else {
       const Rec64& R = ww.rec[lane];
-      status = R.n == 0 ? 3 : finish_status(R.u, R.v, R.r, R.n, ou, ov, orr);
+      status = R.n == 0 ? 3 : finish_status(R.u, R.v, R.r, R.n, 2.0 / sm.cell64.iu, 2.0 / sm.cell64.iv, ou, ov, orr);
     }
     if (valid) {
       uv_out[2 * q] = ou;

@@ -195,3 +195,23 @@ def test_one_surface_from_many_streams_and_threads(nurbs):
         for rep in range(6):
             uv, st, res = (x.cpu().numpy() for x in outs[k][rep])
             assert np.array_equal(st, ref[k][1]) and np.array_equal(uv, ref[k][0], equal_nan=True), (k, rep)
+
+
+def test_pcurve_of_a_curve_on_the_surface(nurbs):
+    """p-curve extraction (the reference README's use of inversion): the samples of a 3-D curve
+    lying on the surface, C(t) = S(u(t), v(t)) with (u, v) a closed loop in the domain, are
+    inverted in one batch; the recovered parameters are the loop's to 1e-9 and consecutive
+    samples stay close (no jumps between branches)."""
+    from gpu_nurbs_gb300 import synth
+    s = nurbs.Surface(synth.surface_large())
+    t = np.linspace(0.0, 1.0, 4001)
+    uv = np.stack([0.5 + 0.3 * np.cos(2 * np.pi * t), 0.5 + 0.2 * np.sin(4 * np.pi * t)], 1)
+    C = s.eval(T(uv), nurbs.S).cpu().numpy().T.copy()         # (n, 3) samples of the curve
+    for prec in (1, 0):
+        g_uv, st, res = (x.cpu().numpy() for x in s.invert(T(C), prec))
+        assert (st == nurbs.INV_FOUND).mean() > 0.999
+        ok = st == nurbs.INV_FOUND
+        assert np.abs(g_uv[ok] - uv[ok]).max() <= 1e-9
+        assert res[ok].max() <= 1e-12
+        step = np.abs(np.diff(g_uv, axis=0)).max(1)
+        assert np.nanmax(step) < 5 * np.abs(np.diff(uv, axis=0)).max()
