@@ -215,3 +215,24 @@ def test_pcurve_of_a_curve_on_the_surface(nurbs):
         assert res[ok].max() <= 1e-12
         step = np.abs(np.diff(g_uv, axis=0)).max(1)
         assert np.nanmax(step) < 5 * np.abs(np.diff(uv, axis=0)).max()
+
+
+@pytest.mark.parametrize("offset", [(1000.0, -500.0, 250.0), (1e5, 2e5, -3e4)], ids=["1e3", "1e5"])
+def test_translated_surface(nurbs, offset):
+    """The same surface far from the origin (CAD coordinates): inversion still matches the
+    oracle, and finds the same parameters as for the surface at the origin."""
+    sf = surface(3, 3, 12, 12, 12)
+    moved = dict(sf, cps=sf["cps"] + np.asarray(offset))
+    o, om = O.OracleSurface(sf), O.OracleSurface(moved)
+    P = queries(o, 2048, 13)
+    Pm = P + np.asarray(offset)
+    for prec in (1, 0):
+        g_uv, g_st, g_res = (x.cpu().numpy() for x in nurbs.Surface(moved).invert(T(Pm), prec))
+        ouv, ost, ores, _ = om.invert(Pm)
+        c = classify_inversion(g_uv, g_st, g_res, ouv, ost, ores, Pm)
+        assert c["fail_no_candidate"] == 0, c
+        assert c["fail_unique"] + c["fail_ambiguous"] <= 0.01 * len(P), c
+        b_uv, b_st, _ = (x.cpu().numpy() for x in nurbs.Surface(sf).invert(T(P), prec))
+        both = (g_st == 0) & (b_st == 0)
+        assert both.mean() > 0.95
+        assert np.abs(g_uv[both] - b_uv[both]).max() <= 1e-6
