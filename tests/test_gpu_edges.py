@@ -236,3 +236,23 @@ def test_translated_surface(nurbs, offset):
         both = (g_st == 0) & (b_st == 0)
         assert both.mean() > 0.95
         assert np.abs(g_uv[both] - b_uv[both]).max() <= 1e-6
+
+
+@pytest.mark.parametrize("scale", [1e-3, 1e3], ids=["1e-3", "1e3"])
+def test_scaled_surface(nurbs, scale):
+    """The same surface in other units (metres vs millimetres): same parameters, oracle parity."""
+    sf = surface(3, 3, 12, 12, 14)
+    scaled = dict(sf, cps=sf["cps"] * scale)
+    o, os_ = O.OracleSurface(sf), O.OracleSurface(scaled)
+    P = queries(o, 2048, 15)
+    Ps = P * scale
+    for prec in (1, 0):
+        g_uv, g_st, g_res = (x.cpu().numpy() for x in nurbs.Surface(scaled).invert(T(Ps), prec))
+        ouv, ost, ores, _ = os_.invert(Ps)
+        c = classify_inversion(g_uv, g_st, g_res, ouv, ost, ores, Ps)
+        assert c["fail_no_candidate"] == 0, c
+        assert c["fail_unique"] + c["fail_ambiguous"] <= 0.01 * len(P), c
+        b_uv, b_st, _ = (x.cpu().numpy() for x in nurbs.Surface(sf).invert(T(P), prec))
+        both = (g_st == 0) & (b_st == 0)
+        assert both.mean() > 0.95
+        assert np.abs(g_uv[both] - b_uv[both]).max() <= 1e-6
