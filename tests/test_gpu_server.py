@@ -146,3 +146,28 @@ def test_replay_trace(nurbs, served, request):
                                                   torch.as_tensor(P[sl], device="cuda"), 1)]
         assert same_within_tolerance(d, (uv[sl], st[sl], res[sl]), P[sl])
     srv.close()
+
+
+def test_rejected_requests_and_shutdown(nurbs, served, request):
+    """Requests the server cannot take fail with a status (unknown surface and oversized
+    request at submission, an invalid surface on its upload ticket); destroying the server with
+    requests still queued behind a pause returns promptly (they complete with NURBS_E_STATE)."""
+    surfs, pool, ids = served
+    srv = nurbs.Server(pool, slots=1, max_batch_queries=256)
+    P = queries(surfs[0], 16, np.random.default_rng(8))
+    with pytest.raises(nurbs.NurbsError) as e:
+        srv.submit_invert(10 ** 6, P)
+    assert e.value.code == nurbs.E_INVALID
+    with pytest.raises(nurbs.NurbsError) as e:
+        srv.submit_invert(int(ids[0]), np.zeros((257, 3)))
+    assert e.value.code == nurbs.E_UNSUPPORTED
+    bad = dict(surfs[0], knots_u=np.asarray(surfs[0]["knots_u"])[::-1].copy())
+    t, sid = srv.submit_upload(bad)
+    assert srv.wait(t) == nurbs.E_INVALID and sid[0] < 0
+    srv.pause(True)
+    for _ in range(3):
+        srv.submit_invert(int(ids[0]), P)
+    import ctypes as C
+    h = srv.h
+    srv.h = C.c_void_p()  # destroy through the C-ABI while requests are queued
+    assert nurbs.lib().nurbs_server_destroy(h) == 0
