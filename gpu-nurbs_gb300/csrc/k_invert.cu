@@ -41,8 +41,10 @@ namespace {
 
 using namespace inv;
 
+// Register budget: 6 CTAs per SM (80 registers) for the mixed kernel of degrees up to 3; degree 5
+// keeps 128 registers (4 CTAs per SM), its larger Horner state spilling at 80.
 template <int P, int Q, int MODE>
-__global__ void __launch_bounds__(kThreads, MODE == kModeMixed ? kMinBlocksMixed : 4)
+__global__ void __launch_bounds__(kThreads, MODE == kModeMixed ? ((P == 5 || Q == 5) ? 4 : kMinBlocksMixed) : 4)
     k_invert(SurfDev s, const double* __restrict__ Pq, int64_t n, double* __restrict__ uv_out,
              int* __restrict__ st_out, double* __restrict__ res_out, unsigned* __restrict__ counter,
              int64_t n_big) {
