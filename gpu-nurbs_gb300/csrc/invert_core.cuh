@@ -261,7 +261,8 @@ __device__ __forceinline__ void merge64(Rec64& R, int cu, int cv, double u, doub
   R.u[slot] = u; R.v[slot] = v; R.r[slot] = r; R.cu[slot] = cu; R.cv[slot] = cv;
 }
 
-// best minimum and status (FOUND / AMBIGUOUS), as the oracle decides them
+// best minimum and status (FOUND / AMBIGUOUS): FOUND unless another distinct minimum is as
+// close within 1e-6 relative
 // A minimum within (tu, tv) of the best is the same minimum: results that converged to one
 // point can fall on both sides of a grid-cell boundary (an exact parameter such as 0.5 is one).
 __device__ __forceinline__ int finish_status(const double* us, const double* vs, const double* rs, int n, double tu,

@@ -17,8 +17,10 @@
 
 namespace gnurbs {
 
-// Nrc table for one span and one column c (1-based), see nurbs_oracle.c span_basis_matrix.
-// N[r-1][c-1] = Nrc(knot, d, r, c, I, I, d), I = span - (d-1); out is the span's (d+1)^2 matrix.
+// Nrc table for one span and one column c (1-based): the reference's recurrence
+// (src/NURBS/Evaluate.cu:90-103) evaluated bottom-up, each (r, j) entry once, in the
+// reference's expression order.  N[r-1][c-1] = Nrc(knot, d, r, c, I, I, d), I = span - (d-1);
+// out is the span's (d+1)^2 matrix.
 __device__ void basis_column(const double* __restrict__ knot, int d, int span, int c, double* __restrict__ out) {
   const int k = d + 1;
   const int I = span - (d - 1);

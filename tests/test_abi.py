@@ -137,3 +137,15 @@ def test_pool_surface_bytes_admission_size(nurbs):
     bad = dict(small, knots_u=small["knots_u"][::-1].copy())
     with pytest.raises(nurbs.NurbsError):
         nurbs.surface_bytes(bad)
+
+
+def test_product_does_not_use_the_oracle():
+    """The library and its binding never reach the oracle (test infrastructure only): no
+    import, path or symbol of it in the package sources or the public headers."""
+    import glob
+    files = glob.glob(os.path.join(ROOT, "gpu-nurbs_gb300", "*.py")) + \
+        glob.glob(os.path.join(ROOT, "gpu-nurbs_gb300", "csrc", "*")) + glob.glob(os.path.join(ROOT, "include", "*"))
+    assert files
+    for f in files:
+        text = open(f, errors="replace").read()
+        assert "import oracle" not in text and "orc_" not in text and "liboracle" not in text, f
