@@ -149,7 +149,11 @@ __device__ __forceinline__ bool finish64(const Ctx& c, double px, double py, dou
 // MIXED: the final FP64 Newton steps from an FP32 minimum, then the residual.
 template <int P, int Q>
 __device__ bool final64(const Ctx& c, double px, double py, double pz, double& u, double& v, double& res) {
-  int hu = 0, hv = 0, hu32 = 0, hv32 = 0;
+  // span hints from the FP32 tables (shared memory when staged): the FP64 search then only
+  // confirms them with two reads instead of bisecting the FP64 tables in global memory
+  int hu = fast::find_seg_hint(c.L32.bu, c.L32.ns_u, (float)u, 0);
+  int hv = fast::find_seg_hint(c.L32.bv, c.L32.ns_v, (float)v, 0);
+  int hu32 = hu, hv32 = hv;
   for (int it = 0; it < kMaxFinal64; ++it) {
     fast::SDer<double> d = fast::eval_at<double, P, Q, 1>(c.L64, c.m64, c.p, c.q, u, v, hu, hv);
     fast::SDer<float> e = fast::eval_at<float, P, Q, 2, true>(c.L32, c.m32, c.p, c.q, (float)u, (float)v, hu32, hv32);
