@@ -296,6 +296,7 @@ struct Staged {
   double ctr[kTreeNodes][2];
   float ctr32[kTreeNodes][2];
   float dom32[4];
+  float far32[4];  // two domain extents around the domain: an FP32 iterate beyond is abandoned
   Cells<float> cell32;
   Cells<double> cell64;
   int nb;
@@ -380,6 +381,11 @@ __device__ __forceinline__ void stage_surface(const SurfDev& s, Staged<KS, MODE>
     sm.dom32[1] = (float)s.dom_u1 + slack;
     sm.dom32[2] = (float)s.dom_v0 - slack;
     sm.dom32[3] = (float)s.dom_v1 + slack;
+    const float fu = 2.0f * (float)(s.dom_u1 - s.dom_u0), fv = 2.0f * (float)(s.dom_v1 - s.dom_v0);
+    sm.far32[0] = (float)s.dom_u0 - fu;
+    sm.far32[1] = (float)s.dom_u1 + fu;
+    sm.far32[2] = (float)s.dom_v0 - fv;
+    sm.far32[3] = (float)s.dom_v1 + fv;
     const double eu = s.dom_u1 - s.dom_u0, ev = s.dom_v1 - s.dom_v0;
     sm.cell32 = {(float)s.dom_u0, (float)s.dom_v0, (float)(1.0 / ((double)kDistinct32 * eu)),
                  (float)(1.0 / ((double)kDistinct32 * ev))};
@@ -540,6 +546,9 @@ __device__ __forceinline__ void invert_chunk(Staged<KS, MODE>& sm, WarpWork<MODE
         int res = kContinue;
         if (active) {
           res = iterate32<P, Q>(cx, tx, ty, tz, sd, dist);
+          if (res == kContinue && !(sd.u >= sm.far32[0] && sd.u <= sm.far32[1] && sd.v >= sm.far32[2] &&
+                                    sd.v <= sm.far32[3]))
+            res = kFailed;
         }
         const bool done = active && res != kContinue;
         const bool keep = res == kConverged && sd.u >= sm.dom32[0] && sd.u <= sm.dom32[1] && sd.v >= sm.dom32[2] &&
