@@ -26,9 +26,10 @@ constexpr double kTolNewton64 = 1e-10;  // a Newton step this small leaves < 1e-
 constexpr double kTolAny64 = 1e-14;
 constexpr double kDistinct = 1e-7;      // FP64 minima: grid cell size, times the domain's extent
 constexpr float kDistinct32 = 1e-4f;    // FP32 minima: the same
-// Every seed runs to its own end.  Stopping a seed once it nears a minimum its query already
-// found saves ~15-20 % of the iterations, but whether that other seed has finished first
-// depends on the other queries sharing the warp, so results would depend on the batch.
+// Every seed runs to its own end, decided by the seed alone.  Stopping a seed once it nears a
+// minimum its query already found saves ~15-20 % of the iterations, but whether that other seed
+// has finished first depends on the other queries sharing the warp, so results would depend on
+// the batch.
 constexpr int kSols = 4;                // FP64 mode: distinct minima kept per query
 constexpr int kSmemSpans = 256;         // breakpoint tables staged in shared memory up to this
 

@@ -20,9 +20,11 @@
 // idle.  Each warp flattens its chunk's (query, seed) pairs into a task list (warp prefix sum
 // over the candidate counts) and every lane pulls the next task as soon as its seed converges
 // or fails, so all 32 lanes iterate until the warp's list is exhausted.  Finished seeds are merged
-// into per-query records in shared memory, one lane at a time.  Every seed runs to its own end
-// (convergence, failure or the iteration cap), so a query's result does not depend on which
-// other queries share its warp: results are the same alone and in any batch.
+// into per-query records in shared memory (only results that can change a record, one lane at
+// a time).  Every seed runs to its own end (convergence, failure, the iteration cap, or an FP32
+// iterate two domain extents outside the domain), decided by the seed alone, so a query's result
+// does not depend on which other queries share its warp: results are the same alone and in any
+// batch.
 //
 // Precision schedules (template MODE):
 //   FP64  — every evaluation, solve and update in FP64.
