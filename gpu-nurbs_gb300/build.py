@@ -10,7 +10,10 @@ point's result is the same in every kernel that computes it (single surface, poo
 from __future__ import annotations
 
 import concurrent.futures as cf
+import hashlib
+import json
 import os
+import platform
 import shutil
 import subprocess
 import sys
@@ -36,18 +39,46 @@ def nvcc() -> str:
     raise RuntimeError("nvcc not found")
 
 
-def _compile(src: str, verbose: bool) -> str:
+def _digest(parts, files) -> str:
+    """Content hash of a build step: its command line, the host machine and its input files."""
+    h = hashlib.sha256()
+    h.update(platform.machine().encode())
+    for x in parts:
+        h.update(x.encode() + b"\0")
+    for f in files:
+        with open(f, "rb") as fh:
+            h.update(fh.read())
+    return h.hexdigest()
+
+
+def _fresh(out: str, digest: str) -> bool:
+    """An output is reused only when its stamp records the same content hash (sources, flags,
+    machine): modification times are not trusted, since copied trees carry arbitrary ones."""
+    stamp = out + ".stamp"
+    if not (os.path.exists(out) and os.path.exists(stamp)):
+        return False
+    with open(stamp) as f:
+        return f.read().strip() == digest
+
+
+def _stamp(out: str, digest: str):
+    with open(out + ".stamp", "w") as f:
+        f.write(digest + "\n")
+
+
+def _compile(src: str, verbose: bool):
     path = os.path.join(CSRC, src)
     obj = os.path.join(OBJ, src + ".o")
-    deps = [path] + [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith((".h", ".cuh"))]
+    deps = [path] + sorted(os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith((".h", ".cuh")))
     deps.append(os.path.join(INCLUDE, "gpu_nurbs.h"))
-    if os.path.exists(obj) and os.path.getmtime(obj) >= max(os.path.getmtime(d) for d in deps):
-        return obj
     cmd = [nvcc()] + ARCH + COMMON
     if src in EXACT_TUS or src in EXPLICIT_FMA_TUS:
         cmd.append("--fmad=false")
     if src.endswith(".cpp"):
         cmd += ["-x", "cu"]
+    digest = _digest(cmd + [src], deps)
+    if _fresh(obj, digest):
+        return obj, False
     if verbose:
         cmd += ["-Xptxas", "-v"]
     cmd += ["-c", path, "-o", obj]
@@ -56,20 +87,31 @@ def _compile(src: str, verbose: bool) -> str:
         raise RuntimeError(f"nvcc failed for {src}:\n{r.stderr}")
     if verbose and r.stderr:
         sys.stderr.write(r.stderr)
-    return obj
+    _stamp(obj, digest)
+    return obj, True
 
 
 def build(verbose: bool = False, jobs: int | None = None) -> str:
+    """Compiles what changed and links the library.  Writes _build/build_record.json: which
+    translation units were compiled in this call and which were reused (same content hash)."""
     os.makedirs(OBJ, exist_ok=True)
     with cf.ThreadPoolExecutor(max_workers=jobs or min(8, os.cpu_count() or 4)) as ex:
-        objs = list(ex.map(lambda s: _compile(s, verbose), SOURCES))
-    if not os.path.exists(LIB) or os.path.getmtime(LIB) < max(os.path.getmtime(o) for o in objs):
+        res = list(ex.map(lambda s: _compile(s, verbose), SOURCES))
+    objs = [o for o, _ in res]
+    link_cmd = [nvcc()] + ARCH + ["-shared"] + [os.path.basename(o) for o in objs] + ["-lcudart"]
+    digest = _digest(link_cmd, objs)
+    linked = not _fresh(LIB, digest)
+    if linked:
         tmp = LIB + ".tmp"
         cmd = [nvcc()] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stderr}")
         os.replace(tmp, LIB)
+        _stamp(LIB, digest)
+    with open(os.path.join(OBJ, "build_record.json"), "w") as f:
+        json.dump({"machine": platform.machine(), "compiled": [s for s, (_, c) in zip(SOURCES, res) if c],
+                   "reused": [s for s, (_, c) in zip(SOURCES, res) if not c], "linked": linked}, f)
     return LIB
 
 

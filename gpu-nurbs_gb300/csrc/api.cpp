@@ -20,8 +20,10 @@
 using namespace gnurbs;
 
 namespace {
-
 thread_local std::string g_last_error;
+}  // namespace
+
+namespace gnurbs {
 
 int fail(int code, const char* fmt, ...) {
   char buf[512];
@@ -36,6 +38,10 @@ int fail(int code, const char* fmt, ...) {
 int cuda_fail(cudaError_t e, const char* what) {
   return fail(NURBS_E_CUDA, "%s: %s", what, cudaGetErrorString(e));
 }
+
+}  // namespace gnurbs
+
+namespace {
 
 #define CUDA_TRY(expr, what)                         \
   do {                                               \

@@ -13,6 +13,11 @@
 // The scratch is shared by all calls: overlapping calls on the GPU (on different streams or
 // host threads) race on it and must be serialised by the caller.  Each call rewrites all of
 // the scratch it reads (the span tables and their counts are cleared and rebuilt first).
+//
+// The device address of the array is looked up once per device, on the first call made with
+// that device current, and cached.  cudaDeviceReset destroys the context that holds the array;
+// the cached address then names freed memory, so the entry point must not be used again in a
+// process that has reset the device.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -80,12 +85,14 @@ size_t up256(size_t x) { return (x + 255) & ~size_t(255); }
 int scratch_for_current_device(unsigned char** out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess || dev < 0 || dev >= kMaxDevices) return NURBS_E_CUDA;
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+  if (dev < 0 || dev >= kMaxDevices) return fail(NURBS_E_UNSUPPORTED, "device ordinal %d above %d", dev, kMaxDevices - 1);
   std::lock_guard<std::mutex> lock(g_mu);
   if (!g_scratch_ptr[dev]) {
     void* ptr = nullptr;
     e = cudaGetSymbolAddress(&ptr, g_scratch);
-    if (e != cudaSuccess || ptr == nullptr) return NURBS_E_CUDA;
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress of the static scratch");
+    if (ptr == nullptr) return fail(NURBS_E_CUDA, "cudaGetSymbolAddress returned NULL for the static scratch");
     g_scratch_ptr[dev] = static_cast<unsigned char*>(ptr);
   }
   *out = g_scratch_ptr[dev];
@@ -101,9 +108,12 @@ extern "C" int nurbs_get_matrix_n_noalloc(double* matrix_n_dev, int p, int q, in
                                           const double* knots_u_dev, const double* knots_v_dev,
                                           const double* control_points_dev, const double* weights_dev,
                                           void* stream) {
-  if (!matrix_n_dev || !knots_u_dev || !knots_v_dev || !control_points_dev || !weights_dev) return NURBS_E_INVALID;
-  if (p < 1 || q < 1 || p > NURBS_MAX_DEGREE || q > NURBS_MAX_DEGREE || nu < p + 1 || nv < q + 1)
-    return NURBS_E_INVALID;
+  if (!matrix_n_dev || !knots_u_dev || !knots_v_dev || !control_points_dev || !weights_dev)
+    return fail(NURBS_E_INVALID, "NULL argument");
+  if (p < 1 || q < 1 || p > NURBS_MAX_DEGREE || q > NURBS_MAX_DEGREE)
+    return fail(NURBS_E_INVALID, "degrees (%d,%d) outside 1..%d", p, q, NURBS_MAX_DEGREE);
+  if (nu < p + 1 || nv < q + 1)
+    return fail(NURBS_E_INVALID, "control net %dx%d too small for degree (%d,%d)", nu, nv, p, q);
   const int k1 = p + 1, k2 = q + 1;
   // worst case: every knot interval in the domain is a span
   const size_t max_su = (size_t)(nu - p), max_sv = (size_t)(nv - q);
@@ -111,7 +121,9 @@ extern "C" int nurbs_get_matrix_n_noalloc(double* matrix_n_dev, int p, int q, in
   const size_t o_bas_u = o_idx_v + up256(max_sv * 4);
   const size_t o_bas_v = o_bas_u + up256(max_su * k1 * k1 * 8);
   const size_t need = o_bas_v + up256(max_sv * k2 * k2 * 8);
-  if (need > kStaticScratchBytes) return NURBS_E_UNSUPPORTED;  // surface too large for the static scratch
+  if (need > kStaticScratchBytes)
+    return fail(NURBS_E_UNSUPPORTED, "surface needs %zu bytes of scratch in the worst case, above the static %zu",
+                need, kStaticScratchBytes);
   unsigned char* scratch = nullptr;
   int rc = scratch_for_current_device(&scratch);
   if (rc != NURBS_OK) return rc;
@@ -122,14 +134,18 @@ extern "C" int nurbs_get_matrix_n_noalloc(double* matrix_n_dev, int p, int q, in
   double* bas_u = reinterpret_cast<double*>(scratch + o_bas_u);
   double* bas_v = reinterpret_cast<double*>(scratch + o_bas_v);
   // clear the counts left by the previous call, then rebuild the span tables
-  if (cudaMemsetAsync(counts, 0, sizeof(Counts), st) != cudaSuccess) return NURBS_E_CUDA;
+  cudaError_t e = cudaMemsetAsync(counts, 0, sizeof(Counts), st);
+  if (e != cudaSuccess) return cuda_fail(e, "clearing the static scratch");
   k_span_tables<<<1, 32, 0, st>>>(knots_u_dev, p, nu, knots_v_dev, q, nv, (int)max_su, (int)max_sv, counts, idx_u,
                                   idx_v);
-  if (cudaGetLastError() != cudaSuccess) return NURBS_E_CUDA;
+  if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "span-table launch");
   Counts h{};
-  if (cudaMemcpyAsync(&h, counts, sizeof(Counts), cudaMemcpyDeviceToHost, st) != cudaSuccess) return NURBS_E_CUDA;
-  if (cudaStreamSynchronize(st) != cudaSuccess) return NURBS_E_CUDA;
-  if (h.bad_u || h.bad_v) return NURBS_E_INVALID;
+  if ((e = cudaMemcpyAsync(&h, counts, sizeof(Counts), cudaMemcpyDeviceToHost, st)) != cudaSuccess)
+    return cuda_fail(e, "span-count copy");
+  if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return cuda_fail(e, "span-count wait");
+  if (h.bad_u || h.bad_v)
+    return fail(NURBS_E_INVALID, "%s knot vector is not finite and non-decreasing or has an empty domain",
+                h.bad_u ? "u" : "v");
   SurfDev d{};
   d.p = p;
   d.q = q;
@@ -141,8 +157,8 @@ extern "C" int nurbs_get_matrix_n_noalloc(double* matrix_n_dev, int p, int q, in
   d.knot_v = idx_v;
   d.cps = control_points_dev;
   d.weights = weights_dev;
-  cudaError_t e = launch_basis(knots_u_dev, p, idx_u, h.ns_u, bas_u, st);
+  e = launch_basis(knots_u_dev, p, idx_u, h.ns_u, bas_u, st);
   if (e == cudaSuccess) e = launch_basis(knots_v_dev, q, idx_v, h.ns_v, bas_v, st);
   if (e == cudaSuccess) e = launch_span_matrices(d, bas_u, bas_v, matrix_n_dev, nullptr, st);
-  return e == cudaSuccess ? NURBS_OK : NURBS_E_CUDA;
+  return e == cudaSuccess ? NURBS_OK : cuda_fail(e, "matrix-form conversion");
 }

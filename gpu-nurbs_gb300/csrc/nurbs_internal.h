@@ -63,6 +63,11 @@ struct TreeNodeDev {
   double lb[3], rt[3];
 };
 
+// ---- error text of the C-ABI (api.cpp): sets the calling thread's nurbs_last_error() message
+// and returns `code` (cuda_fail: NURBS_E_CUDA with the runtime's error string) ----
+int fail(int code, const char* fmt, ...);
+int cuda_fail(cudaError_t e, const char* what);
+
 // ---- launchers (each returns a cudaError_t from the launch) ----
 // stage a
 cudaError_t launch_basis(const double* knots, int degree, const int* knot_idx, int nspans,

@@ -249,8 +249,12 @@ void scheduler_main(nurbs_server_s* S) {
 int upload_one(nurbs_server_s* S, Request* r, int* id) {
   int rc = nurbs_pool_add(S->pool, 1, &r->desc, S->up_stream, id);
   while (rc == NURBS_E_BUDGET) {
-    // evict the least recently used surface no queued request references
+    // Evict the least recently used surface no queued request references.  The choice and the
+    // release happen under one hold of S->mu, the lock nurbs_server_submit_invert takes to check
+    // that a surface is live and to count its reference: no request can reference the victim
+    // between the check and the release (lock order S->mu, then the pool's lock, as in submit).
     int victim = -1;
+    int released = NURBS_E_INVALID;
     {
       std::lock_guard<std::mutex> lock(S->mu);
       Clock::time_point oldest = Clock::time_point::max();
@@ -259,9 +263,12 @@ int upload_one(nurbs_server_s* S, Request* r, int* id) {
           oldest = kv.second;
           victim = kv.first;
         }
-      if (victim >= 0) S->last_use.erase(victim);
+      if (victim >= 0) {
+        S->last_use.erase(victim);
+        released = pool_release_surface(S->pool, victim);
+      }
     }
-    if (victim < 0 || pool_release_surface(S->pool, victim) != NURBS_OK) break;
+    if (victim < 0 || released != NURBS_OK) break;
     rc = nurbs_pool_add(S->pool, 1, &r->desc, S->up_stream, id);
   }
   return rc;

@@ -132,8 +132,10 @@ int nurbs_get_matrix_n_raw(double* matrix_n_dev, int degree_u, int degree_v, int
  * (cp_v-degree_v)*(degree_v+1)^2*8 bytes (plus alignment) exceeds it return
  * NURBS_E_UNSUPPORTED.  The first call on a device looks up the array's device address
  * (cudaGetSymbolAddress, with that device current); make that first call before any stream
- * capture.  All calls share the array, so calls that overlap on the GPU race: serialise them.
- * Synchronises `stream` once (to read the span counts back). */
+ * capture.  The looked-up address is cached per device: do not call this entry point again
+ * after cudaDeviceReset in the same process (the reset frees the array the cache names).  All
+ * calls share the array, so calls that overlap on the GPU race: serialise them.  Synchronises
+ * `stream` once (to read the span counts back).  Errors set nurbs_last_error(). */
 #define NURBS_NOALLOC_SCRATCH_BYTES (1u << 20)
 int nurbs_get_matrix_n_noalloc(double* matrix_n_dev, int degree_u, int degree_v, int cp_u, int cp_v,
                                const double* knots_u_dev, const double* knots_v_dev,

@@ -67,3 +67,4 @@ def test_noalloc_rejects_surfaces_beyond_the_scratch(nurbs):
     rc = L.nurbs_get_matrix_n_noalloc(out.data_ptr(), p, q, nu, nv, t.data_ptr(), t.data_ptr(), t.data_ptr(),
                                       t.data_ptr(), st)
     assert rc == nurbs.E_UNSUPPORTED
+    assert b"scratch" in nurbs.lib().nurbs_last_error()
