@@ -17,6 +17,13 @@ TREE_NODES = 65
 
 S, SU, SV, SUU, SUV, SVV = 1, 2, 4, 8, 16, 32
 FOUND_UNIQUE, FOUND_AMBIGUOUS, NO_CANDIDATE, NOT_CONVERGED = 0, 1, 2, 3
+# Inversion: iteration cap per trajectory (the CUDA library's FP64 schedule has the same cap),
+# and the perturbations of the stability check: K points whose coordinates (relative to the
+# control net's centre) are scaled by (1 +- 2^-22) or (1 +- 2^-20), two and eight units of FP32
+# rounding.
+MAX_ITER = 40
+PERTURB_K = 8
+PERTURB_EPS = 2.0 ** -22
 
 _dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
 _ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
@@ -58,6 +65,12 @@ def lib():
         L.orc_invert.restype = None
         L.orc_invert.argtypes = [C.POINTER(_Surf), _dp, _dp, _bp, _dp, C.c_int64, C.c_int, _dp, _ip, _dp,
                                  C.c_void_p, C.c_int]
+        L.orc_invert_perturbed.restype = None
+        L.orc_invert_perturbed.argtypes = [C.POINTER(_Surf), _dp, _dp, _bp, _dp, C.c_int64, C.c_int, C.c_int,
+                                           C.c_double, _dp, _ip, _dp, C.c_int]
+        L.orc_invert_fp32_explore.restype = None
+        L.orc_invert_fp32_explore.argtypes = [C.POINTER(_Surf), _dp, _dp, _bp, _dp, C.c_int64, C.c_int, C.c_int,
+                                              C.c_double, _dp, _ip, _dp, C.c_int]
         L.orc_gauss_newton_shipped.restype = C.c_int
         L.orc_gauss_newton_shipped.argtypes = [C.POINTER(_Surf), _dp, _dp, _dp, C.c_double, _dp]
         L.orc_find_span.restype = C.c_int
@@ -123,7 +136,7 @@ class OracleSurface:
             out.append(lst[:n].copy())
         return out
 
-    def invert(self, P: np.ndarray, max_iter: int = 200, threads: int = 0):
+    def invert(self, P: np.ndarray, max_iter: int = MAX_ITER, threads: int = 0):
         t, _, b = self.tree()
         P = np.ascontiguousarray(P, dtype=np.float64).reshape(-1, 3)
         n = P.shape[0]
@@ -134,6 +147,48 @@ class OracleSurface:
         lib().orc_invert(C.byref(self._s), self.matrix_n, np.ascontiguousarray(t.reshape(-1)), b, P, n, max_iter,
                          uv, st, res, it.ctypes.data, threads)
         return uv.reshape(n, 2), st, res, it
+
+    def invert_perturbed(self, P: np.ndarray, K: int = PERTURB_K, eps: float = PERTURB_EPS, max_iter: int = MAX_ITER,
+                         threads: int = 0):
+        """Answers for K perturbations of P at FP32 resolution, carried back to P (see
+        orc_invert_perturbed): uv (K, n, 2), found (K, n) bool, residual (K, n)."""
+        t, _, b = self.tree()
+        P = np.ascontiguousarray(P, dtype=np.float64).reshape(-1, 3)
+        n = P.shape[0]
+        uv = np.empty(2 * K * n, dtype=np.float64)
+        found = np.empty(K * n, dtype=np.int32)
+        res = np.empty(K * n, dtype=np.float64)
+        lib().orc_invert_perturbed(C.byref(self._s), self.matrix_n, np.ascontiguousarray(t.reshape(-1)), b, P, n,
+                                   max_iter, K, eps, uv, found, res, threads)
+        return uv.reshape(K, n, 2), found.reshape(K, n).astype(bool), res.reshape(K, n)
+
+    def invert_fp32_explore(self, P: np.ndarray, perturbation: int = -1, eps: float = PERTURB_EPS,
+                            max_iter: int = MAX_ITER, threads: int = 0):
+        """The inversion with its exploration in FP32 arithmetic (orc_invert_fp32_explore), of the
+        points or of their perturbation `perturbation` (>= 0): uv (n, 2), found (n,) bool,
+        residual (n,), all for the true points."""
+        t, _, b = self.tree()
+        P = np.ascontiguousarray(P, dtype=np.float64).reshape(-1, 3)
+        n = P.shape[0]
+        uv = np.empty(2 * n, dtype=np.float64)
+        found = np.empty(n, dtype=np.int32)
+        res = np.empty(n, dtype=np.float64)
+        lib().orc_invert_fp32_explore(C.byref(self._s), self.matrix_n, np.ascontiguousarray(t.reshape(-1)), b, P, n,
+                                      max_iter, perturbation, eps, uv, found, res, threads)
+        return uv.reshape(n, 2), found.astype(bool), res
+
+    def stability_set(self, P: np.ndarray, threads: int = 0):
+        """The oracle's answers at FP32 resolution, for parity.classify_inversion: the answers
+        for the PERTURB_K perturbed points (FP64), and those of the FP32 exploration of the points
+        and of the same perturbed points, all carried to the true points; stacked (2K+1, n, ...)."""
+        pu, pf, pr = self.invert_perturbed(P, threads=threads)
+        us, fs, rs = [pu], [pf], [pr]
+        for k in range(-1, PERTURB_K):
+            fu, ff, fr = self.invert_fp32_explore(P, perturbation=k, threads=threads)
+            us.append(fu[None])
+            fs.append(ff[None])
+            rs.append(fr[None])
+        return np.concatenate(us), np.concatenate(fs), np.concatenate(rs)
 
     def gauss_newton_shipped(self, seed, P, max_edge):
         uv = np.zeros(2)

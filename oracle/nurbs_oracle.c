@@ -535,61 +535,362 @@ int orc_gauss_newton_shipped(const orc_surface* s, const double* M, const double
     return 0;
 }
 
+/* ------------------------------------------- inversion: the oracle's definition of the answer
+ *
+ * The reference stops Gauss-Newton when |S - P| < max_edge (kernel.cu:178), which cannot reach
+ * 1e-9 parameter error for points off the surface, and returns the first success (kernel.cu:
+ * 458-461).  The oracle's answer is defined instead as follows (a decision on those defects):
+ *   - every candidate node seeds one trajectory at its uv-centre (kernel.cu:154), in ascending
+ *     node order;
+ *   - a trajectory takes the reference's Gauss-Newton update (gn_step, kernel.cu:161-243) while
+ *     its last step was at least ORC_NEWTON_SWITCH in max-norm, and Newton steps once a step has
+ *     fallen below it: H = J^T J + sum_k r_k d2S_k (old second derivatives, Evaluate.cu:667-930)
+ *     when H is positive definite, the reference's GN update otherwise.  Both have the fixed
+ *     point J^T r = 0; GN converges only linearly, at rate ~|r| kappa, which is not small at
+ *     offsets of 1e-2, so a pure-GN definition leaves many queries unconverged;
+ *   - it has converged when a Newton-phase step is <= 1e-10 (the error is then ~1e-20) or any
+ *     step is <= 1e-14, and is dropped when it has not converged after max_iter iterations, when
+ *     its system is singular or when it converges outside the knot domain;
+ *   - the answer is the converged result of least distance (ties: lowest node); it is
+ *     AMBIGUOUS when another result more than 1e-7 away is within 1e-6 relative of it. */
+
+#define ORC_NEWTON_SWITCH 1e-2
+
+/* Newton step at C: returns 0 when H is not positive definite (the caller then takes the GN
+ * update).  r = S - P; H = [Su.Su + r.Suu, Su.Sv + r.Suv; Sv.Sv + r.Svv]; g = [Su.r, Sv.r]. */
+static int newton_step(const orc_surface* s, const double* M, const double C[2], const double P[3], double step[2]) {
+    const int p = s->degree_u, q = s->degree_v;
+    span_loc L = locate(s, M, C[0], C[1]);
+    d4 R = R_of(L.middle, p, q, L.u, L.v);
+    d3 S = cart(R);
+    d3 Su = der_u(L.middle, p, q, L.u, L.v, R, L.spanU);
+    d3 Sv = der_v(L.middle, p, q, L.u, L.v, R, L.spanV);
+    d3 Suu = der_uu(L.middle, p, q, L.u, L.v, R, L.spanU);
+    d3 Suv = der_uv(L.middle, p, q, L.u, L.v, R, L.spanU, L.spanV);
+    d3 Svv = der_vv(L.middle, p, q, L.u, L.v, R, L.spanV);
+    d3 r = {S.x - P[0], S.y - P[1], S.z - P[2]};
+    double h00 = (Su.x * Su.x + Su.y * Su.y + Su.z * Su.z) + (r.x * Suu.x + r.y * Suu.y + r.z * Suu.z);
+    double h01 = (Su.x * Sv.x + Su.y * Sv.y + Su.z * Sv.z) + (r.x * Suv.x + r.y * Suv.y + r.z * Suv.z);
+    double h11 = (Sv.x * Sv.x + Sv.y * Sv.y + Sv.z * Sv.z) + (r.x * Svv.x + r.y * Svv.y + r.z * Svv.z);
+    double det = h00 * h11 - h01 * h01;
+    if (!(h00 > 0 && det > 0)) return 0;
+    double g0 = Su.x * r.x + Su.y * r.y + Su.z * r.z;
+    double g1 = Sv.x * r.x + Sv.y * r.y + Sv.z * r.z;
+    step[0] = (h11 * g0 - h01 * g1) / det;
+    step[1] = (h00 * g1 - h01 * g0) / det;
+    return 1;
+}
+
+/* One trajectory from C (updated in place).  newton: start in the Newton phase (used to polish
+ * a given point).  Returns 1 when it converged; *iters counts the iterations. */
+static int run_trajectory(const orc_surface* s, const double* M, const double P[3], double C[2], int max_iter,
+                          int newton, int* iters) {
+    for (int it = 0; it < max_iter; ++it) {
+        double step[2];
+        if (!(newton && newton_step(s, M, C, P, step))) {
+            d3 S;
+            gn_step(s, M, C, P, &S, step);   /* the reference's update, kernel.cu:161-243 */
+        }
+        if (!(isfinite(step[0]) && isfinite(step[1]))) { *iters = it + 1; return 0; }
+        C[0] = C[0] - step[0];
+        C[1] = C[1] - step[1];
+        double m = fmax(fabs(step[0]), fabs(step[1]));
+        if ((newton && m <= 1e-10) || m <= 1e-14) { *iters = it + 1; return 1; }
+        newton = m < ORC_NEWTON_SWITCH;
+    }
+    *iters = max_iter;
+    return 0;
+}
+
+static void invert_one(const orc_surface* s, const double* M, const orc_tree_node* tree, const unsigned char* built,
+                       const double* Pk, int max_iter, const double dom[4], double* uv, int* status, double* residual,
+                       int* iters) {
+    int list[ORC_TREE_NODES];
+    int nc = orc_candidates(tree, built, Pk, list);
+    double best_uv[2] = {NAN, NAN}, best_r = INFINITY;
+    double sol_uv[ORC_TREE_NODES][2], sol_r[ORC_TREE_NODES];
+    int nsol = 0, total = 0;
+    for (int c = 0; c < nc; ++c) {
+        const orc_tree_node* T = &tree[list[c]];
+        /* seed = uv-centre of the node (kernel.cu:154) */
+        double C[2] = {(T->uv_lb[0] + T->uv_rt[0]) / 2, (T->uv_lb[1] + T->uv_rt[1]) / 2};
+        int its = 0;
+        int converged = run_trajectory(s, M, Pk, C, max_iter, 0, &its);
+        total += its;
+        if (!converged) continue;
+        if (!(C[0] >= dom[0] && C[0] <= dom[1] && C[1] >= dom[2] && C[1] <= dom[3])) continue;
+        double r = dist3(surface_point(s, M, C), Pk);
+        if (!isfinite(r)) continue;
+        sol_uv[nsol][0] = C[0];
+        sol_uv[nsol][1] = C[1];
+        sol_r[nsol] = r;
+        ++nsol;
+        if (r < best_r) { best_r = r; best_uv[0] = C[0]; best_uv[1] = C[1]; }
+    }
+    int st;
+    if (nc == 0) st = ORC_NO_CANDIDATE;
+    else if (nsol == 0) st = ORC_NOT_CONVERGED;
+    else {
+        st = ORC_FOUND_UNIQUE;
+        for (int t = 0; t < nsol; ++t) {
+            int same = fabs(sol_uv[t][0] - best_uv[0]) <= 1e-7 && fabs(sol_uv[t][1] - best_uv[1]) <= 1e-7;
+            if (!same && sol_r[t] <= best_r * (1 + 1e-6) + 1e-12) st = ORC_FOUND_AMBIGUOUS;
+        }
+    }
+    uv[0] = best_uv[0];
+    uv[1] = best_uv[1];
+    *status = st;
+    *residual = nsol ? best_r : NAN;
+    if (iters) *iters = total;
+}
+
+static void domain_of(const orc_surface* s, double dom[4]) {
+    dom[0] = s->knots_u[s->degree_u];
+    dom[1] = s->knots_u[s->cp_u];
+    dom[2] = s->knots_v[s->degree_v];
+    dom[3] = s->knots_v[s->cp_v];
+}
+
 void orc_invert(const orc_surface* s, const double* M, const orc_tree_node* tree, const unsigned char* built,
                 const double* P, int64_t n, int max_iter, double* uv, int* status, double* residual, int* iters,
                 int threads) {
-    const double u0 = s->knots_u[s->degree_u], u1 = s->knots_u[s->cp_u];
-    const double v0 = s->knots_v[s->degree_v], v1 = s->knots_v[s->cp_v];
+    double dom[4];
+    domain_of(s, dom);
+#ifdef _OPENMP
+    if (threads <= 0) threads = omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 64) num_threads(threads)
+#endif
+    for (int64_t k = 0; k < n; ++k)
+        invert_one(s, M, tree, built, P + 3 * k, max_iter, dom, uv + 2 * k, status + k, residual + k,
+                   iters ? iters + k : NULL);
+}
+
+/* ------------------------------------------------------ stability of the answer at FP32 resolution */
+
+/* Centre of the control net's bounding box: FP32 arithmetic of the surface is done relative to
+ * it, and perturbations at FP32 resolution are relative to it. */
+static void surface_origin(const orc_surface* s, double org[3]) {
+    for (int c = 0; c < 3; ++c) {
+        double lo = s->cps[c], hi = lo;
+        for (int i = 1; i < s->cp_u * s->cp_v; ++i) {
+            lo = fmin(lo, s->cps[3 * i + c]);
+            hi = fmax(hi, s->cps[3 * i + c]);
+        }
+        org[c] = 0.5 * (lo + hi);
+    }
+}
+
+/* Sign (+1/-1) of perturbation k of coordinate i: a fixed hash (splitmix64), so the perturbed
+ * points are the same on every machine. */
+static double perturb_sign(int k, int64_t i) {
+    uint64_t z = (uint64_t)(k + 1) * 0x9E3779B97F4A7C15ull + (uint64_t)i * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    return (z & 1) ? 1.0 : -1.0;
+}
+
+/* Perturbation k of coordinate c of point i: (x - org) scaled by (1 +- eps_k), eps_k = eps for
+ * even k and 4 eps for odd k (the FP32 evaluation of S errs by a few units of rounding). */
+static double perturbed(const double org[3], const double* P, int k, int64_t i, int c, double eps) {
+    const double e = (k & 1) ? 4 * eps : eps;
+    return org[c] + (P[c] - org[c]) * (1.0 + e * perturb_sign(k, 3 * i + c));
+}
+
+void orc_invert_perturbed(const orc_surface* s, const double* M, const orc_tree_node* tree,
+                          const unsigned char* built, const double* P, int64_t n, int max_iter, int K, double eps,
+                          double* uv, int* found, double* residual, int threads) {
+    double dom[4], org[3];
+    domain_of(s, dom);
+    surface_origin(s, org);
+#ifdef _OPENMP
+    if (threads <= 0) threads = omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 64) num_threads(threads) collapse(2)
+#endif
+    for (int k = 0; k < K; ++k)
+        for (int64_t i = 0; i < n; ++i) {
+            const double* Pk = P + 3 * i;
+            double Pp[3];
+            for (int c = 0; c < 3; ++c) Pp[c] = perturbed(org, Pk, k, i, c, eps);
+            double C[2];
+            int st, its;
+            double r;
+            invert_one(s, M, tree, built, Pp, max_iter, dom, C, &st, &r, NULL);
+            const int64_t o = (int64_t)k * n + i;
+            int ok = 0;
+            if (st == ORC_FOUND_UNIQUE || st == ORC_FOUND_AMBIGUOUS) {
+                /* the minimum of the true point next to the perturbed answer */
+                ok = run_trajectory(s, M, Pk, C, max_iter, 1, &its) && C[0] >= dom[0] && C[0] <= dom[1] &&
+                     C[1] >= dom[2] && C[1] <= dom[3];
+            }
+            uv[2 * o] = ok ? C[0] : NAN;
+            uv[2 * o + 1] = ok ? C[1] : NAN;
+            found[o] = ok;
+            residual[o] = ok ? dist3(surface_point(s, M, C), Pk) : NAN;
+        }
+}
+
+/* The same trajectories as invert_one computed in FP32 arithmetic (span matrices, local
+ * parameters, evaluation and the 2x2 solves rounded to float), each stopped at the FP32
+ * resolution of the parameters; every distinct FP32 minimum within 5 % of the closest then takes
+ * FP64 Newton steps to the true point's minimum, and the closest of those is the answer.  The FP32
+ * arithmetic works relative to the centre of the control net's bounding box (the span matrices
+ * of the translated surface, the point minus that centre), so its resolution follows the
+ * surface's extent rather than its distance from the origin.  A query whose FP64 answer this does
+ * not reproduce has an answer that FP32 arithmetic cannot determine: some trajectory that reaches
+ * it is chaotic at FP32 resolution. */
+
+typedef struct { float x, y, z; } f3;
+typedef struct { f3 S, Su, Sv, Suu, Suv, Svv; } f3ders;
+
+static float f3dot(f3 a, f3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+
+static f3ders eval32(const orc_surface* s, const double* M, const double org[3], float uu, float vv) {
+    const int p = s->degree_u, q = s->degree_v, k1 = p + 1, k2 = q + 1;
+    const double* ku = s->knots_u;
+    const double* kv = s->knots_v;
+    int m = orc_find_span(p, s->cp_u, ku, (double)uu);
+    int n = orc_find_span(q, s->cp_v, kv, (double)vv);
+    float iu = (float)(1.0 / (ku[m + 1] - ku[m])), iv = (float)(1.0 / (kv[n + 1] - kv[n]));
+    float u = (uu - (float)ku[m]) * iu, v = (vv - (float)kv[n]) * iv;
+    float su = (float)(ku[p + s->cp_u] - ku[0]) * iu, sv = (float)(kv[q + s->cp_v] - kv[0]) * iv;
+    const double* mid = M + orc_matrix_n_position(m, n, p, q, s->cp_u, s->cp_v, 0);
+    float U[8], dU[8], ddU[8], V[8], dV[8], ddV[8];
+    for (int a = 0; a < k1; ++a) {
+        U[a] = a == 0 ? 1.0f : U[a - 1] * u;
+        dU[a] = a == 0 ? 0.0f : (float)a * U[a - 1];
+        ddU[a] = a < 2 ? 0.0f : (float)(a * (a - 1)) * U[a - 2];
+    }
+    for (int b = 0; b < k2; ++b) {
+        V[b] = b == 0 ? 1.0f : V[b - 1] * v;
+        dV[b] = b == 0 ? 0.0f : (float)b * V[b - 1];
+        ddV[b] = b < 2 ? 0.0f : (float)(b * (b - 1)) * V[b - 2];
+    }
+    float R[4] = {0}, Ru[4] = {0}, Rv[4] = {0}, Ruu[4] = {0}, Ruv[4] = {0}, Rvv[4] = {0};
+    for (int c = 0; c < 4; ++c)
+        for (int a = 0; a < k1; ++a) {
+            float t = 0, td = 0, tdd = 0;
+            for (int b = 0; b < k2; ++b) {
+                /* coefficient of the surface translated by -org: xw - org_x w, ... */
+                double mm = mid[c * k1 * k2 + a * k2 + b];
+                float coef = (float)(c < 3 ? mm - org[c] * mid[3 * k1 * k2 + a * k2 + b] : mm);
+                t += coef * V[b];
+                td += coef * dV[b];
+                tdd += coef * ddV[b];
+            }
+            R[c] += U[a] * t;
+            Ru[c] += dU[a] * t;
+            Rv[c] += U[a] * td;
+            Ruu[c] += ddU[a] * t;
+            Ruv[c] += dU[a] * td;
+            Rvv[c] += U[a] * tdd;
+        }
+    float w = R[3], wu = Ru[3] * su, wv = Rv[3] * sv, wuu = Ruu[3] * su * su, wuv = Ruv[3] * su * sv,
+          wvv = Rvv[3] * sv * sv;
+    float S[3], Su[3], Sv[3], Suu[3], Suv[3], Svv[3];
+    for (int c = 0; c < 3; ++c) {
+        S[c] = R[c] / w;
+        Su[c] = (Ru[c] * su - S[c] * wu) / w;
+        Sv[c] = (Rv[c] * sv - S[c] * wv) / w;
+        Suu[c] = (Ruu[c] * su * su - 2 * Su[c] * wu - S[c] * wuu) / w;
+        Suv[c] = (Ruv[c] * su * sv - Su[c] * wv - Sv[c] * wu - S[c] * wuv) / w;
+        Svv[c] = (Rvv[c] * sv * sv - 2 * Sv[c] * wv - S[c] * wvv) / w;
+    }
+    f3ders d = {{S[0], S[1], S[2]}, {Su[0], Su[1], Su[2]}, {Sv[0], Sv[1], Sv[2]},
+                {Suu[0], Suu[1], Suu[2]}, {Suv[0], Suv[1], Suv[2]}, {Svv[0], Svv[1], Svv[2]}};
+    return d;
+}
+
+/* One FP32 trajectory (the FP64 schedule's rules, stopped at FP32 resolution; steps that do not
+ * shrink end it only where the Newton Hessian is positive definite).  Returns 1 when it
+ * converged; dist2 = |S - P|^2 at its last evaluation. */
+static int trajectory32(const orc_surface* s, const double* M, const double org[3], const float P[3], float C[2],
+                        const double dom[4], int max_iter, float* dist2) {
+    const float eu = (float)(dom[1] - dom[0]), ev = (float)(dom[3] - dom[2]);
+    const float far[4] = {(float)dom[0] - 2 * eu, (float)dom[1] + 2 * eu, (float)dom[2] - 2 * ev,
+                          (float)dom[3] + 2 * ev};
+    int newton = 0;
+    float prev = INFINITY;
+    for (int it = 0; it < max_iter; ++it) {
+        f3ders d = eval32(s, M, org, C[0], C[1]);
+        f3 r = {d.S.x - P[0], d.S.y - P[1], d.S.z - P[2]};
+        float h00 = f3dot(d.Su, d.Su), h01 = f3dot(d.Su, d.Sv), h11 = f3dot(d.Sv, d.Sv);
+        float g0 = f3dot(d.Su, r), g1 = f3dot(d.Sv, r);
+        int pd = 0;
+        if (newton) {
+            float n00 = h00 + f3dot(r, d.Suu), n01 = h01 + f3dot(r, d.Suv), n11 = h11 + f3dot(r, d.Svv);
+            if (n00 > 0 && n00 * n11 - n01 * n01 > 0) { h00 = n00; h01 = n01; h11 = n11; pd = 1; }
+        }
+        float det = h00 * h11 - h01 * h01;
+        if (!(det > 0)) return 0;
+        float du = (h11 * g0 - h01 * g1) / det, dv = (h00 * g1 - h01 * g0) / det;
+        if (!(isfinite(du) && isfinite(dv))) return 0;
+        C[0] -= du;
+        C[1] -= dv;
+        float step = fmaxf(fabsf(du), fabsf(dv));
+        *dist2 = f3dot(r, r);
+        float smag = fmaxf(fmaxf(fabsf(d.S.x), fabsf(d.S.y)), fmaxf(fabsf(d.S.z), 1.0f));
+        float tmin2 = fminf(f3dot(d.Su, d.Su), f3dot(d.Sv, d.Sv));
+        float fl = 8.0f * 5.96e-8f * smag;
+        if (step <= 3e-7f || step * step * tmin2 <= fl * fl) return 1;
+        if (pd && step < 1e-4f && step > 0.5f * prev) return 1;
+        prev = step;
+        newton = step < (float)ORC_NEWTON_SWITCH;
+        if (!(C[0] >= far[0] && C[0] <= far[1] && C[1] >= far[2] && C[1] <= far[3])) return 0;
+    }
+    return 0;
+}
+
+void orc_invert_fp32_explore(const orc_surface* s, const double* M, const orc_tree_node* tree,
+                             const unsigned char* built, const double* P, int64_t n, int max_iter, int pk,
+                             double eps, double* uv, int* found, double* residual, int threads) {
+    double dom[4], org[3];
+    domain_of(s, dom);
+    surface_origin(s, org);
+    const double cell_u = 1e-4 * (dom[1] - dom[0]), cell_v = 1e-4 * (dom[3] - dom[2]);
 #ifdef _OPENMP
     if (threads <= 0) threads = omp_get_max_threads();
 #pragma omp parallel for schedule(dynamic, 64) num_threads(threads)
 #endif
     for (int64_t k = 0; k < n; ++k) {
         const double* Pk = P + 3 * k;
+        float Pf[3];
+        for (int c = 0; c < 3; ++c) Pf[c] = (float)((pk < 0 ? Pk[c] : perturbed(org, Pk, pk, k, c, eps)) - org[c]);
         int list[ORC_TREE_NODES];
         int nc = orc_candidates(tree, built, Pk, list);
-        double best_uv[2] = {NAN, NAN}, best_r = INFINITY;
-        double sol_uv[ORC_TREE_NODES][2], sol_r[ORC_TREE_NODES];
-        int nsol = 0, total = 0;
+        float mu[ORC_TREE_NODES], mv[ORC_TREE_NODES], md[ORC_TREE_NODES];
+        long mcu[ORC_TREE_NODES], mcv[ORC_TREE_NODES];
+        int nm = 0;
         for (int c = 0; c < nc; ++c) {
             const orc_tree_node* T = &tree[list[c]];
-            /* seed = uv-centre of the node (kernel.cu:154) */
-            double C[2] = {(T->uv_lb[0] + T->uv_rt[0]) / 2, (T->uv_lb[1] + T->uv_rt[1]) / 2};
-            int converged = 0;
-            for (int it = 0; it < max_iter; ++it) {
-                d3 S;
-                double step[2];
-                gn_step(s, M, C, Pk, &S, step);
-                ++total;
-                if (!(isfinite(step[0]) && isfinite(step[1]))) break;
-                C[0] = C[0] - step[0];
-                C[1] = C[1] - step[1];
-                if (fabs(step[0]) < 1e-15 && fabs(step[1]) < 1e-15) { converged = 1; break; }
-                if (it == max_iter - 1 && fabs(step[0]) <= 1e-12 && fabs(step[1]) <= 1e-12) converged = 1;
-            }
-            if (!converged) continue;
-            if (!(C[0] >= u0 && C[0] <= u1 && C[1] >= v0 && C[1] <= v1)) continue;
+            float C[2] = {(float)((T->uv_lb[0] + T->uv_rt[0]) / 2), (float)((T->uv_lb[1] + T->uv_rt[1]) / 2)};
+            float d2 = 0;
+            if (!trajectory32(s, M, org, Pf, C, dom, max_iter, &d2)) continue;
+            if (!(C[0] >= (float)dom[0] - 1e-4f && C[0] <= (float)dom[1] + 1e-4f && C[1] >= (float)dom[2] - 1e-4f &&
+                  C[1] <= (float)dom[3] + 1e-4f))
+                continue;
+            long cu = (long)floor((C[0] - dom[0]) / cell_u), cv = (long)floor((C[1] - dom[2]) / cell_v);
+            int f = -1;
+            for (int t = 0; t < nm; ++t)
+                if (mcu[t] == cu && mcv[t] == cv) f = t;
+            if (f < 0) { f = nm++; mcu[f] = cu; mcv[f] = cv; md[f] = INFINITY; }
+            if (d2 < md[f]) { md[f] = d2; mu[f] = C[0]; mv[f] = C[1]; }
+        }
+        float dbest = INFINITY;
+        for (int t = 0; t < nm; ++t) dbest = fminf(dbest, md[t]);
+        double bu = NAN, bv = NAN, br = INFINITY;
+        for (int t = 0; t < nm; ++t) {
+            if (!(sqrtf(md[t]) <= sqrtf(dbest) * 1.05f + 1e-5f)) continue;
+            double C[2] = {mu[t], mv[t]};
+            int its;
+            if (!run_trajectory(s, M, Pk, C, max_iter, 1, &its)) continue;
+            if (!(C[0] >= dom[0] && C[0] <= dom[1] && C[1] >= dom[2] && C[1] <= dom[3])) continue;
             double r = dist3(surface_point(s, M, C), Pk);
-            sol_uv[nsol][0] = C[0];
-            sol_uv[nsol][1] = C[1];
-            sol_r[nsol] = r;
-            ++nsol;
-            if (r < best_r) { best_r = r; best_uv[0] = C[0]; best_uv[1] = C[1]; }
+            if (r < br) { br = r; bu = C[0]; bv = C[1]; }
         }
-        int st;
-        if (nc == 0) st = ORC_NO_CANDIDATE;
-        else if (nsol == 0) st = ORC_NOT_CONVERGED;
-        else {
-            st = ORC_FOUND_UNIQUE;
-            for (int t = 0; t < nsol; ++t) {
-                int same = fabs(sol_uv[t][0] - best_uv[0]) <= 1e-7 && fabs(sol_uv[t][1] - best_uv[1]) <= 1e-7;
-                if (!same && sol_r[t] <= best_r * (1 + 1e-6) + 1e-12) st = ORC_FOUND_AMBIGUOUS;
-            }
-        }
-        uv[2 * k] = best_uv[0];
-        uv[2 * k + 1] = best_uv[1];
-        status[k] = st;
-        residual[k] = nsol ? best_r : NAN;
-        if (iters) iters[k] = total;
+        found[k] = isfinite(br);
+        uv[2 * k] = bu;
+        uv[2 * k + 1] = bv;
+        residual[k] = isfinite(br) ? br : NAN;
     }
 }

@@ -89,13 +89,36 @@ int orc_candidates(const orc_tree_node* tree, const unsigned char* built, const 
 #define ORC_NO_CANDIDATE    2
 #define ORC_NOT_CONVERGED   3
 
-/* Converged Gauss-Newton inversion: the reference GN update (kernel.cu:151-249) run from
- * the uv-centre of every candidate node until the step is below 1e-15 or max_iter
- * iterations; results inside the knot domain are kept and the one of least distance is
- * returned.  uv[2n], status[n], residual[n], iters[n] (total GN steps; may be NULL). */
+/* Converged inversion (the oracle's definition, nurbs_oracle.c): from the uv-centre of every
+ * candidate node, the reference GN update (kernel.cu:151-249) while the last step was >= 1e-2
+ * in max-norm, then Newton steps (the GN update where the Hessian is not positive definite)
+ * until a Newton step is <= 1e-10 or any step <= 1e-14, at most max_iter iterations; results
+ * inside the knot domain are kept and the one of least distance is returned.  uv[2n],
+ * status[n], residual[n], iters[n] (total iterations; may be NULL). */
 void orc_invert(const orc_surface* s, const double* matrix_n, const orc_tree_node* tree,
                 const unsigned char* built, const double* P, int64_t n, int max_iter,
                 double* uv, int* status, double* residual, int* iters, int threads);
+
+/* Stability of the answer at FP32 resolution: for k in [0,K) every coordinate of P, taken
+ * relative to the centre of the control net's bounding box, is scaled by (1 +- eps) (even k) or
+ * (1 +- 4 eps) (odd k) with signs from a fixed hash; the perturbed point is inverted as
+ * orc_invert does, and its answer is carried back to the true point by Newton steps.  Outputs
+ * are K*n long (perturbation-major): uv[2Kn], found[Kn] (1 when the perturbed point had an
+ * answer whose Newton polish converged in the domain), residual[Kn] at the true point. */
+void orc_invert_perturbed(const orc_surface* s, const double* matrix_n, const orc_tree_node* tree,
+                          const unsigned char* built, const double* P, int64_t n, int max_iter, int K,
+                          double eps, double* uv, int* found, double* residual, int threads);
+
+/* The same inversion with its exploration in FP32 arithmetic (nurbs_oracle.c): every
+ * trajectory computed in float relative to the control net's centre and stopped at FP32
+ * resolution, the distinct FP32 minima within 5 % of the closest carried to the true point's
+ * minimum by FP64 Newton steps.  pk >= 0: the FP32 phase explores perturbation pk (as
+ * orc_invert_perturbed makes it) of each point; pk < 0: the point itself.  uv[2n], found[n],
+ * residual[n]; a query whose FP64 answer differs from this one has an answer that FP32
+ * arithmetic cannot determine. */
+void orc_invert_fp32_explore(const orc_surface* s, const double* matrix_n, const orc_tree_node* tree,
+                             const unsigned char* built, const double* P, int64_t n, int max_iter, int pk,
+                             double eps, double* uv, int* found, double* residual, int threads);
 
 /* The reference's GaussNewton exactly as shipped (kernel.cu:151-249): <= 10 steps,
  * success when |S-P| < max_edge before a step.  Returns 1 on success and writes uv. */

@@ -11,6 +11,8 @@ Inversion, per query, by the oracle's status:
   FOUND_AMBIGUOUS  pass if the GPU residual is no worse (same bound);
   NO_CANDIDATE     the GPU must report NO_CANDIDATE too (candidate sets are bit-exact);
   NOT_CONVERGED    no requirement (counted).
+With the oracle's answers at FP32 resolution, FOUND_UNIQUE queries whose answer changes under
+them are UNSTABLE (see classify_inversion).
 """
 import numpy as np
 
@@ -32,10 +34,26 @@ def eval_errors(ev, ref):
     return out
 
 
-def classify_inversion(uv, st, res, ouv, ost, ores, P, res_abs=1e-14):
+def stable_mask(ouv, ost, perturbed):
+    """FOUND_UNIQUE queries whose answer the oracle also gives for every perturbed copy of the
+    point (oracle.OracleSurface.stability_set), to UV_TOL after carrying it back to P."""
+    ouv = np.asarray(ouv).reshape(-1, 2)
+    puv, pfound, _ = perturbed
+    same = np.all(pfound & (np.abs(puv - ouv[None]).max(2) <= UV_TOL), axis=0)
+    return (ost == 0) & same
+
+
+def classify_inversion(uv, st, res, ouv, ost, ores, P, res_abs=1e-14, perturbed=None):
     """res_abs: absolute residual slack per unit of max(1, |P|_inf); 1e-14 unless the surface's
     FP64 evaluation itself is less accurate than that (high degrees), in which case the caller
-    passes the measured relative difference of S between the two evaluations."""
+    passes the measured relative difference of S between the two evaluations.
+
+    perturbed: the oracle's answers at FP32 resolution (OracleSurface.stability_set).  With it,
+    FOUND_UNIQUE queries whose answer changes under some of them are UNSTABLE: the oracle itself
+    gives different minima for points, or for arithmetic, that FP32 cannot tell apart.  An
+    UNSTABLE query passes when the result is found and no farther than the farthest of those
+    answers (or when one of them had no answer and none was found); FOUND_UNIQUE queries that are
+    stable keep the strict requirement."""
     uv = np.asarray(uv).reshape(-1, 2)
     ouv = np.asarray(ouv).reshape(-1, 2)
     scale = np.maximum(np.abs(np.asarray(P).reshape(-1, 3)).max(1), 1.0)
@@ -44,6 +62,16 @@ def classify_inversion(uv, st, res, ouv, ost, ores, P, res_abs=1e-14):
     same = found & (np.abs(uv - ouv).max(1) <= UV_TOL) & no_worse
     closer = found & (res < ores - 1e-12)
     uniq = ost == 0
+    unstable = np.zeros(len(st), bool)
+    fail_us = np.zeros(len(st), bool)
+    if perturbed is not None:
+        unstable = uniq & ~stable_mask(ouv, ost, perturbed)
+        _, pfound, pres = perturbed
+        worst = np.maximum(ores, np.where(pfound, pres, -np.inf).max(0))
+        some_none = ~np.all(pfound, axis=0)
+        ok_us = (found & (res <= worst * (1 + 1e-12) + res_abs * scale)) | (some_none & (st == 3))
+        fail_us = unstable & ~ok_us
+        uniq = uniq & ~unstable
     amb = ost == 1
     nocand = ost == 2
     nconv = ost == 3
@@ -51,10 +79,32 @@ def classify_inversion(uv, st, res, ouv, ost, ores, P, res_abs=1e-14):
     fail_a = amb & ~(found & no_worse)
     fail_nc = nocand & (st != 2)
     return dict(n=len(st), unique=int(uniq.sum()), same=int((uniq & same).sum()), closer=int((uniq & closer & ~same).sum()),
-                fail_unique=int(fail_u.sum()), ambiguous=int(amb.sum()), fail_ambiguous=int(fail_a.sum()),
+                fail_unique=int(fail_u.sum()), unstable=int(unstable.sum()),
+                unstable_same=int((unstable & same).sum()), fail_unstable=int(fail_us.sum()),
+                ambiguous=int(amb.sum()), fail_ambiguous=int(fail_a.sum()),
                 no_candidate=int(nocand.sum()), fail_no_candidate=int(fail_nc.sum()),
                 oracle_not_converged=int(nconv.sum()), gpu_found_where_oracle_not=int((nconv & found).sum()),
                 max_uv_err_same=float(np.abs(uv - ouv).max(1)[uniq & same].max()) if (uniq & same).any() else 0.0,
                 p99_uv_err_same=float(np.percentile(np.abs(uv - ouv).max(1)[uniq & same], 99))
                 if (uniq & same).any() else 0.0,
-                fail_idx=np.nonzero(fail_u | fail_a | fail_nc)[0])
+                fail_idx=np.nonzero(fail_u | fail_a | fail_nc | fail_us)[0])
+
+
+# UNSTABLE queries are counted, not excused wholesale: a test fails when more than this fraction
+# of its queries is UNSTABLE (the 64x64 workload has ~0.3 %).
+MAX_UNSTABLE_FRAC = 0.01
+
+
+def oracle_parity(o, P, uv, st, res, res_abs=1e-14):
+    """Classifies a GPU inversion against the oracle surface `o`, with the oracle's answers at
+    FP32 resolution (OracleSurface.stability_set) deciding which FOUND_UNIQUE queries are
+    UNSTABLE."""
+    ouv, ost, ores, _ = o.invert(P)
+    return classify_inversion(uv, st, res, ouv, ost, ores, P, res_abs=res_abs, perturbed=o.stability_set(P))
+
+
+def assert_exact(c, what=""):
+    """No failure in any class, and UNSTABLE queries within MAX_UNSTABLE_FRAC."""
+    fails = {k: c[k] for k in ("fail_unique", "fail_unstable", "fail_ambiguous", "fail_no_candidate")}
+    assert not any(fails.values()), (what, c)
+    assert c["unstable"] <= MAX_UNSTABLE_FRAC * c["n"], (what, c)

@@ -13,7 +13,7 @@ import pytest
 
 import oracle as O
 from conftest import golden_files, load_golden, GOLDEN
-from parity import eval_errors
+from parity import classify_inversion, eval_errors, stable_mask
 
 MODEL_FILES = [f for f in golden_files() if os.path.basename(f).startswith(("model_", "synth_"))]
 
@@ -123,3 +123,78 @@ def test_oracle_high_degree_eval_against_40_digit_values():
         sf.update({k: int(z[tag + k]) for k in ("p", "q", "nu", "nv")})
         errs = eval_errors(O.OracleSurface(sf).eval(z[tag + "uv"], 63), z[tag + "truth"])
         assert max(errs) < 1e-9, (tag, errs)
+
+
+def _large_sample(n, seed=21):
+    from gpu_nurbs_gb300 import synth
+    surf = synth.surface_large()
+    o = O.OracleSurface(surf)
+    uv, off = synth.query_params(n, seed, "large")
+    E = o.eval(uv, 7)
+    return o, synth.form_queries(E[0:3].T, E[3:6].T, E[6:9].T, off)
+
+
+def test_oracle_answers_are_local_minima():
+    """The oracle's definition (GN update, then Newton steps once the step is below 1e-2) pins
+    nearly every query of the 64x64 workload, and every answer is a minimum of the distance:
+    the gradient J^T r vanishes to rounding and the Hessian J^T J + r.d2S is positive definite."""
+    o, P = _large_sample(2048)
+    uv, st, res, _ = o.invert(P)
+    found = st <= 1
+    assert (st == O.NOT_CONVERGED).mean() < 0.005
+    E = o.eval(uv[found], 63)
+    S, Su, Sv, Suu, Suv, Svv = (E[3 * b:3 * b + 3].T for b in range(6))
+    r = S - P[found]
+    g = np.stack([(Su * r).sum(1), (Sv * r).sum(1)], 1)
+    scale = np.linalg.norm(r, axis=1) * np.maximum(np.linalg.norm(Su, axis=1), np.linalg.norm(Sv, axis=1))
+    assert np.all(np.abs(g).max(1) <= 1e-9 * np.maximum(scale, 1e-300) + 1e-15)
+    h00 = (Su * Su).sum(1) + (r * Suu).sum(1)
+    h01 = (Su * Sv).sum(1) + (r * Suv).sum(1)
+    h11 = (Sv * Sv).sum(1) + (r * Svv).sum(1)
+    assert np.all(h00 > 0) and np.all(h00 * h11 - h01 * h01 > 0)
+    assert np.allclose(res[found], np.linalg.norm(r, axis=1), rtol=1e-12, atol=1e-15)
+
+
+def test_oracle_stability_set_on_a_well_conditioned_surface():
+    """On the 8x8 surface with 1e-3 offsets the FP64 answer survives every FP32-resolution
+    perturbation and the FP32 exploration: no query is UNSTABLE."""
+    from gpu_nurbs_gb300 import synth
+    surf = synth.surface_small()
+    o = O.OracleSurface(surf)
+    uv, off = synth.query_params(2000, 12, "small")
+    E = o.eval(uv, 7)
+    P = synth.form_queries(E[0:3].T, E[3:6].T, E[6:9].T, off)
+    ouv, ost, ores, _ = o.invert(P)
+    pset = o.stability_set(P)
+    assert pset[0].shape == (2 * O.PERTURB_K + 1, len(P), 2)
+    uniq = ost == O.FOUND_UNIQUE
+    assert np.array_equal(stable_mask(ouv, ost, pset), uniq)
+    fu, ff, fr = o.invert_fp32_explore(P)
+    assert np.abs(fu[uniq] - ouv[uniq]).max() <= 1e-12
+
+
+def test_parity_classifier_catches_planted_mistakes():
+    """A wrong minimum on a stable query fails; on an UNSTABLE query a result no worse than the
+    oracle's farthest answer passes and a farther one fails; a missing answer fails."""
+    o, P = _large_sample(3000, seed=22)
+    ouv, ost, ores, _ = o.invert(P)
+    pset = o.stability_set(P)
+    stable = stable_mask(ouv, ost, pset)
+    unstable = (ost == O.FOUND_UNIQUE) & ~stable
+    assert unstable.sum() >= 1 and unstable.mean() < 0.01
+    uv, st, res = ouv.copy(), ost.copy(), ores.copy()
+    c = classify_inversion(uv, st, res, ouv, ost, ores, P, perturbed=pset)
+    assert c["fail_unique"] == c["fail_unstable"] == 0 and c["unstable"] == unstable.sum()
+    i = int(np.nonzero(stable)[0][0])
+    uv[i] += 1e-8                       # another point of the same minimum's neighbourhood
+    res[i] *= 1 + 1e-9
+    st[int(np.nonzero(stable)[0][1])] = O.NOT_CONVERGED
+    j = int(np.nonzero(unstable)[0][0])
+    worst = np.nanmax(np.where(pset[1][:, j], pset[2][:, j], -np.inf))
+    uv[j] = [0.123, 0.456]
+    res[j] = max(worst, ores[j]) * 1.01  # farther than every answer the oracle gives
+    c = classify_inversion(uv, st, res, ouv, ost, ores, P, perturbed=pset)
+    assert c["fail_unique"] == 2 and c["fail_unstable"] == 1
+    res[j] = max(worst, ores[j])         # as far as the farthest: passes
+    c = classify_inversion(uv, st, res, ouv, ost, ores, P, perturbed=pset)
+    assert c["fail_unstable"] == 0
