@@ -17,9 +17,11 @@ constexpr int kModeMixed = 1;
 constexpr int kWarps = 4;          // warps per CTA
 constexpr int kThreads = 32 * kWarps;
 constexpr int kMinBlocksMixed = 6;  // CTAs per SM the mixed kernels are register-budgeted for (80 registers)
-constexpr int kMaxIter32 = 24;     // FP32 iterations per seed
+constexpr int kMaxIter32 = 40;     // FP32 iterations per seed (the FP64 cap: the oracle's too)
 constexpr int kMaxIter64 = 40;     // FP64-mode iterations per seed
-constexpr int kMaxFinal64 = 6;     // MIXED: FP64 steps (2 normally)
+constexpr int kMaxFinal64 = 24;    // MIXED: FP64 steps (2 normally)
+constexpr int kFinal32Curv = 3;    // MIXED: FP64 steps with the FP32 curvature term before the FP64 one
+constexpr float kPolishMargin = 0.05f;  // MIXED: a runner-up this close to the best also takes the FP64 steps
 constexpr double kNewtonSwitch = 1e-2;  // GN while the step is larger, Newton below
 constexpr float kTol32 = 3e-7f;
 constexpr double kTolNewton64 = 1e-10;  // a Newton step this small leaves < 1e-19 error
@@ -49,29 +51,32 @@ __device__ __forceinline__ T det2(T h00, T h01, T h11) {
   return fast::mad(h00, h11, -(h01 * h01));
 }
 
-// One (Gauss-)Newton step from the derivatives at C.  Returns false when the system is
-// singular.  Newton uses H = J^T J + r.d2S when that H is positive definite, else the
-// Gauss-Newton matrix J^T J (the reference's update, kernel.cu:195-243).  FAST: FP32
-// reciprocal by the hardware approximation.
+// One (Gauss-)Newton step from the derivatives at C.  Newton uses H = J^T J + r.d2S when that
+// H is positive definite, else the Gauss-Newton matrix J^T J (the reference's update,
+// kernel.cu:195-243).  Returns kSingular when the system is singular, kStepGN or kStepNewton
+// for the matrix it used.  FAST: FP32 reciprocal by the hardware approximation.
+enum StepKind { kSingular = 0, kStepGN = 1, kStepNewton = 2 };
 template <typename T, typename TH, bool FAST>
-__device__ __forceinline__ bool solve_step(const v3<T>& r, const v3<T>& Su, const v3<T>& Sv, const v3<TH>& Suu,
-                                           const v3<TH>& Suv, const v3<TH>& Svv, bool newton, T& du, T& dv) {
+__device__ __forceinline__ int solve_step(const v3<T>& r, const v3<T>& Su, const v3<T>& Sv, const v3<TH>& Suu,
+                                          const v3<TH>& Suv, const v3<TH>& Svv, bool newton, T& du, T& dv) {
   T h00 = dot3(Su, Su), h01 = dot3(Su, Sv), h11 = dot3(Sv, Sv);
   const T g0 = dot3(Su, r), g1 = dot3(Sv, r);
+  int kind = kStepGN;
   if (newton) {
     const T n00 = h00 + dot3c(r, Suu), n01 = h01 + dot3c(r, Suv), n11 = h11 + dot3c(r, Svv);
     if (n00 > T(0) && det2(n00, n01, n11) > T(0)) {
       h00 = n00;
       h01 = n01;
       h11 = n11;
+      kind = kStepNewton;
     }
   }
   const T det = det2(h00, h01, h11);
-  if (!(det > T(0))) return false;
+  if (!(det > T(0))) return kSingular;
   const T inv = fast::rcp<FAST>(det);
   du = fast::mad(h11, g0, -(h01 * g1)) * inv;
   dv = fast::mad(h00, g1, -(h01 * g0)) * inv;
-  return true;
+  return kind;
 }
 
 // Where one kernel finds the span tables: breakpoints in shared memory when they fit.
@@ -95,24 +100,29 @@ struct Seed {
 enum StepResult { kContinue = 0, kConverged = 1, kFailed = 2 };
 
 // One FP32 iteration of a seed.  Convergence: the step is at the FP32 resolution of the
-// parameters (rounding of S mapped through the shorter tangent: step * |S_t|min <= 8 ulp(|S|)),
-// or Newton steps stop shrinking.  dist2 = |S - P|^2 before the step.
+// parameters (the change of S it makes, |Su du + Sv dv|, is within 8 ulp(|S|)), or Newton steps
+// (with a positive definite Hessian) stop shrinking.  Where the Hessian is not
+// positive definite the iterate is near a saddle of the distance, from which the GN steps creep
+// away slowly: steps that do not shrink there are no sign of convergence.  dist2 = |S - P|^2
+// before the step.
 template <int P, int Q>
 __device__ __forceinline__ int iterate32(const Ctx& c, float px, float py, float pz, Seed<float>& st, float& dist2) {
   fast::SDer<float> d = fast::eval_at<float, P, Q, 2, true>(c.L32, c.m32, c.p, c.q, st.u, st.v, st.hu, st.hv);
   v3<float> r = {d.S.x - px, d.S.y - py, d.S.z - pz};
   float du, dv;
-  if (!solve_step<float, float, true>(r, d.Su, d.Sv, d.Suu, d.Suv, d.Svv, st.newton, du, dv)) return kFailed;
+  const int kind = solve_step<float, float, true>(r, d.Su, d.Sv, d.Suu, d.Suv, d.Svv, st.newton, du, dv);
+  if (kind == kSingular) return kFailed;
   if (!(isfinite(du) && isfinite(dv))) return kFailed;
   st.u -= du;
   st.v -= dv;
   float step = fmaxf(fabsf(du), fabsf(dv));
   dist2 = dot3(r, r);
   float smag = fmaxf(fmaxf(fabsf(d.S.x), fabsf(d.S.y)), fmaxf(fabsf(d.S.z), 1.0f));
-  float tmin2 = fminf(dot3(d.Su, d.Su), dot3(d.Sv, d.Sv));
+  const v3<float> dS = {fast::mad(d.Sv.x, dv, d.Su.x * du), fast::mad(d.Sv.y, dv, d.Su.y * du),
+                        fast::mad(d.Sv.z, dv, d.Su.z * du)};
   float fl = 8.0f * 5.96e-8f * smag;
-  if (step <= kTol32 || step * step * tmin2 <= fl * fl) return kConverged;
-  if (st.newton && step < 1e-4f && step > 0.5f * st.prev) return kConverged;
+  if (step <= kTol32 || dot3(dS, dS) <= fl * fl) return kConverged;
+  if (kind == kStepNewton && step < 1e-4f && step > 0.5f * st.prev) return kConverged;
   st.prev = step;
   st.newton = step < (float)kNewtonSwitch;
   if (++st.it >= kMaxIter32) return kFailed;
@@ -147,7 +157,11 @@ __device__ __forceinline__ bool finish64(const Ctx& c, double px, double py, dou
   return (u >= c.dom_u0 && u <= c.dom_u1 && v >= c.dom_v0 && v <= c.dom_v1) && isfinite(res);
 }
 
-// MIXED: the final FP64 Newton steps from an FP32 minimum, then the residual.
+// MIXED: the final FP64 Newton steps from an FP32 minimum, then the residual.  The first
+// kFinal32Curv steps take the Hessian's curvature term from FP32 second derivatives (it only
+// sets the rate of convergence, and two steps normally reach the tolerance); later steps take
+// it in FP64, which converges where the minimum is nearly degenerate (a flat valley, where the
+// FP32 term's error is comparable to the Hessian's smallest eigenvalue).
 template <int P, int Q>
 __device__ bool final64(const Ctx& c, double px, double py, double pz, double& u, double& v, double& res) {
   // span hints from the FP32 tables (shared memory when staged): the FP64 search then only
@@ -156,11 +170,21 @@ __device__ bool final64(const Ctx& c, double px, double py, double pz, double& u
   int hv = fast::find_seg_hint(c.L32.bv, c.L32.ns_v, (float)v, 0);
   int hu32 = hu, hv32 = hv;
   for (int it = 0; it < kMaxFinal64; ++it) {
-    fast::SDer<double> d = fast::eval_at<double, P, Q, 1>(c.L64, c.m64, c.p, c.q, u, v, hu, hv);
-    fast::SDer<float> e = fast::eval_at<float, P, Q, 2, true>(c.L32, c.m32, c.p, c.q, (float)u, (float)v, hu32, hv32);
-    v3<double> r = {d.S.x - px, d.S.y - py, d.S.z - pz};
+    fast::SDer<double> d;
     double du, dv;
-    if (!solve_step<double, float, false>(r, d.Su, d.Sv, e.Suu, e.Suv, e.Svv, true, du, dv)) return false;
+    int kind;
+    v3<double> r;
+    if (it < kFinal32Curv) {
+      d = fast::eval_at<double, P, Q, 1>(c.L64, c.m64, c.p, c.q, u, v, hu, hv);
+      fast::SDer<float> e = fast::eval_at<float, P, Q, 2, true>(c.L32, c.m32, c.p, c.q, (float)u, (float)v, hu32, hv32);
+      r = {d.S.x - px, d.S.y - py, d.S.z - pz};
+      kind = solve_step<double, float, false>(r, d.Su, d.Sv, e.Suu, e.Suv, e.Svv, true, du, dv);
+    } else {
+      d = fast::eval_at<double, P, Q, 2>(c.L64, c.m64, c.p, c.q, u, v, hu, hv);
+      r = {d.S.x - px, d.S.y - py, d.S.z - pz};
+      kind = solve_step<double, double, false>(r, d.Su, d.Sv, d.Suu, d.Suv, d.Svv, true, du, dv);
+    }
+    if (kind == kSingular) return false;
     if (!(isfinite(du) && isfinite(dv))) return false;
     u -= du;
     v -= dv;
@@ -200,6 +224,7 @@ __device__ __forceinline__ int select_bit(uint64_t m, int k) {
 struct Rec32 {  // per-query FP32 record: best and best distinct runner-up (squared distances)
   float u1, v1, d1, u2, v2, d2;
   int cu1, cv1;  // grid cell of the best
+  float ue, ve, de;  // the closest FP32 minimum just outside the domain (edge record)
 };
 
 // Total order on results (distance, then u, then v): the minimum of a set does not depend on
@@ -296,7 +321,9 @@ struct Staged {
   const TreeNodeDev* tree;     // exact FP64 boxes, read only near a face (global memory, L2)
   double ctr[kTreeNodes][2];
   float ctr32[kTreeNodes][2];
+  double org[3];    // origin of the FP32 tables: FP32 iterations see P - org
   float dom32[4];
+  float near32[4];  // 1 % of the extent around the domain: FP32 minima here are edge records
   float far32[4];  // two domain extents around the domain: an FP32 iterate beyond is abandoned
   Cells<float> cell32;
   Cells<double> cell64;
@@ -377,12 +404,19 @@ __device__ __forceinline__ void stage_surface(const SurfDev& s, Staged<KS, MODE>
   if (tid == 0) {
     sm.nb = nb;
     sm.tree = s.tree;
+    sm.org[0] = s.org[0];
+    sm.org[1] = s.org[1];
+    sm.org[2] = s.org[2];
     const float slack = 1e-4f;  // FP32 domain test is a prefilter; the FP64 phase decides
     sm.dom32[0] = (float)s.dom_u0 - slack;
     sm.dom32[1] = (float)s.dom_u1 + slack;
     sm.dom32[2] = (float)s.dom_v0 - slack;
     sm.dom32[3] = (float)s.dom_v1 + slack;
     const float fu = 2.0f * (float)(s.dom_u1 - s.dom_u0), fv = 2.0f * (float)(s.dom_v1 - s.dom_v0);
+    sm.near32[0] = (float)s.dom_u0 - 5e-3f * fu;
+    sm.near32[1] = (float)s.dom_u1 + 5e-3f * fu;
+    sm.near32[2] = (float)s.dom_v0 - 5e-3f * fv;
+    sm.near32[3] = (float)s.dom_v1 + 5e-3f * fv;
     sm.far32[0] = (float)s.dom_u0 - fu;
     sm.far32[1] = (float)s.dom_u1 + fu;
     sm.far32[2] = (float)s.dom_v0 - fv;
@@ -459,9 +493,10 @@ __device__ __forceinline__ void invert_chunk(Staged<KS, MODE>& sm, WarpWork<MODE
       }
       ww.slpref[lane] = incl - cnt;
     }
-    ww.sp32[lane][0] = fx;
-    ww.sp32[lane][1] = fy;
-    ww.sp32[lane][2] = fz;
+    // the FP32 iterations work relative to the FP32 tables' origin
+    ww.sp32[lane][0] = (float)(px - sm.org[0]);
+    ww.sp32[lane][1] = (float)(py - sm.org[1]);
+    ww.sp32[lane][2] = (float)(pz - sm.org[2]);
     if constexpr (MODE != kModeMixed) {
       ww.sp64[lane][0] = px;
       ww.sp64[lane][1] = py;
@@ -473,7 +508,8 @@ __device__ __forceinline__ void invert_chunk(Staged<KS, MODE>& sm, WarpWork<MODE
       Rec32& R = ww.rec[lane];
       R.d1 = INFINITY;
       R.d2 = INFINITY;
-      R.u1 = R.v1 = R.u2 = R.v2 = 0.f;
+      R.de = INFINITY;
+      R.u1 = R.v1 = R.u2 = R.v2 = R.ue = R.ve = 0.f;
       R.cu1 = R.cv1 = 0;
     } else {
       ww.rec[lane].n = 0;
@@ -554,6 +590,11 @@ __device__ __forceinline__ void invert_chunk(Staged<KS, MODE>& sm, WarpWork<MODE
         const bool done = active && res != kContinue;
         const bool keep = res == kConverged && sd.u >= sm.dom32[0] && sd.u <= sm.dom32[1] && sd.v >= sm.dom32[2] &&
                           sd.v <= sm.dom32[3];
+        // An FP32 minimum within 1 % of the extent outside the domain: near an edge FP32 arithmetic
+        // can end outside while FP64 steps from there reach a minimum inside.  The closest such
+        // result of a query is kept apart and takes the final FP64 steps too when it is close.
+        const bool edge = done && res == kConverged && !keep && sd.u >= sm.near32[0] && sd.u <= sm.near32[1] &&
+                          sd.v >= sm.near32[2] && sd.v <= sm.near32[3];
         __syncwarp();
         int cu = 0, cv = 0;
         bool upd = done && keep;
@@ -567,10 +608,15 @@ __device__ __forceinline__ void invert_chunk(Staged<KS, MODE>& sm, WarpWork<MODE
           else
             upd = before(dist, sd.u, sd.v, R.d1, R.u1, R.v1) || before(dist, sd.u, sd.v, R.d2, R.u2, R.v2);
         }
-        unsigned fm = __ballot_sync(FULL, upd);
+        const bool upe = edge && before(dist, sd.u, sd.v, ww.rec[ql].de, ww.rec[ql].ue, ww.rec[ql].ve);
+        unsigned fm = __ballot_sync(FULL, upd || upe);
         while (fm) {
           int j = __ffs(fm) - 1;
-          if (lane == j) merge32(ww.rec[ql], cu, cv, sd.u, sd.v, dist);
+          if (lane == j) {
+            Rec32& R = ww.rec[ql];
+            if (upd) merge32(R, cu, cv, sd.u, sd.v, dist);
+            else if (before(dist, sd.u, sd.v, R.de, R.ue, R.ve)) { R.ue = sd.u; R.ve = sd.v; R.de = dist; }
+          }
           __syncwarp();
           fm &= fm - 1;
         }
@@ -639,28 +685,41 @@ __device__ __forceinline__ void invert_chunk(Staged<KS, MODE>& sm, WarpWork<MODE
       px = Pq[3 * q];
       py = Pq[3 * q + 1];
       pz = Pq[3 * q + 2];
-      double us[2], vs[2], rs[2];
+      double us[3], vs[3], rs[3];
       int ns = 0;
-      const Rec32& R = ww.rec[lane];
-      if (R.d1 < INFINITY) {
-        // the runner-up also takes the FP64 steps when the best fails there, or when it is within
-        // 0.1 % of the best; one next to the best is the same minimum split by a cell boundary
-        const float e1 = sqrtf(R.d1) * 1.001f + 1e-5f;
-        const bool second = R.d2 < INFINITY && !(fabsf(R.u2 - R.u1) <= kDistinct32 && fabsf(R.v2 - R.v1) <= kDistinct32);
-        const bool tie = second && R.d2 <= e1 * e1;
-        double u = R.u1, v = R.v1, r;
-        const bool ok1 = final64<P, Q>(cx, px, py, pz, u, v, r);
-        if (ok1) { us[ns] = u; vs[ns] = v; rs[ns] = r; ++ns; }
-        if (ok1 ? tie : second) {
-          double u2 = R.u2, v2 = R.v2, r2;
-          if (final64<P, Q>(cx, px, py, pz, u2, v2, r2)) {
-            bool same = ns == 1 && fabs(u2 - us[0]) <= kDistinct && fabs(v2 - vs[0]) <= kDistinct;
-            if (same) {
-              if (r2 < rs[0]) { us[0] = u2; vs[0] = v2; rs[0] = r2; }
-            } else {
-              us[ns] = u2; vs[ns] = v2; rs[ns] = r2; ++ns;
-            }
+      // FP64 minima reached from the records; two within kDistinct are one minimum (split by a
+      // cell boundary), which keeps its smaller residual
+      auto add = [&](double u, double v, double r) {
+        for (int k = 0; k < ns; ++k)
+          if (fabs(u - us[k]) <= kDistinct && fabs(v - vs[k]) <= kDistinct) {
+            if (r < rs[k]) { us[k] = u; vs[k] = v; rs[k] = r; }
+            return;
           }
+        us[ns] = u; vs[ns] = v; rs[ns] = r; ++ns;
+      };
+      const Rec32& R = ww.rec[lane];
+      const float dbest = fminf(R.d1, R.de);
+      if (dbest < INFINITY) {
+        // the runner-up also takes the FP64 steps when the best fails there, or when it is within
+        // kPolishMargin of the best (an FP32 iterate that stopped in a flat valley overstates its
+        // minimum's distance); one next to the best is the same minimum split by a cell boundary.
+        // The edge record takes them when it is within the same margin.
+        const float e1 = sqrtf(dbest) * (1.0f + kPolishMargin) + 1e-5f;
+        if (R.d1 < INFINITY) {
+          const bool second =
+              R.d2 < INFINITY && !(fabsf(R.u2 - R.u1) <= kDistinct32 && fabsf(R.v2 - R.v1) <= kDistinct32);
+          const bool tie = second && R.d2 <= e1 * e1;
+          double u = R.u1, v = R.v1, r;
+          const bool ok1 = final64<P, Q>(cx, px, py, pz, u, v, r);
+          if (ok1) add(u, v, r);
+          if (ok1 ? tie : second) {
+            double u2 = R.u2, v2 = R.v2, r2;
+            if (final64<P, Q>(cx, px, py, pz, u2, v2, r2)) add(u2, v2, r2);
+          }
+        }
+        if (R.de <= e1 * e1) {
+          double u3 = R.ue, v3 = R.ve, r3;
+          if (final64<P, Q>(cx, px, py, pz, u3, v3, r3)) add(u3, v3, r3);
         }
       }
       status = ns == 0 ? 3 : finish_status(us, vs, rs, ns, kDistinct, kDistinct, ou, ov, orr);

@@ -118,8 +118,29 @@ __device__ void span_component(const SurfDev& s, const double* __restrict__ basi
         ref_out[pos] = acc;
       } else {
         m64[((size_t)span * k1 * k2 + a * k2 + l) * 4 + c] = acc;
-        m32[((size_t)span * span_coefs32(p, q) + a * k2 + l) * 4 + c] = (float)acc;
+        if (c == 3) m32[((size_t)span * span_coefs32(p, q) + a * k2 + l) * 4 + c] = (float)acc;
       }
+    }
+  if (ref_out || c == 3) return;
+  // FP32 table: the same span matrix for the surface translated by -org (the matrix form is
+  // linear in the weighted control points: Middle_c = (P_c - org_c) * w), computed in FP64 and
+  // rounded once
+  for (int a = 0; a <= p; ++a)
+    for (int b = 0; b <= q; ++b) {
+      size_t idx = (size_t)(a + i - p) * s.nv + (b + j - q);
+      mid[a * k2 + b] = (s.cps[3 * idx + c] - s.org[c]) * s.weights[idx];
+    }
+  for (int a = 0; a < k1; ++a)
+    for (int l = 0; l < k2; ++l) {
+      double acc = 0;
+      for (int tt = 0; tt < k2; ++tt) acc += mid[a * k2 + tt] * Nv[l * k2 + tt];
+      tmp[a * k2 + l] = acc;
+    }
+  for (int a = 0; a < k1; ++a)
+    for (int l = 0; l < k2; ++l) {
+      double acc = 0;
+      for (int ss = 0; ss < k1; ++ss) acc += Nu[a * k1 + ss] * tmp[ss * k2 + l];
+      m32[((size_t)span * span_coefs32(p, q) + a * k2 + l) * 4 + c] = (float)acc;
     }
 }
 

@@ -27,6 +27,11 @@ __global__ void __launch_bounds__(256) k_eval(SurfDev s, const T* __restrict__ u
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
     T u = uv[2 * i], v = uv[2 * i + 1];
     fast::SDer<T> d = fast::eval_point<T, P, Q, ORDER>(s, u, v);
+    if constexpr (sizeof(T) == 4) {  // FP32 tables hold the surface relative to org
+      d.S.x += s.org32[0];
+      d.S.y += s.org32[1];
+      d.S.z += s.org32[2];
+    }
     int o = 0;
     auto put = [&](const v3<T>& a) {
       st_stream(out + (int64_t)(3 * o + 0) * n + i, a.x);

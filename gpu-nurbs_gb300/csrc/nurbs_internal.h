@@ -26,7 +26,10 @@ constexpr int kPts = kGap + 1;    // PointsPerEdge
 //   knot_u[ns_u], knot_v[ns_v]       knot index m of span s (k[m] = bu[s]) for the reference layout
 //   m64[ns_u*ns_v][k1][k2][4]        span matrices, homogeneous components (xw, yw, zw, w)
 //                                    innermost, so one (a,b) coefficient is one 32-byte vector
-//   m32                              the same rounded to FP32 (16 bytes per coefficient)
+//   m32                              the same for the surface translated by -org, rounded to FP32
+//                                    (16 bytes per coefficient): FP32 evaluation works in coordinates
+//                                    relative to the control net's centre, so its resolution is set by
+//                                    the surface's extent, not by its distance from the origin
 //   tree[65]                         TreeNodeDev; divided[65], built[65]
 struct SurfDev {
   int p, q, nu, nv;
@@ -34,6 +37,8 @@ struct SurfDev {
   double range_u, range_v;   // k[last]-k[0] (derivative scale numerator, kernel.cu:167-168)
   float range_u32, range_v32;
   double dom_u0, dom_u1, dom_v0, dom_v1;  // knot domain [k[p], k[nu]] x [k[q], k[nv]]
+  double org[3];          // origin of the FP32 tables: centre of the control net's bounding box
+  float org32[3];
   const double* bu;
   const double* bv;
   const double* inv_du;

@@ -2,6 +2,7 @@
 // layout of its device block.  Shared by the single-surface handle (api.cpp) and the pool
 // (pool.cpp).
 #pragma once
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -144,6 +145,15 @@ inline void fill_surface(const SurfaceHost& S, char* img, char* in_dev, char* ou
   d.range_u32 = (float)d.range_u;
   d.range_v32 = (float)d.range_v;
   d.dom_u0 = S.ku[S.p]; d.dom_u1 = S.ku[S.nu]; d.dom_v0 = S.kv[S.q]; d.dom_v1 = S.kv[S.nv];
+  for (int c = 0; c < 3; ++c) {
+    double lo = S.cps[c], hi = S.cps[c];
+    for (size_t k = 3 + c; k < S.cps.size(); k += 3) {
+      lo = std::min(lo, S.cps[k]);
+      hi = std::max(hi, S.cps[k]);
+    }
+    d.org[c] = 0.5 * (lo + hi);
+    d.org32[c] = (float)d.org[c];
+  }
   d.bu = (const double*)(in_dev + S.o_bu); d.bv = (const double*)(in_dev + S.o_bv);
   d.inv_du = (const double*)(in_dev + S.o_idu); d.inv_dv = (const double*)(in_dev + S.o_idv);
   d.bu32 = (const float*)(in_dev + S.o_bu32); d.bv32 = (const float*)(in_dev + S.o_bv32);

