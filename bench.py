@@ -9,6 +9,13 @@ A step = one nurbs_invert launch over the whole query batch with the queries res
 host->device copy of the queries and the device->host copy of uv/status/residual are inside
 each timed step.  L2 is flushed (a 512 MB write) before every timed step.
 
+On one GPU the same line also carries sub-records of the other workloads, each with its own
+clock samples: "batched" (4096 uneven surfaces, one persistent launch from a CUDA graph, mixed vs
+FP64, oracle parity sample), "quintic" (degree 5, 256x256 net, 2^24 queries, per-query parameter
+error against the oracle), "eval_large" (2^26 evaluations of S..Svv, FP64 and FP32, with their
+rooflines) and "serving" (continuous batching over a pool of 10^4 surfaces: peak throughput,
+p50/p99 at half of peak, FP64 server at the top rate).  --headline-only leaves them out.
+
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload ...]
 
 Under torchrun (N > 1) every rank inverts its own batch of the same size (weak scaling, no
@@ -94,9 +101,9 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-# DRAM bytes (read + write) per launch of the dominant kernel, from one ncu capture each
-# (profiles/k_invert_large.md, profiles/k_eval_large.md), per unit of work so that they scale
-# to the launch size: traffic grows with the number of queries or points.
+# DRAM bytes (read + write) per launch of the dominant kernel, from one ncu capture each of the
+# same kernel on the same workload, per unit of work so that they scale to the launch size:
+# traffic grows with the number of queries or points.
 TRAFFIC_PER_UNIT = {
     "large": (33.88e6 + 16.49e6) / (1 << 20),   # mixed k_invert, bytes per query (2^20-query capture)
     "eval-large": (69.05e6 + 542.67e6) / (1 << 22),  # FP64 k_eval S..Svv, bytes per point (2^22 points)
@@ -122,6 +129,57 @@ def mean_step_ms_over_ranks(ts, world, device):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         tot = float(t.item())
     return tot / len(ts)
+
+
+def event_timer(torch, flush):
+    """Times fn over `steps` steps with CUDA events on the current stream; L2 is flushed (a
+    512 MB write) before each step."""
+    stream = torch.cuda.current_stream()
+
+    def timed(fn, steps):
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        for k in range(steps):
+            flush.fill_(float(k))
+            evs[k][0].record(stream)
+            fn()
+            evs[k][1].record(stream)
+        torch.cuda.synchronize()
+        return [e0.elapsed_time(e1) for e0, e1 in evs]
+    return timed
+
+
+def host_cores():
+    return len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
+
+
+def oracle_parity_sample(surf, P, g_uv, g_st, g_res, res_abs=1e-14):
+    """Checks a GPU inversion on a bounded sample against the oracle (the CPU-baseline leg's
+    own results), with the oracle's answers at FP32 resolution deciding which queries are
+    UNSTABLE; adds the parameter error of the matching queries (max, p99).  Returns the parity
+    record and the oracle's wall time for the plain inversion of the sample."""
+    import oracle as O
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from parity import classify_inversion
+    cores = host_cores()
+    o = O.OracleSurface(surf)
+    o.tree()
+    t0 = time.perf_counter()
+    ouv, ost, ores, _ = o.invert(P, threads=cores)
+    dt = time.perf_counter() - t0
+    c = classify_inversion(g_uv, g_st, g_res, ouv, ost, ores, P, res_abs=res_abs,
+                           perturbed=o.stability_set(P, threads=cores))
+    return {k: v for k, v in c.items() if k != "fail_idx"}, dt
+
+
+def merge_parity(tot, c):
+    for k, v in c.items():
+        if k.startswith("max_"):
+            tot[k] = max(tot.get(k, 0.0), v)
+        elif k.startswith("p99_"):
+            tot.setdefault(k + "_per_surface", []).append(v)
+        else:
+            tot[k] = tot.get(k, 0) + v
+    return tot
 
 
 def make_workload(gn, torch, name, n, seed):
@@ -180,17 +238,7 @@ def run_ours(a):
     st = torch.empty(n, dtype=torch.int32, device="cuda")
     res = torch.empty(n, dtype=torch.float64, device="cuda")
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
-    stream = torch.cuda.current_stream()
-
-    def timed(fn, steps):
-        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
-        for k in range(steps):
-            flush.fill_(float(k))
-            evs[k][0].record(stream)
-            fn()
-            evs[k][1].record(stream)
-        torch.cuda.synchronize()
-        return [e0.elapsed_time(e1) for e0, e1 in evs]
+    timed = event_timer(torch, flush)
 
     def barrier():
         torch.cuda.synchronize()
@@ -288,14 +336,52 @@ def run_ours(a):
         "clocks": clk,
         "gpu_launches": a.steps,
     }
+    work = work_counts(gn, s, Pd)
+    if work:
+        # the FP32 pipe with the work the kernel actually did: FP32 seed iterations x flops each
+        fi = flop_iter32(surf["p"], surf["q"])
+        f32 = work["seed_iterations"] * fi
+        line["roofline"]["fp32_actual"] = {
+            "fp32_iterations_per_query": work["seed_iterations"] / n,
+            "final_fp64_polishes_per_query": work["final_polishes"] / n,
+            "flop_per_fp32_iteration": fi,
+            "achieved": f32 / (ms_mixed / 1e3) / 1e12, "peak": peak32, "unit": "TFLOP/s",
+            "frac": f32 / (ms_mixed / 1e3) / 1e12 / peak32 if peak32 else None}
     if not a.no_cpu:
         line["cpu_baseline"], line["parity_sample"] = cpu_baseline(surf, P, a.cpu_sample, g_uv, g_st, res_mixed)
+    if world == 1 and not a.headline_only and a.workload == "large":
+        for name, fn in (("batched", batched_record), ("quintic", quintic_record), ("eval_large", eval_record),
+                         ("serving", serving_record)):
+            t0 = time.perf_counter()
+            try:
+                line[name] = fn(a, compact=True)
+            except Exception as e:  # a failed sub-record is reported, the headline stands
+                line[name] = {"error": f"{type(e).__name__}: {e}"}
+            line[name]["wall_s"] = round(time.perf_counter() - t0, 1)
+            print(f"[bench] {name} {line[name]['wall_s']} s", file=sys.stderr, flush=True)
     print(json.dumps(line))
     if world > 1:
         dist.destroy_process_group()
 
 
-def run_batched(a):
+def flop_iter32(p, q):
+    """Algorithmic flops of one FP32 seed iteration: S..Svv (the evaluation count of the
+    measurement section: 2 [4 k1 k2 n_v + 4 k1 n_out] with n_v = 3, n_out = 6), the quotient rule
+    (~12 per output component) and the 2x2 Newton solve (~30)."""
+    k1, k2 = p + 1, q + 1
+    return 2 * (4 * k1 * k2 * 3 + 4 * k1 * 6) + 12 * 18 + 30
+
+
+def work_counts(gn, s, Pd):
+    """Seed iterations of one mixed inversion of Pd, counted by the library's counting variant
+    of the kernel (untimed)."""
+    try:
+        return s.count_work(Pd, gn.PREC_MIXED)
+    except (AttributeError, gn.NurbsError):
+        return None
+
+
+def batched_record(a, compact=False):
     """Batched uneven workload: 4096 surfaces (p,q in {2,3,5}, nets 4..48), per-surface query
     counts log-uniform in 16..65536, queries S(u,v) + N(0,1e-3) n; one persistent launch per
     step, replayed from a CUDA graph, launch configuration picked by the pool's autotuner."""
@@ -303,6 +389,7 @@ def run_batched(a):
     gn = load_pkg()
     from gpu_nurbs_gb300 import synth
     t_start = time.perf_counter()
+    steps = 6 if compact else a.steps
 
     def phase(msg):
         print(f"[batched] {time.perf_counter() - t_start:8.2f}s {msg}", file=sys.stderr, flush=True)
@@ -340,18 +427,9 @@ def run_batched(a):
     phase("graphs captured")
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     stream = torch.cuda.current_stream()
+    timed = event_timer(torch, flush)
 
-    def timed(fn, steps):
-        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
-        for k in range(steps):
-            flush.fill_(float(k))
-            evs[k][0].record(stream)
-            fn()
-            evs[k][1].record(stream)
-        torch.cuda.synchronize()
-        return [e0.elapsed_time(e1) for e0, e1 in evs]
-
-    for _ in range(a.warmup):
+    for _ in range(3 if compact else max(3, a.warmup)):
         g_mixed.launch()
     torch.cuda.synchronize()
     phase("mixed warm-up done")
@@ -360,10 +438,10 @@ def run_batched(a):
     Ph = Pd.cpu().pin_memory()
     hout = [torch.empty(x.shape, dtype=x.dtype).pin_memory() for x in out]
     clocks = Clocks(0)
-    t_mixed = timed(g_mixed.launch, a.steps)
+    t_mixed = timed(g_mixed.launch, steps)
     phase("mixed timed")
     t_e2e, parts = [], []
-    for k in range(1 + max(3, a.steps // 2)):   # the first pass (untimed) maps the pinned buffers
+    for k in range(1 + max(3, steps // 2)):   # the first pass (untimed) maps the pinned buffers
         flush.fill_(float(k))
         ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
         torch.cuda.synchronize()
@@ -381,13 +459,12 @@ def run_batched(a):
             t_e2e.append((time.perf_counter() - t0) * 1e3)
             parts.append([round(ev[i].elapsed_time(ev[i + 1]), 2) for i in range(3)])
     phase("e2e timed")
-    clk = clocks.stop()
-    phase("clocks read")
     g_fp64.launch()
     torch.cuda.synchronize()
     phase("fp64 warm-up done")
-    t_fp64 = timed(g_fp64.launch, max(2, a.steps // 8))
+    t_fp64 = timed(g_fp64.launch, max(2, steps // 8))
     phase("fp64 timed")
+    clk = clocks.stop()
     g_mixed.launch()
     torch.cuda.synchronize()
     g_uv, g_st, g_res = (x.cpu().numpy() for x in out)
@@ -397,9 +474,9 @@ def run_batched(a):
     ms_e2e = sum(t_e2e) / len(t_e2e)
     found = g_st == 0
     err = np.abs(g_uv - uv_true).max(1)
-    line = {
-        "metric": METRIC, "value": n / (ms_mixed / 1e3), "unit": "inversions/s", "n_gpus": 1, "steps": a.steps,
-        "warmup": a.warmup, "ms_per_step": ms_mixed, "higher_is_better": True, "scaling": "weak",
+    rec = {
+        "metric": METRIC, "value": n / (ms_mixed / 1e3), "unit": "inversions/s", "n_gpus": 1, "steps": steps,
+        "warmup": 3, "ms_per_step": ms_mixed, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "fp32+fp64 (mixed)", "data": "synthetic (seeded)",
         "config": {"workload": f"batched: {len(surfs)} surfaces, p,q in {{2,3,5}}, nets 4..48, {n} queries "
                                "(log-uniform 16..65536 per surface), offsets N(0,1e-3)",
@@ -413,39 +490,159 @@ def run_batched(a):
         "e2e": {"value": n / (ms_e2e / 1e3), "unit": "inversions/s", "h2d_bytes_per_step": n * 24,
                 "d2h_bytes_per_step": n * 28, "ms_per_step": ms_e2e,
                 "step_ms": [round(t, 3) for t in t_e2e], "h2d_kernel_d2h_ms": parts},
-        "clocks": clk, "gpu_launches": a.steps,
+        "clocks": clk, "gpu_launches": steps,
     }
     if not a.no_cpu:
         # oracle on the first surfaces' queries (a bounded sample), checking this run's results
-        import oracle as O
-        sys.path.insert(0, os.path.join(ROOT, "tests"))
-        from parity import classify_inversion
-        cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
         P_h = Ph.numpy()
-        tot = dict()
-        dt = 0.0
-        done = 0
-        k = 0
+        tot, dt, done, k = dict(), 0.0, 0, 0
         while done < a.cpu_sample and k < len(surfs):
             sl = slice(int(offsets[k]), int(min(offsets[k + 1], offsets[k] + a.cpu_sample - done)))
-            o = O.OracleSurface(surfs[k])
-            o.tree()
-            t0 = time.perf_counter()
-            ouv, ost, ores, _ = o.invert(P_h[sl], threads=cores)
-            dt += time.perf_counter() - t0
-            c = classify_inversion(g_uv[sl], g_st[sl], g_res[sl], ouv, ost, ores, P_h[sl])
-            for kk, v in c.items():
-                if kk not in ("fail_idx", "max_uv_err_same"):
-                    tot[kk] = tot.get(kk, 0) + v
+            c, t = oracle_parity_sample(surfs[k], P_h[sl], g_uv[sl], g_st[sl], g_res[sl])
+            merge_parity(tot, c)
+            dt += t
             done += sl.stop - sl.start
             k += 1
-        line["cpu_baseline"] = {"value": done / dt, "unit": "inversions/s", "cores": cores, "kind": "port",
-                                "sample": f"{done} queries of the first {k} surfaces, converged-GN oracle"}
-        line["parity_sample"] = tot
-    print(json.dumps(line))
+        tot["p99_uv_err_same_max_over_surfaces"] = max(tot.pop("p99_uv_err_same_per_surface", [0.0]))
+        rec["cpu_baseline"] = {"value": done / dt, "unit": "inversions/s", "cores": host_cores(), "kind": "port",
+                               "sample": f"{done} queries of the first {k} surfaces, the oracle's inversion"}
+        rec["parity_sample"] = tot
+    if compact:
+        keep = ("value", "unit", "ms_per_step", "fp64_value", "mixed_vs_fp64", "e2e", "config", "clocks",
+                "parity_sample", "accuracy", "steps")
+        rec = {k: rec[k] for k in keep if k in rec}
+        rec["e2e"] = {k: rec["e2e"][k] for k in ("value", "ms_per_step", "h2d_bytes_per_step", "d2h_bytes_per_step")}
+    return rec
 
 
-def run_serving(a):
+def run_batched(a):
+    print(json.dumps(batched_record(a)))
+
+
+def quintic_record(a, compact=False):
+    """Degree-5 256x256 surface, 2^24 queries S(u,v) + N(0,1e-3) n: mixed and FP64 inversions/s,
+    and the per-query parameter error against the oracle (max, p99) on a bounded sample."""
+    import torch
+    gn = load_pkg()
+    n = 1 << 24
+    steps = 5 if compact else a.steps
+    surf, s, uv_true, P = make_workload(gn, torch, "quintic", n, 1000)
+    Pd = torch.as_tensor(P, device="cuda")
+    out = (torch.empty((n, 2), dtype=torch.float64, device="cuda"), torch.empty(n, dtype=torch.int32, device="cuda"),
+           torch.empty(n, dtype=torch.float64, device="cuda"))
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    timed = event_timer(torch, flush)
+    inv_mixed = lambda: s.invert(Pd, gn.PREC_MIXED, out=out)
+    inv_fp64 = lambda: s.invert(Pd, gn.PREC_FP64, out=out)
+    for _ in range(3):
+        inv_mixed()
+    inv_fp64()
+    torch.cuda.synchronize()
+    clocks = Clocks(0)
+    t_mixed = timed(inv_mixed, steps)
+    t_fp64 = timed(inv_fp64, 2)
+    clk = clocks.stop()
+    inv_mixed()
+    g_uv, g_st, g_res = (x.cpu().numpy() for x in out)
+    ms_mixed, ms_fp64 = sum(t_mixed) / len(t_mixed), sum(t_fp64) / len(t_fp64)
+    rec = {"value": n / (ms_mixed / 1e3), "unit": "inversions/s", "ms_per_step": ms_mixed, "steps": steps,
+           "fp64_value": n / (ms_fp64 / 1e3), "fp64_ms_per_step": ms_fp64, "mixed_vs_fp64": ms_fp64 / ms_mixed,
+           "config": {"workload": workload_label("quintic", n), "l2": "flushed (512 MB write) before each step"},
+           "clocks": clk}
+    if not a.no_cpu:
+        m = min(a.cpu_sample // 2, n)
+        import oracle as O
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+        from parity import eval_errors
+        # residuals can differ by as much as the two FP64 evaluations of S do at degree 5
+        ev = s.eval(torch.as_tensor(uv_true[:m], device="cuda"), gn.S).cpu().numpy()
+        res_abs = max(1e-14, 4 * eval_errors(ev, O.OracleSurface(surf).eval(uv_true[:m], 1))[0])
+        c, dt = oracle_parity_sample(surf, P[:m], g_uv[:m], g_st[:m], g_res[:m], res_abs=res_abs)
+        rec["parity_sample"] = c
+        rec["cpu_baseline"] = {"value": m / dt, "unit": "inversions/s", "cores": host_cores(), "kind": "port",
+                               "sample": f"{m} queries of the workload, the oracle's inversion"}
+    return rec
+
+
+def measured_hbm_gbs():
+    """HBM copy bandwidth of the GB300s (the measured-peaks file), else the fallback."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured copy bandwidth of this pool's GB300"
+    except (OSError, ValueError, KeyError):
+        return 6800.0, "fallback 6.8 TB/s"
+
+
+def eval_record(a, compact=False, which="eval-large"):
+    """Batched evaluation throughput: 'eval-small' = 2^20 (u,v) on the 8x8 bicubic surface with
+    S, Su, Sv; 'eval-large' = 2^26 (u,v) on the 64x64 bicubic surface with S..Svv.  FP64 and FP32."""
+    import torch
+    gn = load_pkg()
+    from gpu_nurbs_gb300 import synth
+    small = which == "eval-small"
+    surf = synth.surface_small() if small else synth.surface_large()
+    mask = 7 if small else 63
+    n = (1 << 20) if small else (1 << 26)
+    steps = 8 if compact else a.steps
+    s = gn.Surface(surf)
+    r = synth.Rng(synth.SEED_BASE + 77)
+    uv = torch.as_tensor(np.stack([r.uniform(n), r.uniform(n)], 1), device="cuda")
+    uv32 = uv.float()
+    nb = bin(mask).count("1")
+    out = torch.empty((3 * nb, n), dtype=torch.float64, device="cuda")
+    out32 = torch.empty((3 * nb, n), dtype=torch.float32, device="cuda")
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    timed = event_timer(torch, flush)
+    L = gn.lib()
+
+    def ev64():
+        gn.check(L.nurbs_eval(s.h, uv.data_ptr(), n, mask, out.data_ptr(), gn.PREC_FP64, gn._stream()), "eval")
+
+    def ev32():
+        gn.check(L.nurbs_eval_f32(s.h, uv32.data_ptr(), n, mask, out32.data_ptr(), gn._stream()), "eval")
+
+    for _ in range(3):
+        ev64()
+        ev32()
+    torch.cuda.synchronize()
+    clocks = Clocks(0)
+    t64 = timed(ev64, steps)
+    t32 = timed(ev32, steps)
+    clk = clocks.stop()
+    ms64, ms32 = sum(t64) / len(t64), sum(t32) / len(t32)
+    peak64, peak32 = fp64_peak_tflops(torch)
+    hbm, hbm_src = measured_hbm_gbs()
+    k1, k2 = surf["p"] + 1, surf["q"] + 1
+    nv_, nout = (2, 3) if small else (3, 6)
+    flop = 2 * (4 * k1 * k2 * nv_ + 4 * k1 * nout)       # algorithmic flops per point
+    bytes64, bytes32 = 16 + 24 * nout, 8 + 12 * nout
+    ach64 = flop * n / (ms64 / 1e3) / 1e12
+    gbs32 = bytes32 * n / (ms32 / 1e3) / 1e9
+    return {
+        "metric": "evaluations/s (FP64, " + ("S,Su,Sv" if small else "S..Svv") + ")", "value": n / (ms64 / 1e3),
+        "unit": "points/s", "n_gpus": 1, "steps": steps, "warmup": 3, "ms_per_step": ms64,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp64", "data": "synthetic (seeded)",
+        "config": {"workload": which, "points_per_step": n, "outputs": "SoA",
+                   "l2": "flushed (512 MB write) before each step"},
+        "fp32_value": n / (ms32 / 1e3), "fp32_ms_per_step": ms32,
+        "roofline": {"bound": "fp64", "achieved": ach64, "peak": peak64, "unit": "TFLOP/s",
+                     "frac": ach64 / peak64 if peak64 else None,
+                     "traffic": TRAFFIC_PER_UNIT[which] * n if which in TRAFFIC_PER_UNIT else None,
+                     "traffic_unit": "bytes per launch",
+                     "flop_per_point": flop, "bytes_per_point_fp64": bytes64, "bytes_per_point_fp32": bytes32,
+                     "hbm_achieved_gbs": bytes64 * n / (ms64 / 1e3) / 1e9,
+                     "fp32": {"bound": "hbm", "achieved": gbs32, "peak": hbm, "unit": "GB/s",
+                              "frac": gbs32 / hbm if hbm else None, "peak_source": hbm_src},
+                     "fp32_achieved_tflops": flop * n / (ms32 / 1e3) / 1e12, "fp32_peak": peak32},
+        "clocks": clk, "gpu_launches": 2 * steps,
+    }
+
+
+def run_eval(a):
+    print(json.dumps(eval_record(a, which=a.workload)))
+
+
+def serving_record(a, compact=False):
     """Serving: a pool of 10^4 surfaces (generated as the batched workload) under a 20 GB budget;
     Poisson request arrivals swept over rates; each request targets a surface drawn Zipf(1.1)
     with 1..4096 queries (log-uniform), 10% of requests upload a new surface.  Requests are
@@ -455,6 +652,8 @@ def run_serving(a):
     gn = load_pkg()
     from gpu_nurbs_gb300 import synth
     t_start = time.perf_counter()
+    serve_seconds = min(a.serve_seconds, 0.5) if compact else a.serve_seconds
+    rates = [1e4, 1e5, 3e5, 1e6] if compact else [float(x) for x in a.rates.split(",")]
 
     def phase(msg):
         print(f"[serving] {time.perf_counter() - t_start:8.2f}s {msg}", file=sys.stderr, flush=True)
@@ -472,9 +671,8 @@ def run_serving(a):
     pz /= pz.sum()
     perm = r.g.permutation(npool)
     upload_bank = synth.batched_surfaces(2000, seed=synth.SEED_BASE + 4 + 2)[0]
-    rates = [float(x) for x in a.rates.split(",")]
 
-    def trace(rate, nreq, precision_server):
+    def trace(rate, nreq):
         kind = (r.uniform(nreq) < a.upload_frac).astype(np.int32)
         sizes = np.where(kind == 0, np.exp(r.uniform(nreq, 0.0, np.log(4096.0))).astype(np.int64), 0)
         sizes = np.maximum(sizes, kind == 0)
@@ -496,10 +694,12 @@ def run_serving(a):
         return arrival, kind, req_ids, qoff, P, uidx, sizes
 
     def serve(rate, nreq, precision):
-        arrival, kind, req_ids, qoff, P, uidx, sizes = trace(rate, nreq, precision)
+        arrival, kind, req_ids, qoff, P, uidx, sizes = trace(rate, nreq)
         srv = gn.Server(pool, slots=a.slots, max_batch_queries=1 << 16, max_batch_requests=4096, precision=precision)
+        clocks = Clocks(0)
         uv, st, res, lat, results, uids = srv.replay(arrival, kind, req_ids, qoff, P, upload_bank, uidx,
                                                      timeout_ms=600000)
+        clk = clocks.stop()
         stats = srv.stats()
         srv.close()
         # uploaded surfaces are released again so every rate starts from the same pool
@@ -522,126 +722,59 @@ def run_serving(a):
                 "gpu_ms_per_batch": stats.gpu_ms / max(1, stats.batches),
                 "dispatch_us_per_batch": stats.dispatch_us / max(1, stats.batches),
                 "retire_us_per_batch": stats.retire_us / max(1, stats.batches),
-                "found_frac": float((st[np.repeat(inv, sizes)] == 0).mean()) if sizes.sum() else None}
+                "found_frac": float((st[np.repeat(inv, sizes)] == 0).mean()) if sizes.sum() else None,
+                "clocks": clk}
 
     sweep = []
     for rate in rates:
-        nreq = int(min(max(rate * a.serve_seconds, 2000), a.max_requests))
+        nreq = int(min(max(rate * serve_seconds, 2000), a.max_requests))
         sweep.append(serve(rate, nreq, gn.PREC_MIXED))
         phase(f"rate {rate:.0f}: p50 {sweep[-1]['p50_ms']:.3f} ms p99 {sweep[-1]['p99_ms']:.3f} ms, "
               f"{sweep[-1]['achieved_queries_s'] / 1e6:.1f} M queries/s")
     peak = max(sweep, key=lambda d: d["achieved_req_s"])
     half_rate = peak["achieved_req_s"] / 2
-    half = serve(half_rate, int(min(max(half_rate * a.serve_seconds, 2000), a.max_requests)), gn.PREC_MIXED)
+    half = serve(half_rate, int(min(max(half_rate * serve_seconds, 2000), a.max_requests)), gn.PREC_MIXED)
     phase(f"half peak {half_rate:.0f} req/s: p99 {half['p99_ms']:.3f} ms")
-    fp64_peak = serve(rates[-1], int(min(max(rates[-1] * a.serve_seconds, 2000), a.max_requests) // 4), gn.PREC_FP64)
+    fp64_peak = serve(rates[-1], int(min(max(rates[-1] * serve_seconds, 2000), a.max_requests) // 4), gn.PREC_FP64)
     phase("fp64 peak measured")
-    line = {
+    rec = {
         "metric": "serve p99 latency at half of peak throughput (mixed)", "value": half["p99_ms"], "unit": "ms",
         "n_gpus": 1, "steps": len(rates) + 2, "warmup": 0, "ms_per_step": None, "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None, "dtype": "fp32+fp64 (mixed)", "data": "synthetic (seeded)",
         "config": {"workload": f"serving: pool of {npool} surfaces (batched-workload distribution), 20 GB budget, "
                                "Poisson arrivals, Zipf(1.1) surfaces, 1..4096 queries/request log-uniform, "
                                "10% uploads", "slots": a.slots, "max_batch_queries": 1 << 16,
-                   "queries_per_warp_chunk": a.serve_chunk},
+                   "queries_per_warp_chunk": a.serve_chunk, "rates_req_s": rates, "seconds_per_rate": serve_seconds},
         "peak": {"req_s": peak["achieved_req_s"], "queries_s": peak["achieved_queries_s"]},
         "half_peak": half, "sweep": sweep,
         "fp64_server_at_top_rate": fp64_peak,
         "mixed_vs_fp64_peak_queries_s": peak["achieved_queries_s"] / fp64_peak["achieved_queries_s"],
+        "clocks": half["clocks"],
         "gpu_launches": None,
     }
-    print(json.dumps(line))
+    if compact:
+        rec = {"value": rec["value"], "unit": "ms", "metric": rec["metric"], "peak": rec["peak"],
+               "half_peak": {k: half[k] for k in ("rate_req_s", "achieved_req_s", "achieved_queries_s", "p50_ms",
+                                                  "p99_ms", "ok_frac", "found_frac", "upload_p99_ms", "clocks")},
+               "fp64_peak_queries_s": fp64_peak["achieved_queries_s"],
+               "mixed_vs_fp64_peak_queries_s": rec["mixed_vs_fp64_peak_queries_s"],
+               "sweep": [{k: d[k] for k in ("rate_req_s", "achieved_req_s", "achieved_queries_s", "p50_ms", "p99_ms")}
+                         for d in sweep],
+               "config": rec["config"], "clocks": half["clocks"]}
+    return rec
 
 
-def run_eval(a):
-    """Batched evaluation throughput: 'eval-small' = 2^20 (u,v) on the 8x8 bicubic surface with
-    S, Su, Sv; 'eval-large' = 2^26 (u,v) on the 64x64 bicubic surface with S..Svv.  FP64 and FP32."""
-    import torch
-    gn = load_pkg()
-    from gpu_nurbs_gb300 import synth
-    small = a.workload == "eval-small"
-    surf = synth.surface_small() if small else synth.surface_large()
-    mask = 7 if small else 63
-    n = a.queries if a.queries != (1 << 20) or small else (1 << 26)
-    s = gn.Surface(surf)
-    r = synth.Rng(synth.SEED_BASE + 77)
-    uv = torch.as_tensor(np.stack([r.uniform(n), r.uniform(n)], 1), device="cuda")
-    uv32 = uv.float()
-    nb = bin(mask).count("1")
-    out = torch.empty((3 * nb, n), dtype=torch.float64, device="cuda")
-    out32 = torch.empty((3 * nb, n), dtype=torch.float32, device="cuda")
-    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
-    stream = torch.cuda.current_stream()
-    L = gn.lib()
-
-    def ev64():
-        gn.check(L.nurbs_eval(s.h, uv.data_ptr(), n, mask, out.data_ptr(), gn.PREC_FP64, gn._stream()), "eval")
-
-    def ev32():
-        gn.check(L.nurbs_eval_f32(s.h, uv32.data_ptr(), n, mask, out32.data_ptr(), gn._stream()), "eval")
-
-    def timed(fn, steps):
-        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
-        for k in range(steps):
-            flush.fill_(float(k))
-            evs[k][0].record(stream)
-            fn()
-            evs[k][1].record(stream)
-        torch.cuda.synchronize()
-        return [e0.elapsed_time(e1) for e0, e1 in evs]
-
-    for _ in range(a.warmup):
-        ev64()
-        ev32()
-    torch.cuda.synchronize()
-    clocks = Clocks(0)
-    t64 = timed(ev64, a.steps)
-    t32 = timed(ev32, a.steps)
-    clk = clocks.stop()
-    ms64, ms32 = sum(t64) / len(t64), sum(t32) / len(t32)
-    peak64, peak32 = fp64_peak_tflops(torch)
-    k1, k2 = surf["p"] + 1, surf["q"] + 1
-    nv_, nout = (2, 3) if small else (3, 6)
-    flop = 2 * (4 * k1 * k2 * nv_ + 4 * k1 * nout)       # algorithmic flops per point
-    bytes64 = 16 + 24 * nout
-    ach64 = flop * n / (ms64 / 1e3) / 1e12
-    line = {
-        "metric": "evaluations/s (FP64, " + ("S,Su,Sv" if small else "S..Svv") + ")", "value": n / (ms64 / 1e3),
-        "unit": "points/s", "n_gpus": 1, "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms64,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp64", "data": "synthetic (seeded)",
-        "config": {"workload": a.workload, "points_per_step": n, "outputs": "SoA FP64",
-                   "l2": "flushed (512 MB write) before each step"},
-        "fp32_value": n / (ms32 / 1e3), "fp32_ms_per_step": ms32,
-        "roofline": {"bound": "fp64", "achieved": ach64, "peak": peak64, "unit": "TFLOP/s",
-                     "frac": ach64 / peak64 if peak64 else None,
-                     "traffic": TRAFFIC_PER_UNIT[a.workload] * n if a.workload in TRAFFIC_PER_UNIT else None,
-                     "traffic_unit": "bytes per launch",
-                     "flop_per_point": flop, "bytes_per_point_fp64": bytes64,
-                     "hbm_achieved_gbs": bytes64 * n / (ms64 / 1e3) / 1e9,
-                     "fp32_hbm_achieved_gbs": (8 + 12 * nout) * n / (ms32 / 1e3) / 1e9,
-                     "fp32_achieved_tflops": flop * n / (ms32 / 1e3) / 1e12, "fp32_peak": peak32},
-        "clocks": clk, "gpu_launches": 2 * a.steps,
-    }
-    print(json.dumps(line))
+def run_serving(a):
+    print(json.dumps(serving_record(a)))
 
 
 def cpu_baseline(surf, P, sample, g_uv, g_st, g_res):
     """The oracle (C restatement of the reference FP64 path) on all host cores, bounded sample;
     its results on that sample also check this run's mixed-precision results."""
-    import oracle as O
-    sys.path.insert(0, os.path.join(ROOT, "tests"))
-    from parity import classify_inversion
-    cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
-    o = O.OracleSurface(surf)
-    o.tree()
     Ps = P[:sample]
-    t0 = time.perf_counter()
-    ouv, ost, ores, _ = o.invert(Ps, threads=cores)
-    dt = time.perf_counter() - t0
-    c = classify_inversion(g_uv[:sample], g_st[:sample], g_res[:sample], ouv, ost, ores, Ps)
-    par = {k: v for k, v in c.items() if k != "fail_idx"}
-    return ({"value": len(Ps) / dt, "unit": "inversions/s", "cores": cores, "kind": "port",
-             "sample": f"{len(Ps)} queries of the same workload, converged-GN oracle, {dt:.2f} s wall"}, par)
+    par, dt = oracle_parity_sample(surf, Ps, g_uv[:sample], g_st[:sample], g_res[:sample])
+    return ({"value": len(Ps) / dt, "unit": "inversions/s", "cores": host_cores(), "kind": "port",
+             "sample": f"{len(Ps)} queries of the same workload, the oracle's inversion, {dt:.2f} s wall"}, par)
 
 
 def run_reference(a):
@@ -700,6 +833,8 @@ def main():
     ap.add_argument("--queries", type=int, default=1 << 20)
     ap.add_argument("--cpu-sample", type=int, default=1 << 14)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--headline-only", action="store_true",
+                    help="the large workload's line without the batched/quintic/eval/serving sub-records")
     a = ap.parse_args()
     if a.impl == "reference":
         run_reference(a)

@@ -87,6 +87,7 @@ SIGNATURES = {
     "nurbs_candidates": (C.c_int, [_vp, _vp, _i64, _vp, _vp, _vp]),
     "nurbs_invert": (C.c_int, [_vp, _vp, _i64, _vp, _vp, _vp, C.c_int, _vp]),
     "nurbs_invert_host": (C.c_int, [_vp, _vp, _i64, _vp, _vp, _vp, C.c_int, _vp]),
+    "nurbs_invert_count": (C.c_int, [_vp, _vp, _i64, C.c_int, _vp, _vp]),
     "nurbs_probe_fp_peak": (C.c_int, [C.c_int, C.POINTER(C.c_double), _vp]),
     "nurbs_pool_create": (C.c_int, [_i64, C.c_int, C.POINTER(_vp)]),
     "nurbs_pool_destroy": (C.c_int, [_vp]),
@@ -294,6 +295,15 @@ class Surface:
         check(lib().nurbs_invert(self.h, _ptr(P), n, _ptr(uv), _ptr(st), _ptr(res), precision, _stream(stream)),
               "nurbs_invert")
         return uv, st, res
+
+    def count_work(self, P, precision: int = PREC_MIXED, stream=None) -> dict:
+        """Work of one inversion of P (CUDA tensor), from the kernel's counting variant:
+        seed iterations and final FP64 polishes."""
+        P = P.contiguous()
+        counts = (C.c_ulonglong * 2)()
+        check(lib().nurbs_invert_count(self.h, _ptr(P), P.shape[0], precision, C.cast(counts, C.c_void_p),
+                                       _stream(stream)), "nurbs_invert_count")
+        return {"seed_iterations": int(counts[0]), "final_polishes": int(counts[1])}
 
     def invert_host(self, P: np.ndarray, precision: int = PREC_MIXED, stream=None, out=None):
         """Host buffers in and out (copies inside the call)."""

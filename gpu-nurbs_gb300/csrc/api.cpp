@@ -369,6 +369,34 @@ int nurbs_invert(nurbs_surface_t s, const double* P_dev, int64_t n, double* uv_d
   return NURBS_OK;
 }
 
+int nurbs_invert_count(nurbs_surface_t s, const double* P_dev, int64_t n, int precision,
+                       unsigned long long* counts_host, void* stream) {
+  if (!s || !counts_host) return fail(NURBS_E_INVALID, "NULL argument");
+  if (n < 0) return fail(NURBS_E_INVALID, "negative count");
+  if (precision != NURBS_PREC_FP64 && precision != NURBS_PREC_MIXED)
+    return fail(NURBS_E_INVALID, "precision %d is not FP64 or MIXED", precision);
+  counts_host[0] = counts_host[1] = 0;
+  if (n == 0) return NURBS_OK;
+  if (!P_dev) return fail(NURBS_E_INVALID, "NULL buffer");
+  cudaStream_t st = (cudaStream_t)stream;
+  const size_t oUV = 256, oS = oUV + align256((size_t)n * 16), oR = oS + align256((size_t)n * 4),
+               total = oR + align256((size_t)n * 8);
+  char* buf = nullptr;
+  CUDA_TRY(cudaMallocAsync((void**)&buf, total, st), "device buffers");
+  unsigned* counter = (unsigned*)buf;
+  unsigned long long* counts = (unsigned long long*)(buf + 64);
+  cudaError_t e = cudaMemsetAsync(buf, 0, 256, st);
+  if (e == cudaSuccess)
+    e = launch_invert_count(s->dev, P_dev, n, (double*)(buf + oUV), (int*)(buf + oS), (double*)(buf + oR), precision,
+                            counter, counts, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(counts_host, counts, 16, cudaMemcpyDeviceToHost, st);
+  cudaError_t e2 = cudaFreeAsync(buf, st);
+  if (e == cudaSuccess) e = e2;
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_fail(e, "counting inversion");
+  return NURBS_OK;
+}
+
 int nurbs_invert_host(nurbs_surface_t s, const double* P_host, int64_t n, double* uv_host, int* status_host,
                       double* residual_host, int precision, void* stream) {
   if (!s) return fail(NURBS_E_INVALID, "NULL surface");

@@ -429,11 +429,15 @@ __device__ __forceinline__ void stage_surface(const SurfDev& s, Staged<KS, MODE>
 }
 
 // One warp inverts the queries [q0, min(q0+32, qend)) of the staged surface.
-template <int P, int Q, int MODE, int KS>
+// COUNT: the work-counting variant (nurbs_invert_count): seed iterations and final FP64 polishes
+// are added to counts[0] and counts[1]; the results are the same.
+template <int P, int Q, int MODE, int KS, bool COUNT = false>
 __device__ __forceinline__ void invert_chunk(Staged<KS, MODE>& sm, WarpWork<MODE>& ww, const Ctx& cx,
                                              const double* __restrict__ Pq,
                                              int64_t q0, int64_t qend, double* __restrict__ uv_out,
-                                             int* __restrict__ st_out, double* __restrict__ res_out) {
+                                             int* __restrict__ st_out, double* __restrict__ res_out,
+                                             unsigned long long* __restrict__ counts = nullptr) {
+  unsigned n_iter = 0, n_final = 0;
   const int lane = threadIdx.x & 31;
   const unsigned FULL = 0xffffffffu;
   const unsigned lt_mask = (1u << lane) - 1u;
@@ -583,6 +587,7 @@ __device__ __forceinline__ void invert_chunk(Staged<KS, MODE>& sm, WarpWork<MODE
         int res = kContinue;
         if (active) {
           res = iterate32<P, Q>(cx, tx, ty, tz, sd, dist);
+          if constexpr (COUNT) ++n_iter;
           if (res == kContinue && !(sd.u >= sm.far32[0] && sd.u <= sm.far32[1] && sd.v >= sm.far32[2] &&
                                     sd.v <= sm.far32[3]))
             res = kFailed;
@@ -651,6 +656,7 @@ __device__ __forceinline__ void invert_chunk(Staged<KS, MODE>& sm, WarpWork<MODE
         bool keep = false;
         if (active) {
           res = iterate64<P, Q>(cx, tx, ty, tz, sd);
+          if constexpr (COUNT) ++n_iter;
           if (res == kConverged) keep = finish64<P, Q>(cx, tx, ty, tz, sd.u, sd.v, sd.hu, sd.hv, rr);
         }
         const bool done = active && res != kContinue;
@@ -711,14 +717,17 @@ __device__ __forceinline__ void invert_chunk(Staged<KS, MODE>& sm, WarpWork<MODE
           const bool tie = second && R.d2 <= e1 * e1;
           double u = R.u1, v = R.v1, r;
           const bool ok1 = final64<P, Q>(cx, px, py, pz, u, v, r);
+          if constexpr (COUNT) ++n_final;
           if (ok1) add(u, v, r);
           if (ok1 ? tie : second) {
             double u2 = R.u2, v2 = R.v2, r2;
+            if constexpr (COUNT) ++n_final;
             if (final64<P, Q>(cx, px, py, pz, u2, v2, r2)) add(u2, v2, r2);
           }
         }
         if (R.de <= e1 * e1) {
           double u3 = R.ue, v3 = R.ve, r3;
+          if constexpr (COUNT) ++n_final;
           if (final64<P, Q>(cx, px, py, pz, u3, v3, r3)) add(u3, v3, r3);
         }
       }
@@ -734,6 +743,17 @@ __device__ __forceinline__ void invert_chunk(Staged<KS, MODE>& sm, WarpWork<MODE
       res_out[q] = orr;
     }
     __syncwarp();
+  }
+  if constexpr (COUNT) {
+    unsigned long long a = n_iter, b = n_final;
+    for (int o = 16; o > 0; o >>= 1) {
+      a += __shfl_xor_sync(0xffffffffu, a, o);
+      b += __shfl_xor_sync(0xffffffffu, b, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+      atomicAdd(counts, a);
+      atomicAdd(counts + 1, b);
+    }
   }
 }
 

@@ -69,6 +69,51 @@ __global__ void __launch_bounds__(kThreads, MODE == kModeMixed ? ((P == 5 || Q =
   }
 }
 
+// The work-counting variant: the same per-query computation, 32-query chunks from the counter,
+// FP32/FP64 seed iterations and final FP64 polishes added to counts[0..1].  Diagnostic only.
+template <int P, int Q, int MODE>
+__global__ void __launch_bounds__(kThreads, 4)
+    k_invert_count(SurfDev s, const double* __restrict__ Pq, int64_t n, double* __restrict__ uv_out,
+                   int* __restrict__ st_out, double* __restrict__ res_out, unsigned* __restrict__ counter,
+                   unsigned long long* __restrict__ counts) {
+  __shared__ Staged<kSmemSpans, MODE> sm;
+  __shared__ WarpWork<MODE> ww[kWarps];
+  Ctx cx;
+  stage_surface<kSmemSpans>(s, sm, cx, threadIdx.x, blockDim.x);
+  __syncthreads();
+  const int warp = threadIdx.x >> 5;
+  const int64_t units = (n + 31) / 32;
+  for (;;) {
+    unsigned ch = 0;
+    if ((threadIdx.x & 31) == 0) ch = atomicAdd(counter, 1u);
+    ch = __shfl_sync(0xffffffffu, ch, 0);
+    if ((int64_t)ch >= units) break;
+    const int64_t q0 = (int64_t)ch * 32;
+    invert_chunk<P, Q, MODE, kSmemSpans, true>(sm, ww[warp], cx, Pq, q0, min(q0 + 32, n), uv_out, st_out, res_out,
+                                               counts);
+  }
+}
+
+template <int P, int Q, int MODE>
+cudaError_t launch_count_mode(const SurfDev& s, const double* P_, int64_t n, double* uv, int* st_, double* res,
+                              unsigned* counter, unsigned long long* counts, cudaStream_t st) {
+  if ((n + 31) / 32 > 0x3fffffffLL) return cudaErrorInvalidValue;
+  int sms = 0;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  int64_t blocks = std::min<int64_t>((n + 32 * kWarps - 1) / (32 * kWarps), (int64_t)(sms > 0 ? sms : 1) * 4);
+  k_invert_count<P, Q, MODE><<<(unsigned)blocks, kThreads, 0, st>>>(s, P_, n, uv, st_, res, counter, counts);
+  return cudaGetLastError();
+}
+
+template <int P, int Q>
+cudaError_t launch_count_pq(const SurfDev& s, const double* P_, int64_t n, double* uv, int* st_, double* res,
+                            int prec, unsigned* counter, unsigned long long* counts, cudaStream_t st) {
+  if (prec == 1) return launch_count_mode<P, Q, kModeMixed>(s, P_, n, uv, st_, res, counter, counts, st);
+  return launch_count_mode<P, Q, kModeFP64>(s, P_, n, uv, st_, res, counter, counts, st);
+}
+
 // CTAs of a kernel that fit on the current GPU at once (queried once per kernel and device).
 template <class K>
 int64_t resident_ctas(K kernel) {
@@ -108,6 +153,15 @@ cudaError_t launch_pq(const SurfDev& s, const double* P_, int64_t n, double* uv,
 }
 
 }  // namespace
+
+cudaError_t launch_invert_count(const SurfDev& s, const double* P, int64_t n, double* uv, int* status,
+                                double* residual, int precision, unsigned* counter, unsigned long long* counts,
+                                cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  if (s.p == 3 && s.q == 3) return launch_count_pq<3, 3>(s, P, n, uv, status, residual, precision, counter, counts, st);
+  if (s.p == 5 && s.q == 5) return launch_count_pq<5, 5>(s, P, n, uv, status, residual, precision, counter, counts, st);
+  return launch_count_pq<0, 0>(s, P, n, uv, status, residual, precision, counter, counts, st);
+}
 
 cudaError_t launch_invert(const SurfDev& s, const double* P, int64_t n, double* uv, int* status, double* residual,
                           int precision, unsigned* counter, cudaStream_t st) {

@@ -122,5 +122,9 @@ cudaError_t launch_invert_pool(const SurfDev* table, const InvTile* tiles, int n
 // stage d.  counter: one device word, zero when the launch starts (the kernel's chunk counter).
 cudaError_t launch_invert(const SurfDev& s, const double* P, int64_t n, double* uv, int* status,
                           double* residual, int precision, unsigned* counter, cudaStream_t st);
+// the work-counting variant; counts[0] += seed iterations, counts[1] += final FP64 polishes
+cudaError_t launch_invert_count(const SurfDev& s, const double* P, int64_t n, double* uv, int* status,
+                                double* residual, int precision, unsigned* counter, unsigned long long* counts,
+                                cudaStream_t st);
 
 }  // namespace gnurbs

@@ -180,6 +180,12 @@ int nurbs_candidates(nurbs_surface_t s, const double* P_dev, int64_t n, int* lis
  * residual_dev[n] = |S(uv) - P| in FP64.  precision: NURBS_PREC_FP64 or NURBS_PREC_MIXED. */
 int nurbs_invert(nurbs_surface_t s, const double* P_dev, int64_t n, double* uv_dev, int* status_dev,
                  double* residual_dev, int precision, void* stream);
+/* Diagnostic: the work one nurbs_invert of the same queries does, from a counting variant of
+ * the kernel (same results, not timed): counts_host[0] = seed iterations (FP32 iterations for
+ * NURBS_PREC_MIXED, FP64 for NURBS_PREC_FP64), counts_host[1] = final FP64 polishes (mixed).
+ * No counterpart in the reference.  Waits for `stream`. */
+int nurbs_invert_count(nurbs_surface_t s, const double* P_dev, int64_t n, int precision,
+                       unsigned long long* counts_host, void* stream);
 /* Same with host buffers: copies P in, runs, copies results out, waits.  Pinned host memory
  * gives the fastest copies. */
 int nurbs_invert_host(nurbs_surface_t s, const double* P_host, int64_t n, double* uv_host, int* status_host,

@@ -286,3 +286,23 @@ def test_invalid_arguments_return_status(nurbs, cuda):
     s.eval(uv[:0], 1)
     s.invert(T(g["P"], cuda)[:0], 1)
     torch.cuda.synchronize()
+
+
+def test_work_counter(nurbs, cuda):
+    """The counting variant of the inversion kernel: deterministic counts, at least one seed
+    iteration per candidate of a query and at most the cap per candidate, and one to three final
+    FP64 polishes per query with an FP32 minimum (mixed)."""
+    from gpu_nurbs_gb300 import synth
+    surf = synth.surface_large()
+    o, _, P = _queries(surf, 4096, 8, "large")
+    s = nurbs.Surface(surf)
+    cand = sum(len(c) for c in o.candidates(P))
+    for precision in (0, 1):
+        w1 = s.count_work(T(P, cuda), precision)
+        w2 = s.count_work(T(P, cuda), precision)
+        assert w1 == w2
+        assert cand <= w1["seed_iterations"] <= 40 * cand
+        if precision == 1:
+            assert 0.9 * len(P) <= w1["final_polishes"] <= 3 * len(P)
+        else:
+            assert w1["final_polishes"] == 0
