@@ -205,6 +205,7 @@ int nurbs_surface_create(int p, int q, int nu, int nv, const double* knots_u, co
   if (e == cudaSuccess) e = launch_basis(d.knots_v, q, d.knot_v, d.ns_v, s->basis_v, st);
   if (e == cudaSuccess) e = launch_span_matrices(d, s->basis_u, s->basis_v, (double*)d.m64, (float*)d.m32, st);
   if (e == cudaSuccess) e = launch_tree(d, st);
+  if (e == cudaSuccess) e = launch_centre_ders(d, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // img must outlive the copy
   if (e != cudaSuccess) {
     cudaFree(s->arena);
@@ -333,6 +334,7 @@ int nurbs_build_tree(nurbs_surface_t s, int levels, void* stream) {
   if (levels != 2) return fail(NURBS_E_UNSUPPORTED, "only the 2-level tree is supported (got %d)", levels);
   cudaStream_t st = (cudaStream_t)stream;
   CUDA_TRY(launch_tree(s->dev, st), "tree launch");
+  CUDA_TRY(launch_centre_ders(s->dev, st), "seed-centre derivatives");
   CUDA_TRY(cudaStreamSynchronize(st), "tree sync");
   s->tree_built = true;
   return NURBS_OK;

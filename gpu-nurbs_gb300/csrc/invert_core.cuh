@@ -147,6 +147,40 @@ __device__ __forceinline__ int iterate64(const Ctx& c, double px, double py, dou
   return kContinue;
 }
 
+// The first iteration of a seed from its node centre's precomputed S, Su, Sv (cd = 9 values,
+// the same bits the evaluation there gives): the seed advances to its second iteration when the
+// first one continues it, and is left at the centre otherwise, for iterate32/iterate64 to repeat
+// that first iteration and end the seed.  The step is the GN update (the Newton phase starts
+// after a step below kNewtonSwitch).
+template <typename T>
+__device__ __forceinline__ void first_step(const T* __restrict__ cd, T px, T py, T pz, const float far[4],
+                                           Seed<T>& st) {
+  const v3<T> S = {cd[0], cd[1], cd[2]}, Su = {cd[3], cd[4], cd[5]}, Sv = {cd[6], cd[7], cd[8]};
+  const v3<T> r = {S.x - px, S.y - py, S.z - pz};
+  T du, dv;
+  if (solve_step<T, T, sizeof(T) == 4>(r, Su, Sv, Su, Su, Su, false, du, dv) == kSingular) return;
+  if (!(isfinite(du) && isfinite(dv))) return;
+  const T u = st.u - du, v = st.v - dv;
+  T step;
+  if constexpr (sizeof(T) == 4) step = fmaxf(fabsf(du), fabsf(dv));
+  else step = fmax(fabs(du), fabs(dv));
+  if constexpr (sizeof(T) == 4) {
+    const float smag = fmaxf(fmaxf(fabsf(S.x), fabsf(S.y)), fmaxf(fabsf(S.z), 1.0f));
+    const v3<float> dS = {fast::mad(Sv.x, dv, Su.x * du), fast::mad(Sv.y, dv, Su.y * du),
+                          fast::mad(Sv.z, dv, Su.z * du)};
+    const float fl = 8.0f * 5.96e-8f * smag;
+    if (step <= kTol32 || dot3(dS, dS) <= fl * fl) return;  // converged at once: left to iterate32
+    if (!(u >= far[0] && u <= far[1] && v >= far[2] && v <= far[3])) return;
+  } else {
+    if (step <= kTolAny64) return;
+  }
+  st.u = u;
+  st.v = v;
+  st.prev = step;
+  st.newton = step < (T)kNewtonSwitch;
+  st.it = 1;
+}
+
 // FP64 residual at (u,v), with the domain test.
 template <int P, int Q>
 __device__ __forceinline__ bool finish64(const Ctx& c, double px, double py, double pz, double u, double v,
@@ -322,6 +356,8 @@ struct Staged {
   double ctr[kTreeNodes][2];
   float ctr32[kTreeNodes][2];
   double org[3];    // origin of the FP32 tables: FP32 iterations see P - org
+  const float* cd32;   // S, Su, Sv at the node centres (FP32, relative to org), 9 per node
+  const double* cd64;  // the same in FP64
   float dom32[4];
   float near32[4];  // 1 % of the extent around the domain: FP32 minima here are edge records
   float far32[4];  // two domain extents around the domain: an FP32 iterate beyond is abandoned
@@ -404,6 +440,8 @@ __device__ __forceinline__ void stage_surface(const SurfDev& s, Staged<KS, MODE>
   if (tid == 0) {
     sm.nb = nb;
     sm.tree = s.tree;
+    sm.cd32 = s.cd32;
+    sm.cd64 = s.cd64;
     sm.org[0] = s.org[0];
     sm.org[1] = s.org[1];
     sm.org[2] = s.org[2];
@@ -581,6 +619,7 @@ __device__ __forceinline__ void invert_chunk(Staged<KS, MODE>& sm, WarpWork<MODE
         sd.hu = 0;
         sd.hv = 0;
         sd.newton = false;
+        first_step<float>(sm.cd32 + 9 * node, tx, ty, tz, sm.far32, sd);
       };
       if (active) start();
       while (__any_sync(FULL, active)) {
@@ -648,6 +687,7 @@ __device__ __forceinline__ void invert_chunk(Staged<KS, MODE>& sm, WarpWork<MODE
         sd.hu = 0;
         sd.hv = 0;
         sd.newton = false;
+        first_step<double>(sm.cd64 + 9 * node, tx, ty, tz, sm.far32, sd);
       };
       if (active) start();
       while (__any_sync(FULL, active)) {

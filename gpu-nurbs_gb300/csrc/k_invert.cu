@@ -152,7 +152,58 @@ cudaError_t launch_pq(const SurfDev& s, const double* P_, int64_t n, double* uv,
   return launch_mode<P, Q, kModeFP64>(s, P_, n, uv, st_, res, counter, st);
 }
 
+// S, Su, Sv at the uv-centre of every built node, FP32 and FP64: the first iteration of every
+// seed starts there, and its evaluation does not depend on the query.  Computed with the same
+// device functions and arguments as the seed iterations, so the values are the same bits.
+template <int P, int Q>
+__device__ void centre_ders(const SurfDev& s, int k) {
+  if (k >= kTreeNodes || !s.built[k]) return;
+  const TreeNodeDev& T = s.tree[k];
+  const double cu = (T.uv_lb[0] + T.uv_rt[0]) / 2, cv = (T.uv_lb[1] + T.uv_rt[1]) / 2;  // kernel.cu:154
+  const fast::Locator<float> L32 = fast::global_locator<float>(s);
+  const fast::Locator<double> L64 = fast::global_locator<double>(s);
+  int hu = 0, hv = 0;
+  fast::SDer<float> d = fast::eval_at<float, P, Q, 2, true>(L32, s.m32, s.p, s.q, (float)cu, (float)cv, hu, hv);
+  hu = hv = 0;
+  fast::SDer<double> e = fast::eval_at<double, P, Q, 2>(L64, s.m64, s.p, s.q, cu, cv, hu, hv);
+  const float f[9] = {d.S.x, d.S.y, d.S.z, d.Su.x, d.Su.y, d.Su.z, d.Sv.x, d.Sv.y, d.Sv.z};
+  const double g[9] = {e.S.x, e.S.y, e.S.z, e.Su.x, e.Su.y, e.Su.z, e.Sv.x, e.Sv.y, e.Sv.z};
+  for (int c = 0; c < 9; ++c) {
+    s.cd32[9 * k + c] = f[c];
+    s.cd64[9 * k + c] = g[c];
+  }
+}
+
+template <int P, int Q>
+__global__ void k_centre_ders(SurfDev s) {
+  centre_ders<P, Q>(s, threadIdx.x);
+}
+
+__global__ void k_centre_ders_batched(const SurfDev* __restrict__ table, const int* __restrict__ ids) {
+  const SurfDev s = table[ids[blockIdx.x]];
+  if (s.p == 3 && s.q == 3) centre_ders<3, 3>(s, threadIdx.x);
+  else if (s.p == 5 && s.q == 5) centre_ders<5, 5>(s, threadIdx.x);
+  else if (s.p == 2 && s.q == 2) centre_ders<2, 2>(s, threadIdx.x);
+  else centre_ders<0, 0>(s, threadIdx.x);
+}
+
 }  // namespace
+
+cudaError_t launch_centre_ders(const SurfDev& s, cudaStream_t st) {
+  if (s.p == 3 && s.q == 3) k_centre_ders<3, 3><<<1, 96, 0, st>>>(s);
+  else if (s.p == 5 && s.q == 5) k_centre_ders<5, 5><<<1, 96, 0, st>>>(s);
+  else if (s.p == 2 && s.q == 2) k_centre_ders<2, 2><<<1, 96, 0, st>>>(s);
+  else k_centre_ders<0, 0><<<1, 96, 0, st>>>(s);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_centre_ders_batched(const SurfDev* table, const int* ids, int count, cudaStream_t st) {
+  for (int off = 0; off < count; off += 65535) {
+    const int c = count - off < 65535 ? count - off : 65535;
+    k_centre_ders_batched<<<c, 96, 0, st>>>(table, ids + off);
+  }
+  return cudaGetLastError();
+}
 
 cudaError_t launch_invert_count(const SurfDev& s, const double* P, int64_t n, double* uv, int* status,
                                 double* residual, int precision, unsigned* counter, unsigned long long* counts,

@@ -31,6 +31,8 @@ constexpr int kPts = kGap + 1;    // PointsPerEdge
 //                                    relative to the control net's centre, so its resolution is set by
 //                                    the surface's extent, not by its distance from the origin
 //   tree[65]                         TreeNodeDev; divided[65], built[65]
+//   cd32[65][9], cd64[65][9]         S, Su, Sv at every built node's uv-centre (the inversion seeds),
+//                                    FP32 (relative to org) and FP64, written after the tree
 struct SurfDev {
   int p, q, nu, nv;
   int ns_u, ns_v;
@@ -60,6 +62,8 @@ struct SurfDev {
   unsigned char* built;
   double* basis_u;        // per-span basis-to-power matrices (conversion scratch kept with the surface)
   double* basis_v;
+  float* cd32;            // seed-centre derivatives (see above)
+  double* cd64;
 };
 
 // Tree node in the reference TreeNode order (src/kernel/kernel.cuh:30-39), 80 bytes.
@@ -122,6 +126,9 @@ cudaError_t launch_invert_pool(const SurfDev* table, const InvTile* tiles, int n
 // stage d.  counter: one device word, zero when the launch starts (the kernel's chunk counter).
 cudaError_t launch_invert(const SurfDev& s, const double* P, int64_t n, double* uv, int* status,
                           double* residual, int precision, unsigned* counter, cudaStream_t st);
+// S, Su, Sv at the built nodes' uv-centres (cd32/cd64), after the tree is built
+cudaError_t launch_centre_ders(const SurfDev& s, cudaStream_t st);
+cudaError_t launch_centre_ders_batched(const SurfDev* table, const int* ids, int count, cudaStream_t st);
 // the work-counting variant; counts[0] += seed iterations, counts[1] += final FP64 polishes
 cudaError_t launch_invert_count(const SurfDev& s, const double* P, int64_t n, double* uv, int* status,
                                 double* residual, int precision, unsigned* counter, unsigned long long* counts,

@@ -404,6 +404,7 @@ int nurbs_pool_add(nurbs_pool_t P, int count, const nurbs_surface_desc* descs, v
   if (e == cudaSuccess)
     e = launch_span_matrices_batched(P->d_table, (const SpanJob*)(sdev + jb), (int)sjobs.size(), sitems, st);
   if (e == cudaSuccess) e = launch_tree_batched(P->d_table, (const int*)(sdev + jb + js), count, st);
+  if (e == cudaSuccess) e = launch_centre_ders_batched(P->d_table, (const int*)(sdev + jb + js), count, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // host images must outlive the copies
   // 4. publication (locked)
   std::lock_guard<std::mutex> lock(P->mu);
