@@ -26,6 +26,7 @@ OK = 0
 E_INVALID, E_CUDA, E_NOMEM, E_IO, E_PARSE, E_UNSUPPORTED, E_BUDGET, E_TIMEOUT, E_STATE = range(-1, -10, -1)
 S, SU, SV, SUU, SUV, SVV = 1, 2, 4, 8, 16, 32
 PREC_FP64, PREC_MIXED, PREC_FP32 = 0, 1, 2
+PCURVE_JUMP, PCURVE_AMBIGUOUS, PCURVE_NOT_FOUND = 1, 2, 4
 INV_FOUND, INV_AMBIGUOUS, INV_NO_CANDIDATE, INV_NOT_CONVERGED = 0, 1, 2, 3
 PTR_HOST, PTR_DEVICE = 0, 1
 TREE_NODES = 65
@@ -88,6 +89,7 @@ SIGNATURES = {
     "nurbs_invert": (C.c_int, [_vp, _vp, _i64, _vp, _vp, _vp, C.c_int, _vp]),
     "nurbs_invert_host": (C.c_int, [_vp, _vp, _i64, _vp, _vp, _vp, C.c_int, _vp]),
     "nurbs_invert_count": (C.c_int, [_vp, _vp, _i64, C.c_int, _vp, _vp]),
+    "nurbs_pcurve": (C.c_int, [_vp, _vp, _i64, _vp, _vp, _vp, _vp, C.c_int, _vp]),
     "nurbs_probe_fp_peak": (C.c_int, [C.c_int, C.POINTER(C.c_double), _vp]),
     "nurbs_pool_create": (C.c_int, [_i64, C.c_int, C.POINTER(_vp)]),
     "nurbs_pool_destroy": (C.c_int, [_vp]),
@@ -295,6 +297,20 @@ class Surface:
         check(lib().nurbs_invert(self.h, _ptr(P), n, _ptr(uv), _ptr(st), _ptr(res), precision, _stream(stream)),
               "nurbs_invert")
         return uv, st, res
+
+    def pcurve(self, C, precision: int = PREC_MIXED, stream=None):
+        """p-curve of ordered curve samples C ((n,3) CUDA tensor): (uv (n,2), status, residual,
+        flags) with flags PCURVE_JUMP / PCURVE_AMBIGUOUS / PCURVE_NOT_FOUND."""
+        torch = _torch()
+        C = C.contiguous()
+        n = C.shape[0]
+        uv = torch.empty((n, 2), dtype=torch.float64, device=C.device)
+        st = torch.empty(n, dtype=torch.int32, device=C.device)
+        res = torch.empty(n, dtype=torch.float64, device=C.device)
+        fl = torch.empty(n, dtype=torch.int32, device=C.device)
+        check(lib().nurbs_pcurve(self.h, _ptr(C), n, _ptr(uv), _ptr(st), _ptr(res), _ptr(fl), precision,
+                                 _stream(stream)), "nurbs_pcurve")
+        return uv, st, res, fl
 
     def count_work(self, P, precision: int = PREC_MIXED, stream=None) -> dict:
         """Work of one inversion of P (CUDA tensor), from the kernel's counting variant:

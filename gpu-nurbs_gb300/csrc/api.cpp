@@ -371,6 +371,31 @@ int nurbs_invert(nurbs_surface_t s, const double* P_dev, int64_t n, double* uv_d
   return NURBS_OK;
 }
 
+int nurbs_pcurve(nurbs_surface_t s, const double* C_dev, int64_t n, double* uv_dev, int* status_dev,
+                 double* residual_dev, int* flags_dev, int precision, void* stream) {
+  if (!s) return fail(NURBS_E_INVALID, "NULL surface");
+  if (n < 0) return fail(NURBS_E_INVALID, "negative count");
+  if (precision != NURBS_PREC_FP64 && precision != NURBS_PREC_MIXED)
+    return fail(NURBS_E_INVALID, "precision %d is not FP64 or MIXED", precision);
+  if (n == 0) return NURBS_OK;
+  if (!C_dev || !uv_dev || !status_dev || !residual_dev || !flags_dev) return fail(NURBS_E_INVALID, "NULL buffer");
+  cudaStream_t st = (cudaStream_t)stream;
+  // pass-1 answers in scratch: uv (16 n), status (4 n), residual (8 n)
+  const size_t oS = align256((size_t)n * 16), oR = oS + align256((size_t)n * 4), total = oR + align256((size_t)n * 8);
+  char* buf = nullptr;
+  CUDA_TRY(cudaMallocAsync((void**)&buf, total, st), "p-curve scratch");
+  double* uv0 = (double*)buf;
+  int* st0 = (int*)(buf + oS);
+  double* res0 = (double*)(buf + oR);
+  cudaError_t e = invert_on(s, C_dev, n, uv0, st0, res0, precision, st);
+  if (e == cudaSuccess)
+    e = launch_pcurve_passes(s->dev, C_dev, n, uv0, st0, res0, uv_dev, status_dev, residual_dev, flags_dev, st);
+  cudaError_t e2 = cudaFreeAsync(buf, st);
+  if (e == cudaSuccess) e = e2;
+  if (e != cudaSuccess) return cuda_fail(e, "p-curve");
+  return NURBS_OK;
+}
+
 int nurbs_invert_count(nurbs_surface_t s, const double* P_dev, int64_t n, int precision,
                        unsigned long long* counts_host, void* stream) {
   if (!s || !counts_host) return fail(NURBS_E_INVALID, "NULL argument");

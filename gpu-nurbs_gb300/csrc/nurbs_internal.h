@@ -126,6 +126,10 @@ cudaError_t launch_invert_pool(const SurfDev* table, const InvTile* tiles, int n
 // stage d.  counter: one device word, zero when the launch starts (the kernel's chunk counter).
 cudaError_t launch_invert(const SurfDev& s, const double* P, int64_t n, double* uv, int* status,
                           double* residual, int precision, unsigned* counter, cudaStream_t st);
+// p-curves: continuation from the neighbours' pass-1 answers, then flags (k_pcurve.cu)
+cudaError_t launch_pcurve_passes(const SurfDev& s, const double* C, int64_t n, const double* uv0, const int* st0,
+                                 const double* res0, double* uv, int* st, double* res, int* flags,
+                                 cudaStream_t stream);
 // S, Su, Sv at the built nodes' uv-centres (cd32/cd64), after the tree is built
 cudaError_t launch_centre_ders(const SurfDev& s, cudaStream_t st);
 cudaError_t launch_centre_ders_batched(const SurfDev* table, const int* ids, int count, cudaStream_t st);

@@ -180,6 +180,21 @@ int nurbs_candidates(nurbs_surface_t s, const double* P_dev, int64_t n, int* lis
  * residual_dev[n] = |S(uv) - P| in FP64.  precision: NURBS_PREC_FP64 or NURBS_PREC_MIXED. */
 int nurbs_invert(nurbs_surface_t s, const double* P_dev, int64_t n, double* uv_dev, int* status_dev,
                  double* residual_dev, int precision, void* stream);
+/* p-curve of a 3-D curve on the surface: the parameters of its n ordered samples C_dev[3n].
+ * No counterpart in the reference's code (its README names p-curve calculation as the use of
+ * the inversion).  Each sample is inverted as nurbs_invert does (precision FP64 or MIXED); each
+ * then takes FP64 Newton steps from its two neighbours' answers and keeps such a minimum when it
+ * is strictly closer (or when it had none); flags_dev[n] marks NURBS_PCURVE_JUMP (the parameter
+ * step from the previous sample exceeds 4 |chord| / sigma_min(J): a seam, a fold, another
+ * sheet), NURBS_PCURVE_AMBIGUOUS and NURBS_PCURVE_NOT_FOUND.  uv_dev[2n], status_dev[n],
+ * residual_dev[n] as nurbs_invert.  Allocates and frees 48 n bytes of device scratch on
+ * `stream`. */
+#define NURBS_PCURVE_JUMP      1
+#define NURBS_PCURVE_AMBIGUOUS 2
+#define NURBS_PCURVE_NOT_FOUND 4
+int nurbs_pcurve(nurbs_surface_t s, const double* C_dev, int64_t n, double* uv_dev, int* status_dev,
+                 double* residual_dev, int* flags_dev, int precision, void* stream);
+
 /* Diagnostic: the work one nurbs_invert of the same queries does, from a counting variant of
  * the kernel (same results, not timed): counts_host[0] = seed iterations (FP32 iterations for
  * NURBS_PREC_MIXED, FP64 for NURBS_PREC_FP64), counts_host[1] = final FP64 polishes (mixed).

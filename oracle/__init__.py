@@ -71,6 +71,9 @@ def lib():
         L.orc_invert_fp32_explore.restype = None
         L.orc_invert_fp32_explore.argtypes = [C.POINTER(_Surf), _dp, _dp, _bp, _dp, C.c_int64, C.c_int, C.c_int,
                                               C.c_double, _dp, _ip, _dp, C.c_int]
+        L.orc_pcurve.restype = None
+        L.orc_pcurve.argtypes = [C.POINTER(_Surf), _dp, _dp, _bp, _dp, C.c_int64, C.c_int, _dp, _ip, _dp, _ip,
+                                 C.c_int]
         L.orc_gauss_newton_shipped.restype = C.c_int
         L.orc_gauss_newton_shipped.argtypes = [C.POINTER(_Surf), _dp, _dp, _dp, C.c_double, _dp]
         L.orc_find_span.restype = C.c_int
@@ -189,6 +192,19 @@ class OracleSurface:
             fs.append(ff[None])
             rs.append(fr[None])
         return np.concatenate(us), np.concatenate(fs), np.concatenate(rs)
+
+    def pcurve(self, Cs: np.ndarray, max_iter: int = MAX_ITER, threads: int = 0):
+        """p-curve of ordered curve samples (orc_pcurve): uv (n,2), status, residual, flags."""
+        t, _, b = self.tree()
+        Cs = np.ascontiguousarray(Cs, dtype=np.float64).reshape(-1, 3)
+        n = Cs.shape[0]
+        uv = np.empty(2 * n, dtype=np.float64)
+        st = np.empty(n, dtype=np.int32)
+        res = np.empty(n, dtype=np.float64)
+        fl = np.empty(n, dtype=np.int32)
+        lib().orc_pcurve(C.byref(self._s), self.matrix_n, np.ascontiguousarray(t.reshape(-1)), b, Cs, n, max_iter,
+                         uv, st, res, fl, threads)
+        return uv.reshape(n, 2), st, res, fl
 
     def gauss_newton_shipped(self, seed, P, max_edge):
         uv = np.zeros(2)

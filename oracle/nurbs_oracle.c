@@ -894,3 +894,71 @@ void orc_invert_fp32_explore(const orc_surface* s, const double* M, const orc_tr
         residual[k] = isfinite(br) ? br : NAN;
     }
 }
+
+/* ------------------------------------------------------------------------------ p-curves
+ * The oracle of nurbs_pcurve: orc_invert of every sample, then FP64 Newton steps (the
+ * trajectory's Newton phase) from the two neighbours' answers, kept when strictly closer than
+ * the own answer or when there is none; flags from the final answers (jump: parameter step above
+ * 4 |chord| / sigma_min(J) at the sample's answer; ambiguous; not found). */
+void orc_pcurve(const orc_surface* s, const double* M, const orc_tree_node* tree, const unsigned char* built,
+                const double* C, int64_t n, int max_iter, double* uv, int* status, double* residual, int* flags,
+                int threads) {
+    double dom[4];
+    domain_of(s, dom);
+    double* uv0 = (double*)malloc(sizeof(double) * 2 * (size_t)(n > 0 ? n : 1));
+    int* st0 = (int*)malloc(sizeof(int) * (size_t)(n > 0 ? n : 1));
+    double* r0 = (double*)malloc(sizeof(double) * (size_t)(n > 0 ? n : 1));
+    orc_invert(s, M, tree, built, C, n, max_iter, uv0, st0, r0, NULL, threads);
+#ifdef _OPENMP
+    if (threads <= 0) threads = omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 64) num_threads(threads)
+#endif
+    for (int64_t i = 0; i < n; ++i) {
+        const double* Pk = C + 3 * i;
+        double bu = uv0[2 * i], bv = uv0[2 * i + 1], br = r0[i];
+        int bs = st0[i];
+        const double scale = fmax(1.0, fmax(fabs(Pk[0]), fmax(fabs(Pk[1]), fabs(Pk[2]))));
+        for (int side = 0; side < 2; ++side) {
+            const int64_t j = side == 0 ? i - 1 : i + 1;
+            if (j < 0 || j >= n || st0[j] > ORC_FOUND_AMBIGUOUS) continue;
+            double Cc[2] = {uv0[2 * j], uv0[2 * j + 1]};
+            int its;
+            if (!run_trajectory(s, M, Pk, Cc, max_iter, 1, &its)) continue;
+            if (!(Cc[0] >= dom[0] && Cc[0] <= dom[1] && Cc[1] >= dom[2] && Cc[1] <= dom[3])) continue;
+            double r = dist3(surface_point(s, M, Cc), Pk);
+            if (!isfinite(r)) continue;
+            int found = bs <= ORC_FOUND_AMBIGUOUS;
+            if (!found || (r < br - (1e-12 * br + 1e-14 * scale) && (fabs(Cc[0] - bu) > 1e-7 || fabs(Cc[1] - bv) > 1e-7))) {
+                bu = Cc[0]; bv = Cc[1]; br = r; bs = ORC_FOUND_UNIQUE;
+            }
+        }
+        uv[2 * i] = bu;
+        uv[2 * i + 1] = bv;
+        residual[i] = br;
+        status[i] = bs;
+    }
+    for (int64_t i = 0; i < n; ++i) {
+        int f = 0;
+        if (status[i] > ORC_FOUND_AMBIGUOUS) f |= 4;
+        if (status[i] == ORC_FOUND_AMBIGUOUS) f |= 2;
+        if (i > 0 && status[i] <= ORC_FOUND_AMBIGUOUS && status[i - 1] <= ORC_FOUND_AMBIGUOUS) {
+            span_loc L = locate(s, M, uv[2 * i], uv[2 * i + 1]);
+            d4 R = R_of(L.middle, s->degree_u, s->degree_v, L.u, L.v);
+            d3 Su = der_u(L.middle, s->degree_u, s->degree_v, L.u, L.v, R, L.spanU);
+            d3 Sv = der_v(L.middle, s->degree_u, s->degree_v, L.u, L.v, R, L.spanV);
+            double a = Su.x * Su.x + Su.y * Su.y + Su.z * Su.z, b = Su.x * Sv.x + Su.y * Sv.y + Su.z * Sv.z,
+                   c = Sv.x * Sv.x + Sv.y * Sv.y + Sv.z * Sv.z;
+            double m = 0.5 * (a + c), h = 0.5 * (a - c);
+            double lmin = m - sqrt(h * h + b * b);
+            double dx = C[3 * i] - C[3 * i - 3], dy = C[3 * i + 1] - C[3 * i - 2], dz = C[3 * i + 2] - C[3 * i - 1];
+            double chord = sqrt(dx * dx + dy * dy + dz * dz);
+            double du = uv[2 * i] - uv[2 * i - 2], dv = uv[2 * i + 1] - uv[2 * i - 1];
+            double step = sqrt(du * du + dv * dv);
+            if (!(lmin > 0) || step * sqrt(lmin) > 4.0 * chord + 1e-12) f |= 1;
+        }
+        flags[i] = f;
+    }
+    free(uv0);
+    free(st0);
+    free(r0);
+}

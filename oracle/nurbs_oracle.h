@@ -120,6 +120,14 @@ void orc_invert_fp32_explore(const orc_surface* s, const double* matrix_n, const
                              const unsigned char* built, const double* P, int64_t n, int max_iter, int pk,
                              double eps, double* uv, int* found, double* residual, int threads);
 
+/* p-curve of ordered curve samples C[3n] (the oracle of nurbs_pcurve): orc_invert of every
+ * sample, FP64 Newton steps from the neighbours' answers kept when strictly closer (or when the
+ * sample had none), flags (1 jump, 2 ambiguous, 4 not found).  uv[2n], status[n], residual[n],
+ * flags[n]. */
+void orc_pcurve(const orc_surface* s, const double* matrix_n, const orc_tree_node* tree,
+                const unsigned char* built, const double* C, int64_t n, int max_iter, double* uv,
+                int* status, double* residual, int* flags, int threads);
+
 /* The reference's GaussNewton exactly as shipped (kernel.cu:151-249): <= 10 steps,
  * success when |S-P| < max_edge before a step.  Returns 1 on success and writes uv. */
 int orc_gauss_newton_shipped(const orc_surface* s, const double* matrix_n, const double seed[2],

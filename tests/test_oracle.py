@@ -198,3 +198,19 @@ def test_parity_classifier_catches_planted_mistakes():
     res[j] = max(worst, ores[j])         # as far as the farthest: passes
     c = classify_inversion(uv, st, res, ouv, ost, ores, P, perturbed=pset)
     assert c["fail_unstable"] == 0
+
+
+def test_oracle_pcurve_recovers_a_loop_and_flags_a_jump():
+    """The oracle's p-curve: a loop on the 64x64 surface comes back to 1e-12 with no flags; a
+    second loop appended elsewhere is flagged as a jump at the junction only."""
+    from gpu_nurbs_gb300 import synth
+    o = O.OracleSurface(synth.surface_large())
+    t = np.linspace(0, 1, 801)
+    uv = np.stack([0.5 + 0.3 * np.cos(2 * np.pi * t), 0.5 + 0.2 * np.sin(4 * np.pi * t)], 1)
+    uv2 = np.stack([0.3 + 0.1 * np.cos(2 * np.pi * t[:200]), 0.7 + 0.1 * np.sin(2 * np.pi * t[:200])], 1)
+    both = np.concatenate([uv, uv2])
+    C = o.eval(both, 1).T.copy()
+    ruv, st, res, fl = o.pcurve(C)
+    assert np.all(st == O.FOUND_UNIQUE)
+    assert np.abs(ruv - both).max() <= 1e-12
+    assert fl[801] == 1 and np.count_nonzero(fl) == 1
