@@ -46,21 +46,34 @@ def test_pcurve_on_the_surface_matches_the_oracle(nurbs, precision):
 
 
 @pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "mixed"])
-def test_pcurve_near_the_surface_and_a_jump(nurbs, precision):
-    """Samples 1e-3 off the surface along the normal, then a second loop elsewhere appended: the
-    jump flag is set at the junction and nowhere else on the first loop, and every sample
-    matches the oracle's p-curve (parameters, status, residual, flags)."""
+def test_pcurve_near_the_surface(nurbs, precision):
+    """Samples 1e-3 off the 64x64 surface along the normal: every sample matches the oracle's
+    p-curve (parameters, status, residual, flags) and none is flagged."""
     from gpu_nurbs_gb300 import synth
     sf = synth.surface_large()
     s, o = nurbs.Surface(sf), O.OracleSurface(sf)
-    uv = np.concatenate([loop(1500), loop(500, 0.3, 0.7, 0.1, 0.1)])
+    uv = loop(3001)
     E = o.eval(uv, 7)
     C = synth.form_queries(E[0:3].T, E[3:6].T, E[6:9].T, np.full(len(uv), 1e-3))
     g = [x.cpu().numpy() for x in s.pcurve(T(C), precision)]
-    r = o.pcurve(C)
-    compare(g, r)
-    assert g[3][1500] & nurbs.PCURVE_JUMP
-    assert not np.any(g[3][1:1500] & nurbs.PCURVE_JUMP)
+    compare(g, o.pcurve(C))
+    assert np.count_nonzero(g[3]) == 0
+
+
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "mixed"])
+def test_pcurve_seam_jump(nurbs, precision):
+    """A curve around a closed tube crosses its seam (u = 1 meets u = 0): the parameter jumps
+    while the curve does not, and that sample alone carries the jump flag, as in the oracle."""
+    from test_oracle import tube
+    sf = tube()
+    s, o = nurbs.Surface(sf), O.OracleSurface(sf)
+    u = (0.3 + np.arange(300) / 250.0 + 0.5 / 250) % 1.0
+    uv = np.stack([u, np.full(300, 0.4)], 1)
+    C = o.eval(uv, 1).T.copy()
+    g = [x.cpu().numpy() for x in s.pcurve(T(C), precision)]
+    compare(g, o.pcurve(C))
+    wrap = int(np.nonzero(np.diff(u) < 0)[0][0]) + 1
+    assert g[3][wrap] & nurbs.PCURVE_JUMP and np.count_nonzero(g[3] & nurbs.PCURVE_JUMP) == 1
 
 
 def test_pcurve_continuation_repairs_a_sample(nurbs):

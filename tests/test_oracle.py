@@ -200,17 +200,37 @@ def test_parity_classifier_catches_planted_mistakes():
     assert c["fail_unstable"] == 0
 
 
+def tube(nu=12, nv=5):
+    """A bicubic tube: control rows on a circle whose first and last rows coincide, so the
+    surface closes (C0) where u = 0 meets u = 1 and a curve around it crosses that seam."""
+    from gpu_nurbs_gb300 import synth
+    a = 2 * np.pi * np.arange(nu) / (nu - 1)
+    x = np.repeat(np.cos(a), nv)
+    y = np.repeat(np.sin(a), nv)
+    z = np.tile(np.arange(nv) / (nv - 1), nu)
+    return dict(p=3, q=3, nu=nu, nv=nv, knots_u=synth.uniform_knots(3, nu), knots_v=synth.uniform_knots(3, nv),
+                cps=np.stack([x, y, z], 1), weights=np.ones(nu * nv))
+
+
 def test_oracle_pcurve_recovers_a_loop_and_flags_a_jump():
-    """The oracle's p-curve: a loop on the 64x64 surface comes back to 1e-12 with no flags; a
-    second loop appended elsewhere is flagged as a jump at the junction only."""
+    """The oracle's p-curve: a loop on the 64x64 surface comes back to 1e-12 with no flags; on a
+    tube, a curve around it crosses the seam u = 1 -> 0, where the parameter jumps although the
+    curve does not: flagged there and nowhere else."""
     from gpu_nurbs_gb300 import synth
     o = O.OracleSurface(synth.surface_large())
     t = np.linspace(0, 1, 801)
     uv = np.stack([0.5 + 0.3 * np.cos(2 * np.pi * t), 0.5 + 0.2 * np.sin(4 * np.pi * t)], 1)
-    uv2 = np.stack([0.3 + 0.1 * np.cos(2 * np.pi * t[:200]), 0.7 + 0.1 * np.sin(2 * np.pi * t[:200])], 1)
-    both = np.concatenate([uv, uv2])
-    C = o.eval(both, 1).T.copy()
+    C = o.eval(uv, 1).T.copy()
     ruv, st, res, fl = o.pcurve(C)
     assert np.all(st == O.FOUND_UNIQUE)
-    assert np.abs(ruv - both).max() <= 1e-12
-    assert fl[801] == 1 and np.count_nonzero(fl) == 1
+    assert np.abs(ruv - uv).max() <= 1e-12
+    assert np.count_nonzero(fl) == 0
+    ot = O.OracleSurface(tube())
+    u = (0.3 + np.arange(300) / 250.0 + 0.5 / 250) % 1.0
+    uvt = np.stack([u, np.full(300, 0.4)], 1)
+    Ct = ot.eval(uvt, 1).T.copy()
+    ruv, st, res, fl = ot.pcurve(Ct)
+    wrap = int(np.nonzero(np.diff(u) < 0)[0][0]) + 1
+    assert np.all(st <= O.FOUND_AMBIGUOUS)
+    assert fl[wrap] & 1 and np.count_nonzero(fl & 1) == 1
+    assert np.abs(ruv - uvt).max() <= 1e-10
