@@ -25,6 +25,8 @@ LIB_PATH = os.path.join(HERE, "libgpunurbs.so")
 OK = 0
 E_INVALID, E_CUDA, E_NOMEM, E_IO, E_PARSE, E_UNSUPPORTED, E_BUDGET, E_TIMEOUT, E_STATE = range(-1, -10, -1)
 S, SU, SV, SUU, SUV, SVV = 1, 2, 4, 8, 16, 32
+SUUU, SUUV, SUVV, SVVV = 64, 128, 256, 512
+N, NU, NV, NUU, NUV, NVV = 1, 2, 4, 8, 16, 32
 PREC_FP64, PREC_MIXED, PREC_FP32 = 0, 1, 2
 PCURVE_JUMP, PCURVE_AMBIGUOUS, PCURVE_NOT_FOUND = 1, 2, 4
 INV_FOUND, INV_AMBIGUOUS, INV_NO_CANDIDATE, INV_NOT_CONVERGED = 0, 1, 2, 3
@@ -90,6 +92,7 @@ SIGNATURES = {
     "nurbs_invert_host": (C.c_int, [_vp, _vp, _i64, _vp, _vp, _vp, C.c_int, _vp]),
     "nurbs_invert_count": (C.c_int, [_vp, _vp, _i64, C.c_int, _vp, _vp]),
     "nurbs_pcurve": (C.c_int, [_vp, _vp, _i64, _vp, _vp, _vp, _vp, C.c_int, _vp]),
+    "nurbs_eval_normal": (C.c_int, [_vp, _vp, _i64, C.c_uint, _vp, _vp]),
     "nurbs_probe_fp_peak": (C.c_int, [C.c_int, C.POINTER(C.c_double), _vp]),
     "nurbs_pool_create": (C.c_int, [_i64, C.c_int, C.POINTER(_vp)]),
     "nurbs_pool_destroy": (C.c_int, [_vp]),
@@ -252,16 +255,27 @@ class Surface:
         torch = _torch()
         uv = uv.contiguous()
         n = uv.shape[0]
-        nb = bin(mask & 63).count("1")
+        nb = bin(mask & 1023).count("1")
         out = torch.empty((3 * nb, n), dtype=torch.float64, device=uv.device)
         check(lib().nurbs_eval(self.h, _ptr(uv), n, mask, _ptr(out), PREC_FP64, _stream(stream)), "nurbs_eval")
+        return out
+
+    def eval_normal(self, uv, mask: int = N, stream=None):
+        """Normal N = Su x Sv and its derivatives (N, NU, NV, NUU, NUV, NVV bits) at uv ((n,2)
+        CUDA tensor) -> (3*nblocks, n) float64 SoA tensor."""
+        torch = _torch()
+        uv = uv.contiguous()
+        n = uv.shape[0]
+        nb = bin(mask & 63).count("1")
+        out = torch.empty((3 * nb, n), dtype=torch.float64, device=uv.device)
+        check(lib().nurbs_eval_normal(self.h, _ptr(uv), n, mask, _ptr(out), _stream(stream)), "nurbs_eval_normal")
         return out
 
     def eval_f32(self, uv, mask: int = S, stream=None):
         torch = _torch()
         uv = uv.contiguous()
         n = uv.shape[0]
-        nb = bin(mask & 63).count("1")
+        nb = bin(mask & 1023).count("1")
         out = torch.empty((3 * nb, n), dtype=torch.float32, device=uv.device)
         check(lib().nurbs_eval_f32(self.h, _ptr(uv), n, mask, _ptr(out), _stream(stream)), "nurbs_eval_f32")
         return out

@@ -298,7 +298,7 @@ int nurbs_eval(nurbs_surface_t s, const double* uv_dev, int64_t n, unsigned mask
                void* stream) {
   if (!s) return fail(NURBS_E_INVALID, "NULL surface");
   if (n < 0) return fail(NURBS_E_INVALID, "negative count");
-  if (mask == 0 || mask > 63u) return fail(NURBS_E_INVALID, "mask 0x%x outside 1..63", mask);
+  if (mask == 0 || mask > 1023u) return fail(NURBS_E_INVALID, "mask 0x%x outside 1..1023", mask);
   if (precision != NURBS_PREC_FP64) return fail(NURBS_E_INVALID, "nurbs_eval computes in FP64; use nurbs_eval_f32");
   if (n == 0) return NURBS_OK;
   if (!uv_dev || !out_dev) return fail(NURBS_E_INVALID, "NULL buffer");
@@ -309,10 +309,21 @@ int nurbs_eval(nurbs_surface_t s, const double* uv_dev, int64_t n, unsigned mask
 int nurbs_eval_f32(nurbs_surface_t s, const float* uv_dev, int64_t n, unsigned mask, float* out_dev, void* stream) {
   if (!s) return fail(NURBS_E_INVALID, "NULL surface");
   if (n < 0) return fail(NURBS_E_INVALID, "negative count");
-  if (mask == 0 || mask > 63u) return fail(NURBS_E_INVALID, "mask 0x%x outside 1..63", mask);
+  if (mask == 0 || mask > 1023u) return fail(NURBS_E_INVALID, "mask 0x%x outside 1..1023", mask);
   if (n == 0) return NURBS_OK;
   if (!uv_dev || !out_dev) return fail(NURBS_E_INVALID, "NULL buffer");
   CUDA_TRY(launch_eval_f32(s->dev, uv_dev, n, mask, out_dev, (cudaStream_t)stream), "eval launch");
+  return NURBS_OK;
+}
+
+int nurbs_eval_normal(nurbs_surface_t s, const double* uv_dev, int64_t n, unsigned mask, double* out_dev,
+                      void* stream) {
+  if (!s) return fail(NURBS_E_INVALID, "NULL surface");
+  if (n < 0) return fail(NURBS_E_INVALID, "negative count");
+  if (mask == 0 || mask > 63u) return fail(NURBS_E_INVALID, "normal mask 0x%x outside 1..63", mask);
+  if (n == 0) return NURBS_OK;
+  if (!uv_dev || !out_dev) return fail(NURBS_E_INVALID, "NULL buffer");
+  CUDA_TRY(launch_eval_normal(s->dev, uv_dev, n, mask, out_dev, (cudaStream_t)stream), "normal launch");
   return NURBS_OK;
 }
 

@@ -251,19 +251,24 @@ __device__ __forceinline__ void load_coef_pair(const double* m, int idx, v4<doub
   hi = load_coef(m, idx + 1);
 }
 
-// Horner accumulator tracking value and D derivatives (D <= 2).  Coefficients are pushed from
-// the highest power down; after all pushes p = f(x), dp = f'(x), ddp = f''(x)/2.  The first
-// two pushes are peeled so no FMA is spent on zero accumulators.
+// Horner accumulator tracking value and D derivatives (D <= 3).  Coefficients are pushed from
+// the highest power down; after all pushes p = f(x), dp = f'(x), ddp = f''(x)/2 and dddp = the
+// third derivative / 6.  The first pushes are peeled so no FMA is spent on zero accumulators.
 template <typename T, int D>
 struct Horner {
-  v4<T> p, dp, ddp;
+  v4<T> p, dp, ddp, dddp;
   int k;
-  // dp/ddp start at zero: a polynomial of degree < D has vanishing higher derivatives
-  GN_HD Horner() : dp{T(0), T(0), T(0), T(0)}, ddp{T(0), T(0), T(0), T(0)}, k(0) {}
+  // dp/ddp/dddp start at zero: a polynomial of degree < D has vanishing higher derivatives
+  GN_HD Horner()
+      : dp{T(0), T(0), T(0), T(0)}, ddp{T(0), T(0), T(0), T(0)}, dddp{T(0), T(0), T(0), T(0)}, k(0) {}
   GN_HD void push(const v4<T>& c, T x) {
     if (k == 0) {
       p = c;
     } else {
+      if (D >= 3) {
+        if (k == 3) dddp = ddp;
+        else if (k > 3) dddp = vmad(dddp, x, ddp);
+      }
       if (D >= 2) {
         if (k == 2) ddp = dp;
         else if (k > 2) ddp = vmad(ddp, x, dp);
@@ -288,7 +293,7 @@ GN_HD v4<T> zero4() {
 // P, Q > 0 fix the degrees at compile time; P = Q = 0 reads p, q at run time.
 template <typename T>
 struct RDer {
-  v4<T> R, Ru, Rv, Ruu, Ruv, Rvv;
+  v4<T> R, Ru, Rv, Ruu, Ruv, Rvv, Ruuu, Ruuv, Ruvv, Rvvv;
 };
 
 template <typename T, int P, int Q, int ORDER>
@@ -298,9 +303,11 @@ __device__ __forceinline__ RDer<T> span_contract(const T* __restrict__ m, int p_
   const int k2 = qq + 1;
   constexpr int DR = ORDER;                  // derivatives of the u-Horner over t_a
   constexpr int DV = ORDER >= 1 ? ORDER - 1 : 0;
+  constexpr int DVV = ORDER >= 2 ? ORDER - 2 : 0;
   Horner<T, DR> colR;
   Horner<T, DV> colV;
-  Horner<T, 0> colVV;
+  Horner<T, DVV> colVV;
+  Horner<T, 0> colVVV;
 #pragma unroll
   for (int a = (P > 0 ? P : kMaxDegree); a >= 0; --a) {
     if (P == 0 && a > pp) continue;
@@ -332,6 +339,7 @@ __device__ __forceinline__ RDer<T> span_contract(const T* __restrict__ m, int p_
     colR.push(row.p, u);
     if (ORDER >= 1) colV.push(row.dp, u);
     if (ORDER >= 2) colVV.push(row.ddp, u);
+    if (ORDER >= 3) colVVV.push(row.dddp, u);
   }
   RDer<T> o;
   o.R = colR.p;
@@ -344,13 +352,19 @@ __device__ __forceinline__ RDer<T> span_contract(const T* __restrict__ m, int p_
     o.Ruv = colV.dp;
     o.Rvv = {T(2) * colVV.p.x, T(2) * colVV.p.y, T(2) * colVV.p.z, T(2) * colVV.p.w};
   }
+  if (ORDER >= 3) {
+    o.Ruuu = {T(6) * colR.dddp.x, T(6) * colR.dddp.y, T(6) * colR.dddp.z, T(6) * colR.dddp.w};
+    o.Ruuv = {T(2) * colV.ddp.x, T(2) * colV.ddp.y, T(2) * colV.ddp.z, T(2) * colV.ddp.w};
+    o.Ruvv = {T(2) * colVV.dp.x, T(2) * colVV.dp.y, T(2) * colVV.dp.z, T(2) * colVV.dp.w};
+    o.Rvvv = {T(6) * colVVV.p.x, T(6) * colVVV.p.y, T(6) * colVVV.p.z, T(6) * colVVV.p.w};
+  }
   return o;
 }
 
 // Cartesian point and derivatives with respect to the global parameters.
 template <typename T>
 struct SDer {
-  v3<T> S, Su, Sv, Suu, Suv, Svv;
+  v3<T> S, Su, Sv, Suu, Suv, Svv, Suuu, Suuv, Suvv, Svvv;
 };
 
 template <typename T>
@@ -401,6 +415,35 @@ __device__ __forceinline__ SDer<T> quotient(const RDer<T>& d, T su, T sv) {
       o.Suu = {Auu.x * suu, Auu.y * suu, Auu.z * suu};
       o.Suv = {Auv.x * suv, Auv.y * suv, Auv.z * suv};
       o.Svv = {Avv.x * svv, Avv.y * svv, Avv.z * svv};
+      if (ORDER >= 3) {
+        // R = S h differentiated three times (the reference's UUV/UVV forms, Evaluate.cu:963-1020,
+        // carry two wrong signs; these are the quotient rule's):
+        //   S_uuu = (R_uuu - 3 h_u S_uu - 3 h_uu S_u - h_uuu S) / h
+        //   S_uuv = (R_uuv - h_v S_uu - 2 h_u S_uv - 2 h_uv S_u - h_uu S_v - h_uuv S) / h
+        const T huu = d.Ruu.w, huv = d.Ruv.w, hvv = d.Rvv.w;
+        const T hu3 = T(3) * hu, hv3 = T(3) * hv, huu3 = T(3) * huu, hvv3 = T(3) * hvv, huv2 = T(2) * huv;
+        auto c3 = [&](T r, T a2, T a1, T s, T k2, T k1, T k0) { return mad(-k0, s, mad(-k1, a1, mad(-k2, a2, r))) * ih; };
+        v3<T> Auuu = {c3(d.Ruuu.x, Auu.x, Au.x, o.S.x, hu3, huu3, d.Ruuu.w),
+                      c3(d.Ruuu.y, Auu.y, Au.y, o.S.y, hu3, huu3, d.Ruuu.w),
+                      c3(d.Ruuu.z, Auu.z, Au.z, o.S.z, hu3, huu3, d.Ruuu.w)};
+        v3<T> Avvv = {c3(d.Rvvv.x, Avv.x, Av.x, o.S.x, hv3, hvv3, d.Rvvv.w),
+                      c3(d.Rvvv.y, Avv.y, Av.y, o.S.y, hv3, hvv3, d.Rvvv.w),
+                      c3(d.Rvvv.z, Avv.z, Av.z, o.S.z, hv3, hvv3, d.Rvvv.w)};
+        auto c5 = [&](T r, T a_aa, T a_ab, T a_a, T a_b, T s, T hb, T ha2, T hab2, T haa, T h3w) {
+          return mad(-h3w, s, mad(-haa, a_b, mad(-hab2, a_a, mad(-ha2, a_ab, mad(-hb, a_aa, r))))) * ih;
+        };
+        v3<T> Auuv = {c5(d.Ruuv.x, Auu.x, Auv.x, Au.x, Av.x, o.S.x, hv, hu2, huv2, huu, d.Ruuv.w),
+                      c5(d.Ruuv.y, Auu.y, Auv.y, Au.y, Av.y, o.S.y, hv, hu2, huv2, huu, d.Ruuv.w),
+                      c5(d.Ruuv.z, Auu.z, Auv.z, Au.z, Av.z, o.S.z, hv, hu2, huv2, huu, d.Ruuv.w)};
+        v3<T> Auvv = {c5(d.Ruvv.x, Avv.x, Auv.x, Av.x, Au.x, o.S.x, hu, hv2, huv2, hvv, d.Ruvv.w),
+                      c5(d.Ruvv.y, Avv.y, Auv.y, Av.y, Au.y, o.S.y, hu, hv2, huv2, hvv, d.Ruvv.w),
+                      c5(d.Ruvv.z, Avv.z, Auv.z, Av.z, Au.z, o.S.z, hu, hv2, huv2, hvv, d.Ruvv.w)};
+        T suuu = suu * su, suuv = suu * sv, suvv = su * svv, svvv = svv * sv;
+        o.Suuu = {Auuu.x * suuu, Auuu.y * suuu, Auuu.z * suuu};
+        o.Suuv = {Auuv.x * suuv, Auuv.y * suuv, Auuv.z * suuv};
+        o.Suvv = {Auvv.x * suvv, Auvv.y * suvv, Auvv.z * suvv};
+        o.Svvv = {Avvv.x * svvv, Avvv.y * svvv, Avvv.z * svvv};
+      }
     }
     o.Su = {Au.x * su, Au.y * su, Au.z * su};
     o.Sv = {Av.x * sv, Av.y * sv, Av.z * sv};

@@ -48,6 +48,21 @@ extern "C" {
 #define NURBS_SUU  8u
 #define NURBS_SUV 16u
 #define NURBS_SVV 32u
+/* third order (MatrixSurfaceRd{UUU,UUV,UVV,VVV} + MatrixSurfaceDerivative{UUU,UUV,UVV,VVV},
+ * src/NURBS/Evaluate.cu:408-502, 963-1020; the reference's UUV/UVV quotient forms carry two wrong
+ * signs, these follow the quotient rule) */
+#define NURBS_SUUU  64u
+#define NURBS_SUUV 128u
+#define NURBS_SUVV 256u
+#define NURBS_SVVV 512u
+/* surface normal N = Su x Sv (not normalised, TrueNormal, src/NURBS/Evaluate.cu:1111-1117) and its
+ * derivatives, for nurbs_eval_normal */
+#define NURBS_N    1u
+#define NURBS_NU   2u
+#define NURBS_NV   4u
+#define NURBS_NUU  8u
+#define NURBS_NUV 16u
+#define NURBS_NVV 32u
 
 /* precision schedules */
 #define NURBS_PREC_FP64   0   /* every iteration and contraction in FP64 */
@@ -143,12 +158,18 @@ int nurbs_get_matrix_n_noalloc(double* matrix_n_dev, int degree_u, int degree_v,
 
 /* -------------------------------------------------------------- stage b: evaluation */
 /* Batched evaluation at n parameter pairs uv_dev[2n] (global parameters).  out_dev is SoA:
- * for each set bit of mask, in the order S,Su,Sv,Suu,Suv,Svv, three planes of n doubles.
+ * for each set bit of mask, in the order S,Su,Sv,Suu,Suv,Svv,Suuu,Suuv,Suvv,Svvv, three planes
+ * of n doubles.
  * Replaces MatrixSurfacePoint + MatrixSurfaceDerivative{U,V,UU,UV,VV}
  * (src/NURBS/Evaluate.cu:159-227, 535-930) driven per point as EvaluateRandom does
  * (:1023-1038).  precision NURBS_PREC_FP64 only (see nurbs_eval_f32). */
 int nurbs_eval(nurbs_surface_t s, const double* uv_dev, int64_t n, unsigned mask,
                double* out_dev, int precision, void* stream);
+/* Normal N = Su x Sv and its derivatives at n parameter pairs (FP64): for each set bit of mask
+ * (NURBS_N, NU, NV, NUU, NUV, NVV, in that order) three planes of n doubles.  The second
+ * derivatives are SurfaceNormalDerivative{UU,UV,VV} (src/NURBS/Evaluate.cu:1125-1135). */
+int nurbs_eval_normal(nurbs_surface_t s, const double* uv_dev, int64_t n, unsigned mask, double* out_dev,
+                      void* stream);
 /* FP32 variant: float (u,v) in, float SoA out, contraction of the FP32 span matrices. */
 int nurbs_eval_f32(nurbs_surface_t s, const float* uv_dev, int64_t n, unsigned mask,
                    float* out_dev, void* stream);

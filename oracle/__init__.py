@@ -74,6 +74,8 @@ def lib():
         L.orc_pcurve.restype = None
         L.orc_pcurve.argtypes = [C.POINTER(_Surf), _dp, _dp, _bp, _dp, C.c_int64, C.c_int, _dp, _ip, _dp, _ip,
                                  C.c_int]
+        L.orc_eval_normal.restype = None
+        L.orc_eval_normal.argtypes = [C.POINTER(_Surf), _dp, _dp, C.c_int64, C.c_uint, _dp, C.c_int]
         L.orc_gauss_newton_shipped.restype = C.c_int
         L.orc_gauss_newton_shipped.argtypes = [C.POINTER(_Surf), _dp, _dp, _dp, C.c_double, _dp]
         L.orc_find_span.restype = C.c_int
@@ -114,9 +116,17 @@ class OracleSurface:
     def eval(self, uv: np.ndarray, mask: int, threads: int = 0) -> np.ndarray:
         uv = np.ascontiguousarray(uv, dtype=np.float64).reshape(-1, 2)
         n = uv.shape[0]
-        nb = bin(mask & 63).count("1")
+        nb = bin(mask & 1023).count("1")
         out = np.empty(3 * nb * n, dtype=np.float64)
         lib().orc_eval(C.byref(self._s), self.matrix_n, uv, n, mask, out, threads)
+        return out.reshape(3 * nb, n)
+
+    def eval_normal(self, uv: np.ndarray, mask: int, threads: int = 0) -> np.ndarray:
+        uv = np.ascontiguousarray(uv, dtype=np.float64).reshape(-1, 2)
+        n = uv.shape[0]
+        nb = bin(mask & 63).count("1")
+        out = np.empty(3 * nb * n, dtype=np.float64)
+        lib().orc_eval_normal(C.byref(self._s), self.matrix_n, uv, n, mask, out, threads)
         return out.reshape(3 * nb, n)
 
     def tree(self):

@@ -349,6 +349,10 @@ static d3 cart(d4 R) {     /* homogenousToCartesian, src/util/ExtraMath.cu:3-5 *
     return o;
 }
 
+static d3 d3at(const double* a, int b) { d3 o = {a[3 * b], a[3 * b + 1], a[3 * b + 2]}; return o; }
+static d3 d3add(d3 a, d3 b) { d3 o = {a.x + b.x, a.y + b.y, a.z + b.z}; return o; }
+static d3 d3scale(double s, d3 a) { d3 o = {s * a.x, s * a.y, s * a.z}; return o; }
+
 void orc_eval(const orc_surface* s, const double* M, const double* uv, int64_t n, unsigned mask,
               double* out, int threads) {
     const int p = s->degree_u, q = s->degree_v;
@@ -362,7 +366,12 @@ void orc_eval(const orc_surface* s, const double* M, const double* uv, int64_t n
     for (int64_t k = 0; k < n; ++k) {
         span_loc L = locate(s, M, uv[2 * k], uv[2 * k + 1]);
         d4 R = R_of(L.middle, p, q, L.u, L.v);
-        d3 blk[6];
+        d3 blk[10];
+        if (mask & 0x3C0u) {
+            double d[30];
+            orc_ders3(s, M, uv[2 * k], uv[2 * k + 1], d);
+            for (int b3 = 6; b3 < 10; ++b3) blk[b3] = d3at(d, b3);
+        }
         if (mask & ORC_S) blk[0] = cart(R);
         if (mask & ORC_SU) blk[1] = der_u(L.middle, p, q, L.u, L.v, R, L.spanU);
         if (mask & ORC_SV) blk[2] = der_v(L.middle, p, q, L.u, L.v, R, L.spanV);
@@ -370,11 +379,135 @@ void orc_eval(const orc_surface* s, const double* M, const double* uv, int64_t n
         if (mask & ORC_SUV) blk[4] = der_uv(L.middle, p, q, L.u, L.v, R, L.spanU, L.spanV);
         if (mask & ORC_SVV) blk[5] = der_vv(L.middle, p, q, L.u, L.v, R, L.spanV);
         int o = 0;
-        for (int b = 0; b < 6; ++b) {
+        for (int b = 0; b < 10; ++b) {
             if (!((mask >> b) & 1u)) continue;
             out[(3 * o + 0) * n + k] = blk[b].x;
             out[(3 * o + 1) * n + k] = blk[b].y;
             out[(3 * o + 2) * n + k] = blk[b].z;
+            ++o;
+        }
+    }
+}
+
+
+/* ------------------------------------------- third order and normals (new-style quotient rule)
+ *
+ * The reference's projection code (src/kernel/kernel.cu:1386-1560, src/NURBS/Evaluate.cu:
+ * 288-502, 932-1020) forms every derivative from the homogeneous R-derivatives: power vectors
+ * and their derivatives (GetVector, kernel.cu:1386-1450: d^k vectors as (i+k)...(i+1) * U[i]),
+ * R^(a,b) = U^(a) . (M_c . V^(b)) scaled by spanU^a spanV^b (MatrixSurfaceRd*), then
+ * S = R.xyz / h and the quotient rule applied to derivatives already computed.  Its mixed third
+ * derivatives (Evaluate.cu:963-1020) add 2 h_uv S_u and h_uuv S where the rule subtracts them (the
+ * same defect as its new S_uv, D1); here the rule's signs:
+ *   S_uv  = (R_uv  - h_v S_u  - h_u S_v  - h_uv S) / h
+ *   S_uuv = (R_uuv - h_v S_uu - 2 h_u S_uv - 2 h_uv S_u - h_uu S_v - h_uuv S) / h
+ *   S_uvv = (R_uvv - h_u S_vv - 2 h_v S_uv - 2 h_uv S_v - h_vv S_u - h_uvv S) / h
+ * Normal N = S_u x S_v (getNormals, kernel.cu:1043-1058) and SurfaceNormalDerivative{UU,UV,VV}
+ * (Evaluate.cu:1125-1135); first derivatives N_u = S_uu x S_v + S_u x S_uv, N_v likewise. */
+
+static void vectors_k(double t, int k, double* V0, double* V1, double* V2, double* V3) {
+    double now = 1;
+    for (int i = 0; i < k; i++) { V0[i] = now; now *= t; }
+    V1[0] = 0;
+    for (int i = 0; i < k - 1; i++) V1[i + 1] = (i + 1) * V0[i];
+    V2[0] = 0;
+    if (k > 1) V2[1] = 0;
+    for (int i = 0; i < k - 2; i++) V2[i + 2] = (i + 2) * (i + 1) * V0[i];
+    V3[0] = 0;
+    if (k > 1) V3[1] = 0;
+    if (k > 2) V3[2] = 0;
+    for (int i = 0; i < k - 3; i++) V3[i + 3] = (i + 3) * (i + 2) * (i + 1) * V0[i];
+}
+
+static d4 rd(const double* middle, int k1, int k2, const double* vu, const double* vv) {
+    double tmp[4][8];
+    mv4(middle, k1, k2, vv, tmp);
+    return dot4(vu, k1, tmp);
+}
+static d4 d4s(d4 a, double s) { d4 o = {a.x * s, a.y * s, a.z * s, a.w * s}; return o; }
+static d3 cross3(d3 a, d3 b) {   /* cross_product, src/util/Matrix.cu:62-64 */
+    d3 o = {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+    return o;
+}
+
+/* S and its derivatives to third order at (uu, vv): out[0..9] = S, Su, Sv, Suu, Suv, Svv, Suuu,
+ * Suuv, Suvv, Svvv. */
+void orc_ders3(const orc_surface* s, const double* M, double uu, double vv, double out[30]) {
+    const int p = s->degree_u, q = s->degree_v, k1 = p + 1, k2 = q + 1;
+    span_loc L = locate(s, M, uu, vv);
+    double U[4][8], V[4][8];
+    vectors_k(L.u, k1, U[0], U[1], U[2], U[3]);
+    vectors_k(L.v, k2, V[0], V[1], V[2], V[3]);
+    const double su = L.spanU, sv = L.spanV;
+    d4 R = rd(L.middle, k1, k2, U[0], V[0]);
+    d4 Ru = d4s(rd(L.middle, k1, k2, U[1], V[0]), su);
+    d4 Rv = d4s(rd(L.middle, k1, k2, U[0], V[1]), sv);
+    d4 Ruu = d4s(d4s(rd(L.middle, k1, k2, U[2], V[0]), su), su);
+    d4 Ruv = d4s(d4s(rd(L.middle, k1, k2, U[1], V[1]), su), sv);
+    d4 Rvv = d4s(d4s(rd(L.middle, k1, k2, U[0], V[2]), sv), sv);
+    d4 Ruuu = d4s(d4s(d4s(rd(L.middle, k1, k2, U[3], V[0]), su), su), su);
+    d4 Ruuv = d4s(d4s(d4s(rd(L.middle, k1, k2, U[2], V[1]), su), su), sv);
+    d4 Ruvv = d4s(d4s(d4s(rd(L.middle, k1, k2, U[1], V[2]), su), sv), sv);
+    d4 Rvvv = d4s(d4s(d4s(rd(L.middle, k1, k2, U[0], V[3]), sv), sv), sv);
+    const double h = R.w, hu = Ru.w, hv = Rv.w, huu = Ruu.w, huv = Ruv.w, hvv = Rvv.w;
+    d3 S = cart(R), Su, Sv, Suu, Suv, Svv, Suuu, Suuv, Suvv, Svvv;
+#define ORC_Q(o, expr) do { double* oo = &(o).x; for (int c = 0; c < 3; ++c) oo[c] = (expr); } while (0)
+#define CMP(a) (((const double*)&(a))[c])
+    ORC_Q(Su, (CMP(Ru) - hu * CMP(S)) / h);
+    ORC_Q(Sv, (CMP(Rv) - hv * CMP(S)) / h);
+    ORC_Q(Suu, ((CMP(Ruu) - 2 * hu * CMP(Su)) - huu * CMP(S)) / h);
+    ORC_Q(Suv, (((CMP(Ruv) - hv * CMP(Su)) - hu * CMP(Sv)) - huv * CMP(S)) / h);
+    ORC_Q(Svv, ((CMP(Rvv) - 2 * hv * CMP(Sv)) - hvv * CMP(S)) / h);
+    ORC_Q(Suuu, (((CMP(Ruuu) - 3 * hu * CMP(Suu)) - 3 * huu * CMP(Su)) - Ruuu.w * CMP(S)) / h);
+    ORC_Q(Suuv, (((((CMP(Ruuv) - hv * CMP(Suu)) - 2 * hu * CMP(Suv)) - 2 * huv * CMP(Su)) - huu * CMP(Sv)) -
+                 Ruuv.w * CMP(S)) / h);
+    ORC_Q(Suvv, (((((CMP(Ruvv) - hu * CMP(Svv)) - 2 * hv * CMP(Suv)) - 2 * huv * CMP(Sv)) - hvv * CMP(Su)) -
+                 Ruvv.w * CMP(S)) / h);
+    ORC_Q(Svvv, (((CMP(Rvvv) - 3 * hv * CMP(Svv)) - 3 * hvv * CMP(Sv)) - Rvvv.w * CMP(S)) / h);
+#undef CMP
+#undef ORC_Q
+    const d3 all[10] = {S, Su, Sv, Suu, Suv, Svv, Suuu, Suuv, Suvv, Svvv};
+    for (int b = 0; b < 10; ++b) {
+        out[3 * b] = all[b].x;
+        out[3 * b + 1] = all[b].y;
+        out[3 * b + 2] = all[b].z;
+    }
+}
+
+
+/* N, N_u, N_v, N_uu, N_uv, N_vv from the third-order derivatives (see above). */
+void orc_normals(const orc_surface* s, const double* M, double uu, double vv, double out[18]) {
+    double d[30];
+    orc_ders3(s, M, uu, vv, d);
+    const d3 Su = d3at(d, 1), Sv = d3at(d, 2), Suu = d3at(d, 3), Suv = d3at(d, 4), Svv = d3at(d, 5);
+    const d3 Suuu = d3at(d, 6), Suuv = d3at(d, 7), Suvv = d3at(d, 8), Svvv = d3at(d, 9);
+    const d3 N[6] = {
+        cross3(Su, Sv),
+        d3add(cross3(Suu, Sv), cross3(Su, Suv)),
+        d3add(cross3(Suv, Sv), cross3(Su, Svv)),
+        d3add(d3add(cross3(Suuu, Sv), d3scale(2, cross3(Suu, Suv))), cross3(Su, Suuv)),
+        d3add(d3add(d3add(cross3(Suuv, Sv), cross3(Suu, Svv)), cross3(Suv, Suv)), cross3(Su, Suvv)),
+        d3add(d3add(cross3(Suvv, Sv), d3scale(2, cross3(Suv, Svv))), cross3(Su, Svvv))};
+    for (int b = 0; b < 6; ++b) {
+        out[3 * b] = N[b].x;
+        out[3 * b + 1] = N[b].y;
+        out[3 * b + 2] = N[b].z;
+    }
+}
+
+void orc_eval_normal(const orc_surface* s, const double* M, const double* uv, int64_t n, unsigned mask,
+                     double* out, int threads) {
+#ifdef _OPENMP
+    if (threads <= 0) threads = omp_get_max_threads();
+#pragma omp parallel for schedule(static) num_threads(threads)
+#endif
+    for (int64_t k = 0; k < n; ++k) {
+        double N[18];
+        orc_normals(s, M, uv[2 * k], uv[2 * k + 1], N);
+        int o = 0;
+        for (int b = 0; b < 6; ++b) {
+            if (!((mask >> b) & 1u)) continue;
+            for (int c = 0; c < 3; ++c) out[(3 * o + c) * n + k] = N[3 * b + c];
             ++o;
         }
     }

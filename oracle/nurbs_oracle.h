@@ -128,6 +128,15 @@ void orc_pcurve(const orc_surface* s, const double* matrix_n, const orc_tree_nod
                 const unsigned char* built, const double* C, int64_t n, int max_iter, double* uv,
                 int* status, double* residual, int* flags, int threads);
 
+/* S and derivatives to third order (out[30]: S, Su, Sv, Suu, Suv, Svv, Suuu, Suuv, Suvv, Svvv)
+ * and the normal N = Su x Sv with its first and second derivatives (out[18]) at one global
+ * parameter pair, from the homogeneous R-derivatives with the quotient rule's signs
+ * (nurbs_oracle.c); orc_eval_normal is the batched SoA form of nurbs_eval_normal. */
+void orc_ders3(const orc_surface* s, const double* matrix_n, double u, double v, double out[30]);
+void orc_normals(const orc_surface* s, const double* matrix_n, double u, double v, double out[18]);
+void orc_eval_normal(const orc_surface* s, const double* matrix_n, const double* uv, int64_t n, unsigned mask,
+                     double* out, int threads);
+
 /* The reference's GaussNewton exactly as shipped (kernel.cu:151-249): <= 10 steps,
  * success when |S-P| < max_edge before a step.  Returns 1 on success and writes uv. */
 int orc_gauss_newton_shipped(const orc_surface* s, const double* matrix_n, const double seed[2],

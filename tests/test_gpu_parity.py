@@ -261,6 +261,49 @@ def test_eval_f32_close(nurbs, cuda):
     assert max(errs[3:]) < 5e-3, errs
 
 
+def _block_errors(ev, ref):
+    """Max error per 3-row block relative to the block's largest reference norm."""
+    out = []
+    for b in range(ref.shape[0] // 3):
+        r = ref[3 * b:3 * b + 3]
+        x = ev[3 * b:3 * b + 3]
+        out.append(float(np.linalg.norm(x - r, axis=0).max() / max(np.linalg.norm(r, axis=0).max(), 1e-300)))
+    return out
+
+
+def _third_order_cases():
+    from gpu_nurbs_gb300 import synth
+    return {"large": synth.surface_large(), "quintic": synth.surface_quintic(n=24),
+            "rational": synth.surface_random(synth.Rng(77)), "model": surf_of(load_golden(MODEL_FILES[-1]))}
+
+
+@pytest.mark.parametrize("which", ["large", "quintic", "rational", "model"])
+def test_eval_third_order_and_normals(nurbs, cuda, which):
+    """Third derivatives (mask bits 64..512) and the normal with its derivatives against the
+    oracle's power-vector restatement, including the span boundaries and the domain corners:
+    within 1e-11 of each block's magnitude (the fast path contracts in Horner form)."""
+    surf = _third_order_cases()[which]
+    o = O.OracleSurface(surf)
+    rng = np.random.default_rng(9)
+    ku = np.unique(surf["knots_u"][surf["p"]:surf["nu"] + 1])
+    kv = np.unique(surf["knots_v"][surf["q"]:surf["nv"] + 1])
+    uv = rng.random((8192, 2)) * [ku[-1] - ku[0], kv[-1] - kv[0]] + [ku[0], kv[0]]
+    uv[:64, 0] = rng.choice(ku, 64)
+    uv[64:128, 1] = rng.choice(kv, 64)
+    uv[128:132] = [[ku[0], kv[0]], [ku[0], kv[-1]], [ku[-1], kv[0]], [ku[-1], kv[-1]]]
+    s = nurbs.Surface(surf)
+    ev = s.eval(T(uv, cuda), 1023).cpu().numpy()
+    ref = o.eval(uv, 1023)
+    errs = _block_errors(ev, ref)
+    assert max(errs) <= 1e-11, errs
+    part = s.eval(T(uv, cuda), 0b1010000000).cpu().numpy()
+    assert np.array_equal(part, ev[np.r_[21:24, 27:30]])
+    nv = s.eval_normal(T(uv, cuda), 63).cpu().numpy()
+    errs = _block_errors(nv, o.eval_normal(uv, 63))
+    assert max(errs) <= 1e-11, errs
+    assert np.array_equal(s.eval_normal(T(uv, cuda), 0b100100).cpu().numpy(), nv[np.r_[6:9, 15:18]])
+
+
 def test_invalid_arguments_return_status(nurbs, cuda):
     g = load_golden(MODEL_FILES[0])
     bad = surf_of(g)
@@ -279,7 +322,9 @@ def test_invalid_arguments_return_status(nurbs, cuda):
     with pytest.raises(nurbs.NurbsError):
         s.eval(uv, 0)
     with pytest.raises(nurbs.NurbsError):
-        s.eval(uv, 64)
+        s.eval(uv, 1024)
+    with pytest.raises(nurbs.NurbsError):
+        s.eval_normal(uv, 64)
     with pytest.raises(nurbs.NurbsError):
         s.invert(T(g["P"], cuda), precision=7)
     # empty batches are valid no-ops

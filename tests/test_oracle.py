@@ -234,3 +234,53 @@ def test_oracle_pcurve_recovers_a_loop_and_flags_a_jump():
     assert np.all(st <= O.FOUND_AMBIGUOUS)
     assert fl[wrap] & 1 and np.count_nonzero(fl & 1) == 1
     assert np.abs(ruv - uvt).max() <= 1e-10
+
+
+def _fd_sample(surf, n, seed):
+    rng = np.random.default_rng(seed)
+    return np.clip(rng.random((n, 2)), 0.02, 0.98)
+
+
+@pytest.mark.parametrize("kind", ["large", "quintic", "rational"])
+def test_oracle_third_derivatives_and_normals_against_differences(kind):
+    """Third derivatives (Suuu, Suuv, Suvv, Svvv) and the normal's derivatives against central
+    differences of the orders below them, away from span boundaries; and N = Su x Sv against the
+    first derivatives of the reference-order evaluation."""
+    from gpu_nurbs_gb300 import synth
+    if kind == "large":
+        surf = synth.surface_large()
+    elif kind == "quintic":
+        surf = synth.surface_quintic(n=16)
+    else:
+        surf = synth.surface_random(synth.Rng(77))
+    o = O.OracleSurface(surf)
+    ku = np.unique(surf["knots_u"])
+    kv = np.unique(surf["knots_v"])
+    uv = _fd_sample(surf, 400, 5)
+    h = 1e-6
+    # keep both sides of every difference inside one span
+    du = np.abs(uv[:, :1] - ku[None, :]).min(1)
+    dv = np.abs(uv[:, 1:] - kv[None, :]).min(1)
+    uv = uv[(du > 10 * h) & (dv > 10 * h)]
+    n = len(uv)
+    D3 = o.eval(uv, 0x3C0).reshape(4, 3, n)
+    D2 = lambda x: o.eval(x, 0x38).reshape(3, 3, n)  # noqa: E731  Suu, Suv, Svv
+    eu = np.array([h, 0.0])
+    ev = np.array([0.0, h])
+    dU = (D2(uv + eu) - D2(uv - eu)) / (2 * h)
+    dV = (D2(uv + ev) - D2(uv - ev)) / (2 * h)
+    scale = np.abs(D3).max() + np.abs(dU).max()
+    for got, fd in ((D3[0], dU[0]), (D3[1], dU[1]), (D3[1], dV[0]), (D3[2], dU[2]), (D3[2], dV[1]), (D3[3], dV[2])):
+        assert np.abs(got - fd).max() <= 1e-6 * scale
+    E = o.eval(uv, 6).reshape(2, 3, n)
+    N = o.eval_normal(uv, 63).reshape(6, 3, n)
+    assert np.abs(N[0] - np.cross(E[0].T, E[1].T).T).max() <= 1e-12 * np.abs(N[0]).max()
+    Nf = lambda x: o.eval_normal(x, 7).reshape(3, 3, n)  # noqa: E731  N, Nu, Nv
+    nU = (Nf(uv + eu) - Nf(uv - eu)) / (2 * h)
+    nV = (Nf(uv + ev) - Nf(uv - ev)) / (2 * h)
+    sc = np.abs(N).max()
+    for got, fd in ((N[1], nU[0]), (N[2], nV[0]), (N[3], nU[1]), (N[4], nU[2]), (N[4], nV[1]), (N[5], nV[2])):
+        assert np.abs(got - fd).max() <= 1e-6 * sc
+    # a mask selects blocks in order
+    sel = o.eval_normal(uv, 0b101000)
+    assert np.array_equal(sel, np.concatenate([N[3], N[5]]))
