@@ -92,6 +92,8 @@ SIGNATURES = {
     "nurbs_invert_host": (C.c_int, [_vp, _vp, _i64, _vp, _vp, _vp, C.c_int, _vp]),
     "nurbs_invert_count": (C.c_int, [_vp, _vp, _i64, C.c_int, _vp, _vp]),
     "nurbs_pcurve": (C.c_int, [_vp, _vp, _i64, _vp, _vp, _vp, _vp, C.c_int, _vp]),
+    "nurbs_project": (C.c_int, [_vp, _vp, _i64, _vp, _vp, _vp, _vp]),
+    "nurbs_normal_cones_export": (C.c_int, [_vp, _vp, _vp, _vp]),
     "nurbs_eval_normal": (C.c_int, [_vp, _vp, _i64, C.c_uint, _vp, _vp]),
     "nurbs_probe_fp_peak": (C.c_int, [C.c_int, C.POINTER(C.c_double), _vp]),
     "nurbs_pool_create": (C.c_int, [_i64, C.c_int, C.POINTER(_vp)]),
@@ -311,6 +313,32 @@ class Surface:
         check(lib().nurbs_invert(self.h, _ptr(P), n, _ptr(uv), _ptr(st), _ptr(res), precision, _stream(stream)),
               "nurbs_invert")
         return uv, st, res
+
+    def project(self, P, stream=None, out=None):
+        """Closest point over the closed domain (nurbs_project, FP64): P (n,3) float64 CUDA
+        tensor -> (uv (n,2), status (n,), residual (n,))."""
+        torch = _torch()
+        P = P.contiguous()
+        n = P.shape[0]
+        if out is None:
+            uv = torch.empty((n, 2), dtype=torch.float64, device=P.device)
+            st = torch.empty(n, dtype=torch.int32, device=P.device)
+            res = torch.empty(n, dtype=torch.float64, device=P.device)
+        else:
+            uv, st, res = out
+        check(lib().nurbs_project(self.h, _ptr(P), n, _ptr(uv), _ptr(st), _ptr(res), _stream(stream)),
+              "nurbs_project")
+        return uv, st, res
+
+    def normal_cones(self):
+        """The projection's culling data (nurbs_normal_cones_export): normal boxes (65, 6),
+        FP32 records (65, 20), lattice points (65, 81, 3)."""
+        nb = np.zeros((TREE_NODES, 6), np.float64)
+        cr = np.zeros((TREE_NODES, 20), np.float32)
+        lat = np.zeros((TREE_NODES, 81, 3), np.float32)
+        check(lib().nurbs_normal_cones_export(self.h, nb.ctypes.data, cr.ctypes.data, lat.ctypes.data),
+              "nurbs_normal_cones_export")
+        return nb, cr, lat
 
     def pcurve(self, C, precision: int = PREC_MIXED, stream=None):
         """p-curve of ordered curve samples C ((n,3) CUDA tensor): (uv (n,2), status, residual,

@@ -103,6 +103,7 @@ struct nurbs_surface_s {
 // Enqueues one inversion on `st`: waits for the previous user of the counter slot, zeroes the
 // counter, launches, marks the slot.  Inside a stream capture the slot is used without the
 // event handshake (capture cannot wait on work recorded outside it).
+// precision: NURBS_PREC_FP64 / MIXED for the inversion, -1 for the projection (FP64)
 static cudaError_t invert_on(nurbs_surface_s* s, const double* P, int64_t n, double* uv, int* status, double* res,
                              int precision, cudaStream_t st) {
   std::lock_guard<std::mutex> lk(s->mu);
@@ -121,7 +122,9 @@ static cudaError_t invert_on(nurbs_surface_s* s, const double* P, int64_t n, dou
     }
   }
   e = cudaMemsetAsync(s->counters + slot, 0, sizeof(unsigned), st);
-  if (e == cudaSuccess) e = launch_invert(s->dev, P, n, uv, status, res, precision, s->counters + slot, st);
+  if (e == cudaSuccess)
+    e = precision < 0 ? launch_project(s->dev, P, n, uv, status, res, s->counters + slot, st)
+                      : launch_invert(s->dev, P, n, uv, status, res, precision, s->counters + slot, st);
   if (e == cudaSuccess && !capturing) e = cudaEventRecord(s->done[slot], st);
   return e;
 }
@@ -206,6 +209,7 @@ int nurbs_surface_create(int p, int q, int nu, int nv, const double* knots_u, co
   if (e == cudaSuccess) e = launch_span_matrices(d, s->basis_u, s->basis_v, (double*)d.m64, (float*)d.m32, st);
   if (e == cudaSuccess) e = launch_tree(d, st);
   if (e == cudaSuccess) e = launch_centre_ders(d, st);
+  if (e == cudaSuccess) e = launch_cones(d, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // img must outlive the copy
   if (e != cudaSuccess) {
     cudaFree(s->arena);
@@ -346,6 +350,7 @@ int nurbs_build_tree(nurbs_surface_t s, int levels, void* stream) {
   cudaStream_t st = (cudaStream_t)stream;
   CUDA_TRY(launch_tree(s->dev, st), "tree launch");
   CUDA_TRY(launch_centre_ders(s->dev, st), "seed-centre derivatives");
+  CUDA_TRY(launch_cones(s->dev, st), "normal cones");
   CUDA_TRY(cudaStreamSynchronize(st), "tree sync");
   s->tree_built = true;
   return NURBS_OK;
@@ -357,6 +362,27 @@ int nurbs_tree_export(nurbs_surface_t s, double* nodes_host, unsigned char* divi
   CUDA_TRY(cudaMemcpy(nodes_host, s->dev.tree, kTreeNodes * sizeof(TreeNodeDev), cudaMemcpyDeviceToHost), "tree copy");
   CUDA_TRY(cudaMemcpy(divided_host, s->dev.divided, kTreeNodes, cudaMemcpyDeviceToHost), "divided copy");
   CUDA_TRY(cudaMemcpy(built_host, s->dev.built, kTreeNodes, cudaMemcpyDeviceToHost), "built copy");
+  return NURBS_OK;
+}
+
+int nurbs_normal_cones_export(nurbs_surface_t s, double* nbox_host, float* cone_host, float* lattice_host) {
+  if (!s || !nbox_host || !cone_host || !lattice_host) return fail(NURBS_E_INVALID, "NULL argument");
+  CUDA_TRY(cudaMemcpy(nbox_host, s->dev.nbox, kTreeNodes * 6 * sizeof(double), cudaMemcpyDeviceToHost), "cone copy");
+  CUDA_TRY(cudaMemcpy(cone_host, s->dev.cone, kTreeNodes * kConeStride * sizeof(float), cudaMemcpyDeviceToHost),
+           "cone copy");
+  CUDA_TRY(cudaMemcpy(lattice_host, s->dev.lattice, kTreeNodes * kPts * kPts * 3 * sizeof(float),
+                      cudaMemcpyDeviceToHost),
+           "lattice copy");
+  return NURBS_OK;
+}
+
+int nurbs_project(nurbs_surface_t s, const double* P_dev, int64_t n, double* uv_dev, int* status_dev,
+                  double* residual_dev, void* stream) {
+  if (!s) return fail(NURBS_E_INVALID, "NULL surface");
+  if (n < 0) return fail(NURBS_E_INVALID, "negative count");
+  if (n == 0) return NURBS_OK;
+  if (!P_dev || !uv_dev || !status_dev || !residual_dev) return fail(NURBS_E_INVALID, "NULL buffer");
+  CUDA_TRY(invert_on(s, P_dev, n, uv_dev, status_dev, residual_dev, -1, (cudaStream_t)stream), "project launch");
   return NURBS_OK;
 }
 

@@ -1,0 +1,347 @@
+// Point projection (nurbs_project): the closest point of the surface over its closed knot domain,
+// for query points near the surface or far from it.
+//
+// Replaces the reference's unfinished projection (Project, src/kernel/kernel.cu:471-485, a
+// <<<1,1>>> launch for one constant point; NormalBoundingBoxCheck :487-513; NormalBoundingBox
+// :623-704; NormalBoxToNormalTreeNode :1613-1636) with one fused persistent kernel:
+//   1. cull (FP32, relative to the control net's centre, the same operations and roundings as
+//      the oracle's cull, so both select the same nodes): the distance bound UB is the
+//      least distance from P to the 3x3 sub-lattice surface points of every built node; a node is
+//      a candidate when its bound box is within UB of P and its normal cone, taken with both
+//      signs, can face P from some point of the box's bounding ball;
+//   2. each candidate is seeded at its 9x9 lattice point closest to P and iterated with projected
+//      Newton steps and a line search inside the domain (the full Hessian J^T J + r.d2S where it
+//      is positive definite, J^T J elsewhere; a coordinate held at a bound whose descent points
+//      out of the domain, the other taking the 1-D step; every step halved until |S - P| does not
+//      grow), so minima on the boundary, where S - P is not normal to the surface, are found too;
+//   3. the converged results are merged into per-query records (grid cells of the domain, as in
+//      the inversion) and the closest wins; AMBIGUOUS when another minimum is as close.
+// The warp's (query, seed) pairs are flattened into a task list as in the FP64 inversion
+// (round-major), every lane pulling the next task when its seed ends.  FP64 throughout: the
+// iteration count per seed is small and its line search needs distances at full precision.
+#include "invert_core.cuh"
+
+namespace gnurbs {
+namespace {
+
+using namespace inv;
+
+constexpr int kMaxIterProj = 40;  // projected Newton iterations per seed (the oracle's cap)
+constexpr int kMaxHalvings = 30;  // line-search halvings per iteration
+constexpr int kLattice = kPts * kPts;
+
+struct ProjStaged {
+  float cone[kTreeNodes][kConeStride];
+  float sub[kTreeNodes][9][3];  // the 3x3 sub-lattice (1, 4, 7)^2 of every node
+};
+
+struct ProjWarp {
+  unsigned long long smask0[32];
+  unsigned char smask1[32];
+  unsigned srmask[kTreeNodes];
+  int srpref[kTreeNodes + 1];
+  unsigned char psub[32][kTreeNodes];  // seed lattice index of (query, node)
+  Rec64 rec[32];
+  double sp64[32][3];
+};
+
+__device__ __forceinline__ float fdot3(const float* a, const float* b) {
+  return (a[0] * b[0] + a[1] * b[1]) + a[2] * b[2];
+}
+__device__ __forceinline__ double clampd(double x, double lo, double hi) { return x < lo ? lo : (x > hi ? hi : x); }
+
+struct PSeed {
+  double u, v;
+  int it, hu, hv;
+};
+
+// One projected Newton iteration with its line search (see above).
+template <int P, int Q>
+__device__ __forceinline__ int project_iterate(const Ctx& c, double px, double py, double pz, PSeed& sd) {
+  fast::SDer<double> d = fast::eval_at<double, P, Q, 2>(c.L64, c.m64, c.p, c.q, sd.u, sd.v, sd.hu, sd.hv);
+  const v3<double> r = {d.S.x - px, d.S.y - py, d.S.z - pz};
+  const double f = dot3(r, r);
+  const double g0 = dot3(d.Su, r), g1 = dot3(d.Sv, r);
+  const double a00 = dot3(d.Su, d.Su), a01 = dot3(d.Su, d.Sv), a11 = dot3(d.Sv, d.Sv);
+  const double n00 = a00 + dot3(r, d.Suu), n01 = a01 + dot3(r, d.Suv), n11 = a11 + dot3(r, d.Svv);
+  const bool fu = !((sd.u <= c.dom_u0 && g0 > 0) || (sd.u >= c.dom_u1 && g0 < 0));
+  const bool fv = !((sd.v <= c.dom_v0 && g1 > 0) || (sd.v >= c.dom_v1 && g1 < 0));
+  double d0 = 0, d1 = 0;
+  bool newton;
+  if (fu && fv) {
+    newton = n00 > 0 && det2(n00, n01, n11) > 0;
+    const double h00 = newton ? n00 : a00, h01 = newton ? n01 : a01, h11 = newton ? n11 : a11;
+    const double det = det2(h00, h01, h11);
+    if (!(det > 0)) return kFailed;
+    d0 = fast::mad(h11, g0, -(h01 * g1)) / det;
+    d1 = fast::mad(h00, g1, -(h01 * g0)) / det;
+  } else if (fu) {
+    newton = n00 > 0;
+    const double h = newton ? n00 : a00;
+    if (!(h > 0)) return kFailed;
+    d0 = g0 / h;
+  } else if (fv) {
+    newton = n11 > 0;
+    const double h = newton ? n11 : a11;
+    if (!(h > 0)) return kFailed;
+    d1 = g1 / h;
+  } else {
+    return kConverged;  // a corner where the distance grows into the domain
+  }
+  if (!(isfinite(d0) && isfinite(d1))) return kFailed;
+  double alpha = 1, un, vn;
+  for (int ls = 0;; ++ls) {
+    un = clampd(sd.u - alpha * d0, c.dom_u0, c.dom_u1);
+    vn = clampd(sd.v - alpha * d1, c.dom_v0, c.dom_v1);
+    int hu = sd.hu, hv = sd.hv;
+    fast::SDer<double> e = fast::eval_at<double, P, Q, 0>(c.L64, c.m64, c.p, c.q, un, vn, hu, hv);
+    const v3<double> rn = {e.S.x - px, e.S.y - py, e.S.z - pz};
+    if (dot3(rn, rn) <= f || ls == kMaxHalvings) break;
+    alpha *= 0.5;
+  }
+  const double moved = fmax(fabs(un - sd.u), fabs(vn - sd.v));
+  sd.u = un;
+  sd.v = vn;
+  if (moved <= kTolAny64 || (newton && moved <= kTolNewton64)) return kConverged;
+  if (++sd.it >= kMaxIterProj) return kFailed;
+  return kContinue;
+}
+
+// One warp projects the queries [q0, min(q0+32, qend)).
+template <int P, int Q>
+__device__ __forceinline__ void project_chunk(const Staged<kSmemSpans, kModeFP64>& sm, const ProjStaged& ps,
+                                              const float* __restrict__ lattice, ProjWarp& ww, const Ctx& cx,
+                                              const double* __restrict__ Pq, int64_t q0, int64_t qend,
+                                              double* __restrict__ uv_out, int* __restrict__ st_out,
+                                              double* __restrict__ res_out) {
+  const int lane = threadIdx.x & 31;
+  const unsigned FULL = 0xffffffffu;
+  const unsigned lt_mask = (1u << lane) - 1u;
+  const int nbl = sm.nb;
+  const int64_t q = q0 + lane;
+  const bool valid = q < qend;
+  double px = 0, py = 0, pz = 0;
+  if (valid) {
+    px = Pq[3 * q];
+    py = Pq[3 * q + 1];
+    pz = Pq[3 * q + 2];
+  }
+  // ---- cull (the oracle's arithmetic, operation for operation)
+  uint64_t m0 = 0;
+  unsigned m1 = 0;
+  if (valid) {
+    const float Pf[3] = {(float)(px - sm.org[0]), (float)(py - sm.org[1]), (float)(pz - sm.org[2])};
+    float ub2 = INFINITY;
+    for (int k = 0; k < nbl; ++k)
+      for (int j = 0; j < 9; ++j) {
+        const float dd3[3] = {ps.sub[k][j][0] - Pf[0], ps.sub[k][j][1] - Pf[1], ps.sub[k][j][2] - Pf[2]};
+        const float dd = fdot3(dd3, dd3);
+        ub2 = ub2 < dd ? ub2 : dd;
+      }
+    ub2 = ub2 * (1.0f + 0x1p-10f);
+    for (int k = 0; k < nbl; ++k) {
+      const float* rc = ps.cone[k];
+      float g[3];
+      for (int c = 0; c < 3; ++c) {
+        const float lo = rc[9 + c] - Pf[c], hi = Pf[c] - rc[12 + c];
+        g[c] = lo > hi ? lo : hi;
+        g[c] = g[c] > 0.0f ? g[c] : 0.0f;
+      }
+      const bool nearb = fdot3(g, g) <= ub2;
+      const float dv[3] = {Pf[0] - rc[0], Pf[1] - rc[1], Pf[2] - rc[2]};
+      const float dd = fdot3(dv, dv), r = rc[3];
+      float e = dd - r * r;
+      e = e > 0.0f ? e : 0.0f;
+      const bool seen = rc[7] * sqrtf(e) <= fabsf(fdot3(dv, rc + 4)) + rc[8] * r;
+      if (nearb && seen) {
+        // seed: the node's lattice point closest to P (first of equals)
+        const float* L = lattice + (size_t)k * kLattice * 3;
+        float best = INFINITY;
+        int bi = 0;
+        for (int j = 0; j < kLattice; ++j) {
+          const float x[3] = {__ldg(L + 3 * j) - Pf[0], __ldg(L + 3 * j + 1) - Pf[1], __ldg(L + 3 * j + 2) - Pf[2]};
+          const float ee = fdot3(x, x);
+          if (ee < best) {
+            best = ee;
+            bi = j;
+          }
+        }
+        ww.psub[lane][k] = (unsigned char)bi;
+        if (k < 64) m0 |= 1ull << k;
+        else m1 = 1u;
+      }
+    }
+  }
+  const int cnt = __popcll(m0) + (int)m1;
+  // round-major task list: round r holds seed r of every query with more than r seeds
+  const int maxc = __reduce_max_sync(FULL, (unsigned)cnt);
+  int total = 0;
+  for (int r = 0; r < maxc; ++r) {
+    unsigned m = __ballot_sync(FULL, cnt > r);
+    if (lane == 0) {
+      ww.srmask[r] = m;
+      ww.srpref[r] = total;
+    }
+    total += __popc(m);
+  }
+  if (lane == 0) ww.srpref[maxc] = total;
+  ww.sp64[lane][0] = px;
+  ww.sp64[lane][1] = py;
+  ww.sp64[lane][2] = pz;
+  ww.smask0[lane] = m0;
+  ww.smask1[lane] = (unsigned char)m1;
+  ww.rec[lane].n = 0;
+  __syncwarp();
+
+  auto decode = [&](int t, int& ql, int& node) {
+    int r = 0;
+#pragma unroll
+    for (int step = 64; step > 0; step >>= 1)
+      if (r + step < maxc && ww.srpref[r + step] <= t) r += step;
+    const unsigned m = ww.srmask[r];
+    int i = t - ww.srpref[r], pos = 0;
+#pragma unroll
+    for (int w = 16; w > 0; w >>= 1)
+      if (__popc(m & ((1u << (pos + w)) - 1u)) <= i) pos += w;
+    ql = pos;
+    const uint64_t mm = ww.smask0[ql];
+    node = r < __popcll(mm) ? select_bit(mm, r) : 64;
+  };
+
+  int next = 32;
+  int task = lane;
+  bool active = task < total;
+  int ql = 0, node = 0;
+  PSeed sd;
+  double tx = 0, ty = 0, tz = 0;
+  auto start = [&]() {
+    decode(task, ql, node);
+    tx = ww.sp64[ql][0];
+    ty = ww.sp64[ql][1];
+    tz = ww.sp64[ql][2];
+    // the lattice point's parameters, as the samples compute them
+    const int j = ww.psub[ql][node];
+    const unsigned g = node == 0 ? 1u : (unsigned)kGap;
+    const unsigned bx = node == 0 ? 0u : (unsigned)(node - 1) / kGap, by = node == 0 ? 0u : (unsigned)(node - 1) % kGap;
+    const double base_unit = 1.0 / g, unit = base_unit / kGap;
+    sd.u = clampd(base_unit * bx + (j / kPts) * unit, cx.dom_u0, cx.dom_u1);
+    sd.v = clampd(base_unit * by + (j % kPts) * unit, cx.dom_v0, cx.dom_v1);
+    sd.it = 0;
+    sd.hu = 0;
+    sd.hv = 0;
+  };
+  if (active) start();
+  while (__any_sync(FULL, active)) {
+    int res = kContinue;
+    double rr = 0;
+    bool keep = false;
+    if (active) {
+      res = project_iterate<P, Q>(cx, tx, ty, tz, sd);
+      if (res == kConverged) keep = finish64<P, Q>(cx, tx, ty, tz, sd.u, sd.v, sd.hu, sd.hv, rr);
+    }
+    const bool done = active && res != kContinue;
+    __syncwarp();
+    int cu = 0, cv = 0;
+    if (done && keep) cell_of(sm.cell64, sd.u, sd.v, cu, cv);
+    unsigned fm = __ballot_sync(FULL, done && keep);
+    while (fm) {
+      const int j = __ffs(fm) - 1;
+      if (lane == j) merge64(ww.rec[ql], cu, cv, sd.u, sd.v, rr);
+      __syncwarp();
+      fm &= fm - 1;
+    }
+    const unsigned dm = __ballot_sync(FULL, done);
+    if (done) {
+      task = next + __popc(dm & lt_mask);
+      active = task < total;
+      if (active) start();
+    }
+    next += __popc(dm);
+  }
+  __syncwarp();
+  int status;
+  double ou = __longlong_as_double(0x7ff8000000000000ll), ov = ou, orr = ou;
+  const Rec64& R = ww.rec[lane];
+  if (cnt == 0) status = 2;  // NURBS_INV_NO_CANDIDATE (non-finite P)
+  else status = R.n == 0 ? 3 : finish_status(R.u, R.v, R.r, R.n, 2.0 / sm.cell64.iu, 2.0 / sm.cell64.iv, ou, ov, orr);
+  if (valid) {
+    uv_out[2 * q] = ou;
+    uv_out[2 * q + 1] = ov;
+    st_out[q] = status;
+    res_out[q] = orr;
+  }
+  __syncwarp();
+}
+
+// Shared memory (dynamic, above the 48 KB of static allocations): the staged surface, the cone
+// records and sub-lattice points, and the warps' bookkeeping.
+constexpr size_t kOffPs = (sizeof(Staged<kSmemSpans, kModeFP64>) + 15) / 16 * 16;
+constexpr size_t kOffWw = kOffPs + (sizeof(ProjStaged) + 15) / 16 * 16;
+constexpr size_t kProjSmem = kOffWw + sizeof(ProjWarp) * kWarps;
+
+template <int P, int Q>
+__global__ void __launch_bounds__(kThreads, 3)
+    k_project(SurfDev s, const double* __restrict__ Pq, int64_t n, double* __restrict__ uv_out,
+              int* __restrict__ st_out, double* __restrict__ res_out, unsigned* __restrict__ counter) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  Staged<kSmemSpans, kModeFP64>& sm = *reinterpret_cast<Staged<kSmemSpans, kModeFP64>*>(smem);
+  ProjStaged& ps = *reinterpret_cast<ProjStaged*>(smem + kOffPs);
+  ProjWarp* ww = reinterpret_cast<ProjWarp*>(smem + kOffWw);
+  Ctx cx;
+  stage_surface<kSmemSpans>(s, sm, cx, threadIdx.x, blockDim.x);
+  for (int e = threadIdx.x; e < kTreeNodes * kConeStride; e += blockDim.x)
+    ps.cone[e / kConeStride][e % kConeStride] = s.cone[e];
+  for (int e = threadIdx.x; e < kTreeNodes * 9; e += blockDim.x) {
+    const int k = e / 9, j = e % 9, a = 1 + 3 * (j / 3), b = 1 + 3 * (j % 3);
+    const float* x = s.lattice + ((size_t)k * kLattice + kPts * a + b) * 3;
+    ps.sub[k][j][0] = x[0];
+    ps.sub[k][j][1] = x[1];
+    ps.sub[k][j][2] = x[2];
+  }
+  __syncthreads();
+  const int warp = threadIdx.x >> 5;
+  const int64_t units = (n + 31) / 32;
+  for (;;) {
+    unsigned ch = 0;
+    if ((threadIdx.x & 31) == 0) ch = atomicAdd(counter, 1u);
+    ch = __shfl_sync(0xffffffffu, ch, 0);
+    if ((int64_t)ch >= units) break;
+    const int64_t q0 = (int64_t)ch * 32;
+    project_chunk<P, Q>(sm, ps, s.lattice, ww[warp], cx, Pq, q0, min(q0 + 32, n), uv_out, st_out, res_out);
+  }
+}
+
+template <int P, int Q>
+cudaError_t launch_project_pq(const SurfDev& s, const double* P_, int64_t n, double* uv, int* st_, double* res,
+                              unsigned* counter, cudaStream_t st) {
+  const int64_t chunks = (n + 31) / 32;
+  if (chunks > 0x3fffffffLL) return cudaErrorInvalidValue;  // chunk ids are 32-bit
+  static int cached[64] = {0};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) dev = 0;
+  if (!cached[dev]) {
+    cudaError_t e = cudaFuncSetAttribute(k_project<P, Q>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kProjSmem);
+    if (e != cudaSuccess) return e;
+    int sms = 0, per_sm = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_project<P, Q>, kThreads, kProjSmem);
+    cached[dev] = (sms > 0 ? sms : 1) * (per_sm > 0 ? per_sm : 1);
+  }
+  int64_t blocks = (chunks + kWarps - 1) / kWarps;
+  if (blocks > cached[dev]) blocks = cached[dev];
+  k_project<P, Q><<<(unsigned)blocks, kThreads, kProjSmem, st>>>(s, P_, n, uv, st_, res, counter);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_project(const SurfDev& s, const double* P, int64_t n, double* uv, int* status, double* residual,
+                           unsigned* counter, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  if (s.p == 3 && s.q == 3) return launch_project_pq<3, 3>(s, P, n, uv, status, residual, counter, st);
+  if (s.p == 5 && s.q == 5) return launch_project_pq<5, 5>(s, P, n, uv, status, residual, counter, st);
+  return launch_project_pq<0, 0>(s, P, n, uv, status, residual, counter, st);
+}
+
+}  // namespace gnurbs

@@ -16,6 +16,7 @@ __host__ __device__ inline int span_coefs32(int p, int q) {
 }
 constexpr int kGap = 8;           // GapPerEdge (src/kernel/kernel.cuh:17)
 constexpr int kPts = kGap + 1;    // PointsPerEdge
+constexpr int kConeStride = 20;   // floats per normal-cone record
 
 // Device view of one surface.  All pointers are device pointers into the surface's arena.
 //
@@ -33,6 +34,14 @@ constexpr int kPts = kGap + 1;    // PointsPerEdge
 //   tree[65]                         TreeNodeDev; divided[65], built[65]
 //   cd32[65][9], cd64[65][9]         S, Su, Sv at every built node's uv-centre (the inversion seeds),
 //                                    FP32 (relative to org) and FP64, written after the tree
+//   nbox[65][6]                      normal boxes (lb xyz, rt xyz) of the built nodes
+//   cone[65][kConeStride]            FP32 projection culling record of each built node, relative to
+//                                    org: bound-box ball centre (0..2) and radius (3), normal-cone
+//                                    axis (4..6), cos and sin of its half-angle (7, 8; 0 and 1 for
+//                                    every direction), bound box rounded outward (lb 9..11,
+//                                    rt 12..14), zero (15..19)
+//   lattice[65][81][3]               surface points of each node's 9x9 lattice (index 9 tx + ty),
+//                                    FP32 relative to org: distance bounds and projection seeds
 struct SurfDev {
   int p, q, nu, nv;
   int ns_u, ns_v;
@@ -64,6 +73,9 @@ struct SurfDev {
   double* basis_v;
   float* cd32;            // seed-centre derivatives (see above)
   double* cd64;
+  double* nbox;           // normal cones (see above)
+  float* cone;
+  float* lattice;
 };
 
 // Tree node in the reference TreeNode order (src/kernel/kernel.cuh:30-39), 80 bytes.
@@ -132,6 +144,11 @@ cudaError_t launch_invert(const SurfDev& s, const double* P, int64_t n, double* 
 cudaError_t launch_pcurve_passes(const SurfDev& s, const double* C, int64_t n, const double* uv0, const int* st0,
                                  const double* res0, double* uv, int* st, double* res, int* flags,
                                  cudaStream_t stream);
+// normal cones, bound boxes and lattice points of the built nodes (after the tree and the span tables)
+cudaError_t launch_cones(const SurfDev& s, cudaStream_t st);
+// the projection: closest point over the closed domain (k_project.cu)
+cudaError_t launch_project(const SurfDev& s, const double* P, int64_t n, double* uv, int* status,
+                           double* residual, unsigned* counter, cudaStream_t st);
 // S, Su, Sv at the built nodes' uv-centres (cd32/cd64), after the tree is built
 cudaError_t launch_centre_ders(const SurfDev& s, cudaStream_t st);
 cudaError_t launch_centre_ders_batched(const SurfDev* table, const int* ids, int count, cudaStream_t st);

@@ -198,6 +198,88 @@ GN_HD v3<double> der_vv(const Acc& M, int p, int q, double u, double v, v4<doubl
           ((R.z * s1 + (2 * RdV.z) * s2) + RdVV.z / h) * spanV * spanV};
 }
 
+// ---- third order and normals in the new-style quotient rule (the normal-cone build)
+// Power vectors and their derivatives (GetVector, src/kernel/kernel.cu:1386-1450), R-derivatives
+// as U^(a) . (M_c . V^(b)) scaled by spanU^a spanV^b, S = R.xyz / h and the quotient rule with
+// its signs (the reference's mixed third derivatives, Evaluate.cu:963-1020, add two of the terms
+// they subtract).  Term order as written, so the normal cones are bit-identical to the oracle's.
+GN_HD void vectors_k(double t, int k, double* V0, double* V1, double* V2, double* V3) {
+  double now = 1;
+  for (int i = 0; i < k; i++) {
+    V0[i] = now;
+    now *= t;
+  }
+  V1[0] = 0;
+  for (int i = 0; i < k - 1; i++) V1[i + 1] = (i + 1) * V0[i];
+  V2[0] = 0;
+  if (k > 1) V2[1] = 0;
+  for (int i = 0; i < k - 2; i++) V2[i + 2] = (i + 2) * (i + 1) * V0[i];
+  V3[0] = 0;
+  if (k > 1) V3[1] = 0;
+  if (k > 2) V3[2] = 0;
+  for (int i = 0; i < k - 3; i++) V3[i + 3] = (i + 3) * (i + 2) * (i + 1) * V0[i];
+}
+template <class Acc>
+GN_HD v4<double> rd(const Acc& M, int k1, int k2, const double* vu, const double* vv) {
+  double tmp[4][kMaxDegree + 1];
+  mv(M, k1, k2, vv, tmp);
+  return dot4(vu, tmp, k1);
+}
+GN_HD v4<double> scale4(v4<double> a, double s) { return {a.x * s, a.y * s, a.z * s, a.w * s}; }
+GN_HD v3<double> cross(v3<double> a, v3<double> b) {  // cross_product, src/util/Matrix.cu:62-64
+  return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+GN_HD v3<double> add(v3<double> a, v3<double> b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+GN_HD v3<double> twice(v3<double> a) { return {2 * a.x, 2 * a.y, 2 * a.z}; }
+
+// d[0..9] = S, Su, Sv, Suu, Suv, Svv, Suuu, Suuv, Suvv, Svvv at local (u, v) of span M.
+template <class Acc>
+GN_HD void ders3(const Acc& M, int p, int q, double u, double v, double su, double sv, v3<double>* d) {
+  const int k1 = p + 1, k2 = q + 1;
+  double U[4][kMaxDegree + 1], V[4][kMaxDegree + 1];
+  vectors_k(u, k1, U[0], U[1], U[2], U[3]);
+  vectors_k(v, k2, V[0], V[1], V[2], V[3]);
+  const v4<double> R = rd(M, k1, k2, U[0], V[0]);
+  const v4<double> Ru = scale4(rd(M, k1, k2, U[1], V[0]), su);
+  const v4<double> Rv = scale4(rd(M, k1, k2, U[0], V[1]), sv);
+  const v4<double> Ruu = scale4(scale4(rd(M, k1, k2, U[2], V[0]), su), su);
+  const v4<double> Ruv = scale4(scale4(rd(M, k1, k2, U[1], V[1]), su), sv);
+  const v4<double> Rvv = scale4(scale4(rd(M, k1, k2, U[0], V[2]), sv), sv);
+  const v4<double> Ruuu = scale4(scale4(scale4(rd(M, k1, k2, U[3], V[0]), su), su), su);
+  const v4<double> Ruuv = scale4(scale4(scale4(rd(M, k1, k2, U[2], V[1]), su), su), sv);
+  const v4<double> Ruvv = scale4(scale4(scale4(rd(M, k1, k2, U[1], V[2]), su), sv), sv);
+  const v4<double> Rvvv = scale4(scale4(scale4(rd(M, k1, k2, U[0], V[3]), sv), sv), sv);
+  const double h = R.w, hu = Ru.w, hv = Rv.w, huu = Ruu.w, huv = Ruv.w, hvv = Rvv.w;
+  const double Rs[10][3] = {{R.x, R.y, R.z},          {Ru.x, Ru.y, Ru.z},       {Rv.x, Rv.y, Rv.z},
+                            {Ruu.x, Ruu.y, Ruu.z},    {Ruv.x, Ruv.y, Ruv.z},    {Rvv.x, Rvv.y, Rvv.z},
+                            {Ruuu.x, Ruuu.y, Ruuu.z}, {Ruuv.x, Ruuv.y, Ruuv.z}, {Ruvv.x, Ruvv.y, Ruvv.z},
+                            {Rvvv.x, Rvvv.y, Rvvv.z}};
+  double o[10][3];
+  for (int c = 0; c < 3; ++c) {
+    o[0][c] = Rs[0][c] / h;
+    o[1][c] = (Rs[1][c] - hu * o[0][c]) / h;
+    o[2][c] = (Rs[2][c] - hv * o[0][c]) / h;
+    o[3][c] = ((Rs[3][c] - 2 * hu * o[1][c]) - huu * o[0][c]) / h;
+    o[4][c] = (((Rs[4][c] - hv * o[1][c]) - hu * o[2][c]) - huv * o[0][c]) / h;
+    o[5][c] = ((Rs[5][c] - 2 * hv * o[2][c]) - hvv * o[0][c]) / h;
+    o[6][c] = (((Rs[6][c] - 3 * hu * o[3][c]) - 3 * huu * o[1][c]) - Ruuu.w * o[0][c]) / h;
+    o[7][c] = (((((Rs[7][c] - hv * o[3][c]) - 2 * hu * o[4][c]) - 2 * huv * o[1][c]) - huu * o[2][c]) -
+               Ruuv.w * o[0][c]) / h;
+    o[8][c] = (((((Rs[8][c] - hu * o[5][c]) - 2 * hv * o[4][c]) - 2 * huv * o[2][c]) - hvv * o[1][c]) -
+               Ruvv.w * o[0][c]) / h;
+    o[9][c] = (((Rs[9][c] - 3 * hv * o[5][c]) - 3 * hvv * o[2][c]) - Rvvv.w * o[0][c]) / h;
+  }
+  for (int b = 0; b < 10; ++b) d[b] = {o[b][0], o[b][1], o[b][2]};
+}
+
+// N = Su x Sv and N_uu, N_uv, N_vv (n[0..3]) from ders3's d.
+GN_HD void normal_ders2(const v3<double>* d, v3<double>* n) {
+  n[0] = cross(d[1], d[2]);
+  n[1] = add(add(cross(d[6], d[2]), twice(cross(d[3], d[4]))), cross(d[1], d[7]));
+  n[2] = add(add(add(cross(d[7], d[2]), cross(d[3], d[5])), cross(d[4], d[4])), cross(d[1], d[8]));
+  n[3] = add(add(cross(d[8], d[2]), twice(cross(d[4], d[5]))), cross(d[1], d[9]));
+}
+
 // findSpan semantics over the breakpoints of the domain: the largest s in [0, ns-1] with
 // b[s] <= x (x below the domain -> 0, at or above its end -> ns-1), i.e. the knot span m with
 // k[m] <= x < k[m+1] that findSpan (Evaluate.cu:504-533) returns.  Bounded; NaN -> 0.

@@ -201,6 +201,25 @@ int nurbs_candidates(nurbs_surface_t s, const double* P_dev, int64_t n, int* lis
  * residual_dev[n] = |S(uv) - P| in FP64.  precision: NURBS_PREC_FP64 or NURBS_PREC_MIXED. */
 int nurbs_invert(nurbs_surface_t s, const double* P_dev, int64_t n, double* uv_dev, int* status_dev,
                  double* residual_dev, int precision, void* stream);
+/* Point projection: the closest point of the surface over its closed knot domain for each of n
+ * points P_dev[3n], near the surface or far from it.  Replaces the reference's unfinished
+ * Project / NormalBoundingBox / NormalBoxToNormalTreeNode / NormalBoundingBoxCheck
+ * (src/kernel/kernel.cu:471-513, 623-704, 1613-1641; src/main.cu:329-396).  Candidates are the
+ * built nodes whose bound box (the node's box intersected with its control points' box) is within
+ * a distance bound from lattice points and whose normal cone can face P (both signs); each is
+ * seeded at its 9x9 lattice point closest to P and runs projected Newton steps with a line search
+ * inside the domain, so minima on the domain's boundary are found too.  FP64.  Outputs as
+ * nurbs_invert (NURBS_INV_NO_CANDIDATE only for non-finite P).  The cones are built with the tree
+ * (nurbs_surface_create, nurbs_build_tree); single surfaces only (not the pool). */
+int nurbs_project(nurbs_surface_t s, const double* P_dev, int64_t n, double* uv_dev, int* status_dev,
+                  double* residual_dev, void* stream);
+/* Copies the projection's culling data to host memory: nbox[65*6] normal boxes (lb xyz, rt xyz),
+ * cone[65*20] FP32 records relative to the control net's centre (bound-box ball centre and radius,
+ * cone axis, cos and sin of its half-angle (0 and 1: every direction), bound box rounded outward,
+ * zero padding), lattice[65*81*3] the nodes' 9x9 lattice surface points (FP32, relative to the
+ * same centre).  Synchronous. */
+int nurbs_normal_cones_export(nurbs_surface_t s, double* nbox_host, float* cone_host, float* lattice_host);
+
 /* p-curve of a 3-D curve on the surface: the parameters of its n ordered samples C_dev[3n].
  * No counterpart in the reference's code (its README names p-curve calculation as the use of
  * the inversion).  Each sample is inverted as nurbs_invert does (precision FP64 or MIXED); each

@@ -14,6 +14,8 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 TREE_NODES = 65
+CONE_STRIDE = 20    # floats per node of the FP32 cone records (orc_build_cones)
+UPTS = 81           # lattice surface points per node (distance bounds, projection seeds)
 
 S, SU, SV, SUU, SUV, SVV = 1, 2, 4, 8, 16, 32
 FOUND_UNIQUE, FOUND_AMBIGUOUS, NO_CANDIDATE, NOT_CONVERGED = 0, 1, 2, 3
@@ -74,6 +76,17 @@ def lib():
         L.orc_pcurve.restype = None
         L.orc_pcurve.argtypes = [C.POINTER(_Surf), _dp, _dp, _bp, _dp, C.c_int64, C.c_int, _dp, _ip, _dp, _ip,
                                  C.c_int]
+        _fp = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
+        L.orc_build_cones.restype = None
+        L.orc_build_cones.argtypes = [C.POINTER(_Surf), _dp, _dp, _bp, _dp, _fp, _fp]
+        L.orc_project_cull.restype = C.c_int
+        L.orc_project_cull.argtypes = [_dp, _bp, _fp, _fp, _dp, _dp, _ip]
+        L.orc_project.restype = None
+        L.orc_project.argtypes = [C.POINTER(_Surf), _dp, _dp, _bp, _fp, _dp, C.c_int64, C.c_int, _dp, _ip, _dp,
+                                  C.c_void_p, C.c_int]
+        L.orc_project_perturbed.restype = None
+        L.orc_project_perturbed.argtypes = [C.POINTER(_Surf), _dp, _dp, _bp, _fp, _dp, C.c_int64, C.c_int, C.c_int,
+                                            C.c_double, _dp, _ip, _dp, C.c_int]
         L.orc_eval_normal.restype = None
         L.orc_eval_normal.argtypes = [C.POINTER(_Surf), _dp, _dp, C.c_int64, C.c_uint, _dp, C.c_int]
         L.orc_gauss_newton_shipped.restype = C.c_int
@@ -101,6 +114,7 @@ class OracleSurface:
                         self.cps.ctypes.data, self.w.ctypes.data)
         self._M = None
         self._tree = None
+        self._cones = None
 
     @property
     def matrix_n(self) -> np.ndarray:
@@ -161,18 +175,75 @@ class OracleSurface:
                          uv, st, res, it.ctypes.data, threads)
         return uv.reshape(n, 2), st, res, it
 
+    def origin(self) -> np.ndarray:
+        """Centre of the control net's bounding box (the FP32 arithmetic's origin)."""
+        return 0.5 * (self.cps.min(0) + self.cps.max(0))
+
+    def cones(self):
+        """Normal boxes (65, 6), FP32 cone records (65, CONE_STRIDE) and distance-bound points
+        (65, UPTS, 3) of the built nodes (orc_build_cones)."""
+        if self._cones is None:
+            t, _, b = self.tree()
+            nb = np.zeros(TREE_NODES * 6, dtype=np.float64)
+            cr = np.zeros(TREE_NODES * CONE_STRIDE, dtype=np.float32)
+            up = np.zeros(TREE_NODES * UPTS * 3, dtype=np.float32)
+            lib().orc_build_cones(C.byref(self._s), self.matrix_n, np.ascontiguousarray(t.reshape(-1)), b, nb, cr, up)
+            self._cones = (nb.reshape(TREE_NODES, 6), cr.reshape(TREE_NODES, CONE_STRIDE), up.reshape(TREE_NODES, UPTS, 3))
+        return self._cones
+
+    def _cone_arg(self):
+        _, cr, up = self.cones()
+        return np.ascontiguousarray(np.concatenate([cr.reshape(-1), up.reshape(-1)]))
+
+    def project_candidates(self, P: np.ndarray):
+        """Per point: the projection's candidates, 128 * node + the seed's lattice index."""
+        t, _, b = self.tree()
+        _, cr, up = self.cones()
+        cr = np.ascontiguousarray(cr.reshape(-1))
+        up = np.ascontiguousarray(up.reshape(-1))
+        tf = np.ascontiguousarray(t.reshape(-1))
+        org = np.ascontiguousarray(self.origin())
+        P = np.ascontiguousarray(P, dtype=np.float64).reshape(-1, 3)
+        lst = np.zeros(TREE_NODES, dtype=np.int32)
+        out = []
+        for k in range(P.shape[0]):
+            n = lib().orc_project_cull(tf, b, cr, up, np.ascontiguousarray(P[k]), org, lst)
+            out.append(lst[:n].copy())
+        return out
+
+    def project(self, P: np.ndarray, max_iter: int = MAX_ITER, threads: int = 0):
+        """Closest point over the closed domain (orc_project): uv (n,2), status, residual, iters."""
+        t, _, b = self.tree()
+        cr = self._cone_arg()
+        P = np.ascontiguousarray(P, dtype=np.float64).reshape(-1, 3)
+        n = P.shape[0]
+        uv = np.empty(2 * n, dtype=np.float64)
+        st = np.empty(n, dtype=np.int32)
+        res = np.empty(n, dtype=np.float64)
+        it = np.empty(n, dtype=np.int32)
+        lib().orc_project(C.byref(self._s), self.matrix_n, np.ascontiguousarray(t.reshape(-1)), b, cr, P, n,
+                          max_iter, uv, st, res, it.ctypes.data, threads)
+        return uv.reshape(n, 2), st, res, it
+
     def invert_perturbed(self, P: np.ndarray, K: int = PERTURB_K, eps: float = PERTURB_EPS, max_iter: int = MAX_ITER,
-                         threads: int = 0):
+                         threads: int = 0, project: bool = False):
         """Answers for K perturbations of P at FP32 resolution, carried back to P (see
-        orc_invert_perturbed): uv (K, n, 2), found (K, n) bool, residual (K, n)."""
+        orc_invert_perturbed; project: of the projection): uv (K, n, 2), found (K, n) bool,
+        residual (K, n)."""
         t, _, b = self.tree()
         P = np.ascontiguousarray(P, dtype=np.float64).reshape(-1, 3)
         n = P.shape[0]
         uv = np.empty(2 * K * n, dtype=np.float64)
         found = np.empty(K * n, dtype=np.int32)
         res = np.empty(K * n, dtype=np.float64)
-        lib().orc_invert_perturbed(C.byref(self._s), self.matrix_n, np.ascontiguousarray(t.reshape(-1)), b, P, n,
-                                   max_iter, K, eps, uv, found, res, threads)
+        tf = np.ascontiguousarray(t.reshape(-1))
+        if project:
+            lib().orc_project_perturbed(C.byref(self._s), self.matrix_n, tf, b,
+                                        self._cone_arg(), P, n, max_iter, K, eps, uv,
+                                        found, res, threads)
+        else:
+            lib().orc_invert_perturbed(C.byref(self._s), self.matrix_n, tf, b, P, n, max_iter, K, eps, uv, found,
+                                       res, threads)
         return uv.reshape(K, n, 2), found.reshape(K, n).astype(bool), res.reshape(K, n)
 
     def invert_fp32_explore(self, P: np.ndarray, perturbation: int = -1, eps: float = PERTURB_EPS,
@@ -190,11 +261,14 @@ class OracleSurface:
                                       max_iter, perturbation, eps, uv, found, res, threads)
         return uv.reshape(n, 2), found.astype(bool), res
 
-    def stability_set(self, P: np.ndarray, threads: int = 0):
+    def stability_set(self, P: np.ndarray, threads: int = 0, project: bool = False):
         """The oracle's answers at FP32 resolution, for parity.classify_inversion: the answers
         for the PERTURB_K perturbed points (FP64), and those of the FP32 exploration of the points
-        and of the same perturbed points, all carried to the true points; stacked (2K+1, n, ...)."""
-        pu, pf, pr = self.invert_perturbed(P, threads=threads)
+        and of the same perturbed points, all carried to the true points; stacked (2K+1, n, ...).
+        project: of the projection, whose GPU arithmetic is FP64: the K perturbed answers only."""
+        pu, pf, pr = self.invert_perturbed(P, threads=threads, project=project)
+        if project:
+            return pu, pf, pr
         us, fs, rs = [pu], [pf], [pr]
         for k in range(-1, PERTURB_K):
             fu, ff, fr = self.invert_fp32_explore(P, perturbation=k, threads=threads)

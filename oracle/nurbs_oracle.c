@@ -475,10 +475,8 @@ void orc_ders3(const orc_surface* s, const double* M, double uu, double vv, doub
 }
 
 
-/* N, N_u, N_v, N_uu, N_uv, N_vv from the third-order derivatives (see above). */
-void orc_normals(const orc_surface* s, const double* M, double uu, double vv, double out[18]) {
-    double d[30];
-    orc_ders3(s, M, uu, vv, d);
+/* N, N_u, N_v, N_uu, N_uv, N_vv from the third-order derivatives d[30] (see above). */
+static void normals_of(const double d[30], double out[18]) {
     const d3 Su = d3at(d, 1), Sv = d3at(d, 2), Suu = d3at(d, 3), Suv = d3at(d, 4), Svv = d3at(d, 5);
     const d3 Suuu = d3at(d, 6), Suuv = d3at(d, 7), Suvv = d3at(d, 8), Svvv = d3at(d, 9);
     const d3 N[6] = {
@@ -493,6 +491,12 @@ void orc_normals(const orc_surface* s, const double* M, double uu, double vv, do
         out[3 * b + 1] = N[b].y;
         out[3 * b + 2] = N[b].z;
     }
+}
+
+void orc_normals(const orc_surface* s, const double* M, double uu, double vv, double out[18]) {
+    double d[30];
+    orc_ders3(s, M, uu, vv, d);
+    normals_of(d, out);
 }
 
 void orc_eval_normal(const orc_surface* s, const double* M, const double* uv, int64_t n, unsigned mask,
@@ -668,6 +672,260 @@ int orc_gauss_newton_shipped(const orc_surface* s, const double* M, const double
     return 0;
 }
 
+
+/* ---------------------------------------------- normal cones and projection (nurbs_project)
+ *
+ * The reference's projection (Project, src/kernel/kernel.cu:471-485; NormalBoundingBoxCheck
+ * :487-513; NormalBoundingBox :623-704; NormalBoxToNormalTreeNode :1613-1636; GetAngle
+ * :1638-1641; driven by src/main.cu:329-396) is unfinished: NormalNeedDivide returns true, the
+ * query point is a constant, N_M3 is taken from N_uv, the corner test ignores contain_zero and
+ * looks along one side of the normal only, and the first Gauss-Newton success is printed.  The
+ * oracle's definition of nurbs_project, with a decision on each of those:
+ *  - normal box of a built node: the unnormalised normal N = Su x Sv at the node's 9x9 lattice
+ *    (the box tree's samples), its component range widened by K = (M1 + 2 M2 + M3) sqrt(3) /
+ *    (8 (8g)^2) with M1, M2, M3 the largest components of N_uu, N_uv, N_vv over the samples (the
+ *    box tree's bound applied to N), intersected with the parent's normal box;
+ *  - cone: every direction when the box contains 0, is empty, or has a corner 90 degrees or more
+ *    from its centre; otherwise the axis is the box centre and the half-angle the largest angle
+ *    to a corner (as NormalBoxToNormalTreeNode), widened by 2 atan(2^-11) for the FP32 test;
+ *  - bound box of a node: its box intersected with the box of the control points whose basis
+ *    functions are not zero on its parameter rectangle (which holds the surface there by the
+ *    convex hull property; the reference's boxes, sampled and widened by K, are too wide on wavy
+ *    surfaces to bound a distance, the control net too wide on smooth ones);
+ *  - candidates of a query P: the nodes whose bound box is within the distance bound (its distance from P at most UB, the least
+ *    distance from P to the surface points of the nodes' 3x3 sub-lattices (1, 4, 7)^2) and whose bound box's
+ *    bounding ball (centre c, radius r) is seen from P inside the double cone (the normal may point towards P or away from it):
+ *    cos(a) sqrt(|d|^2 - r^2) <= |d.axis| + sin(a) r, d = P - c.  Every direction from P to a
+ *    point of the ball lies within asin(r/|d|) of d, so this accepts every node for which some
+ *    S - P in its box can be parallel to a normal in its cone, and every node the reference's
+ *    corner test accepts unless its box is farther than the bound.  The test runs in FP32 relative to the control net's centre (boxes rounded
+ *    outward), in this order and with these roundings in the CUDA kernel too, so both select the
+ *    same nodes;
+ *  - seeds: per candidate, the point of its 9x9 lattice closest to P (one seed at the centre
+ *    of a node spanning many waves of the surface often converges to a farther minimum);
+ *  - trajectories minimise |S - P|^2 over the closed domain, so that minima on its boundary,
+ *    where S - P is not normal to the surface, are found too: projected Newton steps (the
+ *    Hessian J^T J + r.d2S where it is positive definite, J^T J elsewhere; a coordinate at a
+ *    bound whose descent direction points out of the domain is held there and the other takes
+ *    the 1-D step, Newton where its curvature is positive; the new point is clamped to the
+ *    domain), each halved until the distance does
+ *    not grow (at most 30 times); converged at a move <= 1e-10 after a Newton step or <= 1e-14,
+ *    or at a corner where the distance grows into the domain; at most max_iter iterations;
+ *  - the answer is the closest result; AMBIGUOUS as in the inversion. */
+
+static void surface_origin(const orc_surface* s, double org[3]);
+
+/* x rounded to float towards -inf (down != 0) or +inf: the box stays outside the FP64 box. */
+static float f_round_out(double x, int down) {
+    float f = (float)x;
+    if (down && (double)f > x) f = nextafterf(f, -INFINITY);
+    if (!down && (double)f < x) f = nextafterf(f, INFINITY);
+    return f;
+}
+
+/* Box of the control points whose basis functions are not zero on the node's parameter
+ * rectangle: the surface over that rectangle lies in their convex hull (positive weights).  Not
+ * a box of the reference; a rigorous bound for the distance test.  hb = lb xyz, rt xyz. */
+static void hull_box(const orc_surface* s, const orc_tree_node* T, double hb[6]) {
+    const int p = s->degree_u, q = s->degree_v;
+    int i0 = orc_find_span(p, s->cp_u, s->knots_u, T->uv_lb[0]);
+    int i1 = orc_find_span(p, s->cp_u, s->knots_u, T->uv_rt[0]);
+    int j0 = orc_find_span(q, s->cp_v, s->knots_v, T->uv_lb[1]);
+    int j1 = orc_find_span(q, s->cp_v, s->knots_v, T->uv_rt[1]);
+    if (i1 > i0 && s->knots_u[i1] >= T->uv_rt[0]) --i1;   /* the span starting at the right end */
+    if (j1 > j0 && s->knots_v[j1] >= T->uv_rt[1]) --j1;
+    for (int c = 0; c < 3; ++c) { hb[c] = INFINITY; hb[3 + c] = -INFINITY; }
+    for (int i = i0 - p; i <= i1; ++i)
+        for (int j = j0 - q; j <= j1; ++j) {
+            const double* x = s->cps + 3 * ((int64_t)i * s->cp_v + j);
+            for (int c = 0; c < 3; ++c) {
+                hb[c] = hb[c] > x[c] ? x[c] : hb[c];
+                hb[3 + c] = hb[3 + c] < x[c] ? x[c] : hb[3 + c];
+            }
+        }
+}
+
+static void cone_record(const double hb[6], const double nb[6], const double org[3], float* rec) {
+    double ctr[3], h[3];
+    for (int c = 0; c < 3; ++c) {
+        ctr[c] = (hb[c] + hb[3 + c]) / 2;
+        h[c] = (hb[3 + c] - hb[c]) / 2;
+    }
+    const double r = sqrt(h[0] * h[0] + h[1] * h[1] + h[2] * h[2]);
+    const double cm = fmax(fabs(ctr[0] - org[0]), fmax(fabs(ctr[1] - org[1]), fabs(ctr[2] - org[2])));
+    for (int c = 0; c < 3; ++c) rec[c] = (float)(ctr[c] - org[c]);
+    rec[3] = (float)(r * (1 + 0x1p-20) + cm * 0x1p-20);   /* covers the FP32 rounding of the centre */
+    int all = nb[0] > nb[3] || nb[1] > nb[4] || nb[2] > nb[5];
+    all = all || (nb[0] <= 0 && nb[3] >= 0 && nb[1] <= 0 && nb[4] >= 0 && nb[2] <= 0 && nb[5] >= 0);
+    double cosA = 0, sinA = 1, ax[3] = {0, 0, 1};
+    if (!all) {
+        const double m[3] = {(nb[0] + nb[3]) / 2, (nb[1] + nb[4]) / 2, (nb[2] + nb[5]) / 2};
+        const double mm = sqrt(m[0] * m[0] + m[1] * m[1] + m[2] * m[2]);
+        double cmin = 1;
+        for (int i = 0; i < 2; ++i)
+            for (int j = 0; j < 2; ++j)
+                for (int k = 0; k < 2; ++k) {
+                    const double c[3] = {nb[3 * i], nb[3 * j + 1], nb[3 * k + 2]};
+                    const double cc = (m[0] * c[0] + m[1] * c[1] + m[2] * c[2]) /
+                                      (mm * sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]));
+                    cmin = cmin < cc ? cmin : cc;
+                }
+        if (cmin > 0) {
+            const double sn = sqrt(fmax(0.0, 1 - cmin * cmin));
+            const double t = 0x1p-11, cd = (1 - t * t) / (1 + t * t), sd = (2 * t) / (1 + t * t);
+            const double ca = cmin * cd - sn * sd, sa = sn * cd + cmin * sd;
+            if (ca > 0) {
+                cosA = ca;
+                sinA = sa;
+                ax[0] = m[0] / mm;
+                ax[1] = m[1] / mm;
+                ax[2] = m[2] / mm;
+            }
+        }
+    }
+    for (int c = 0; c < 3; ++c) rec[4 + c] = (float)ax[c];
+    rec[7] = (float)cosA;
+    rec[8] = (float)sinA;
+    for (int c = 0; c < 3; ++c) {
+        rec[9 + c] = f_round_out(hb[c] - org[c], 1);
+        rec[12 + c] = f_round_out(hb[3 + c] - org[c], 0);
+    }
+    for (int c = 15; c < ORC_CONE_STRIDE; ++c) rec[c] = 0;
+}
+
+static void cone_node(const orc_surface* s, const double* M, unsigned g, unsigned bx, unsigned by,
+                      const orc_tree_node* T, const double* parent_nb, const double org[3], double* nb, float* rec,
+                      float* upts) {
+    double base_unit = 1.0 / g;
+    double unit = base_unit / GAP;
+    double base_u = base_unit * bx, base_v = base_unit * by;
+    double M1 = 0, M2 = 0, M3 = 0, mx[3] = {0, 0, 0}, mn[3] = {0, 0, 0};
+    for (int tx = 0; tx < PTS; ++tx)
+        for (int ty = 0; ty < PTS; ++ty) {
+            double p1 = base_u + tx * unit, p2 = base_v + ty * unit;
+            double d[30], N[18];
+            orc_ders3(s, M, p1, p2, d);
+            normals_of(d, N);
+            const double a = max_abs3(d3at(N, 3)), b = max_abs3(d3at(N, 4)), c = max_abs3(d3at(N, 5));
+            {   /* the lattice's surface points: distance bounds and projection seeds */
+                float* o = upts + 3 * (PTS * tx + ty);
+                for (int c = 0; c < 3; ++c) o[c] = (float)(d[c] - org[c]);
+            }
+            if (tx == 0 && ty == 0) {
+                M1 = a; M2 = b; M3 = c;
+                for (int k = 0; k < 3; ++k) mx[k] = mn[k] = N[k];
+            } else {
+                M1 = M1 < a ? a : M1;
+                M2 = M2 < b ? b : M2;
+                M3 = M3 < c ? c : M3;
+                for (int k = 0; k < 3; ++k) {
+                    mx[k] = mx[k] < N[k] ? N[k] : mx[k];
+                    mn[k] = mn[k] > N[k] ? N[k] : mn[k];
+                }
+            }
+        }
+    unsigned den = 8u * GAP * g * GAP * g;
+    double K = (M1 + 2 * M2 + M3) * sqrt(3.0) / den;
+    for (int k = 0; k < 3; ++k) {
+        nb[k] = mn[k] - K;
+        nb[3 + k] = mx[k] + K;
+        if (parent_nb) {
+            nb[k] = fmax(nb[k], parent_nb[k]);
+            nb[3 + k] = fmin(nb[3 + k], parent_nb[3 + k]);
+        }
+    }
+    double hb[6];
+    hull_box(s, T, hb);
+    /* the node's own box where it is narrower (smooth surfaces) */
+    double xb[6];
+    int empty = 0;
+    for (int c = 0; c < 3; ++c) {
+        xb[c] = hb[c] > T->lb[c] ? hb[c] : T->lb[c];
+        xb[3 + c] = hb[3 + c] < T->rt[c] ? hb[3 + c] : T->rt[c];
+        empty = empty || xb[c] > xb[3 + c];
+    }
+    cone_record(empty ? hb : xb, nb, org, rec);
+}
+
+void orc_build_cones(const orc_surface* s, const double* M, const orc_tree_node* tree, const unsigned char* built,
+                     double* nbox, float* cone, float* upts) {
+    double org[3];
+    surface_origin(s, org);
+    memset(nbox, 0, sizeof(double) * 6 * ORC_TREE_NODES);
+    memset(cone, 0, sizeof(float) * ORC_CONE_STRIDE * ORC_TREE_NODES);
+    memset(upts, 0, sizeof(float) * ORC_UPTS * 3 * ORC_TREE_NODES);
+    if (!built[0]) return;
+    cone_node(s, M, 1, 0, 0, &tree[0], NULL, org, nbox, cone, upts);
+    if (!built[1]) return;
+    for (unsigned bx = 0; bx < GAP; ++bx)
+        for (unsigned by = 0; by < GAP; ++by) {
+            int t = 1 + (int)(bx * GAP + by);
+            cone_node(s, M, GAP, bx, by, &tree[t], nbox, org, nbox + 6 * t, cone + ORC_CONE_STRIDE * t,
+                      upts + ORC_UPTS * 3 * t);
+        }
+}
+
+static float fdot3(const float a[3], const float b[3]) { return (a[0] * b[0] + a[1] * b[1]) + a[2] * b[2]; }
+
+/* Projection candidates of P (ascending nodes) and edge seeds (node * 4 + edge, ascending; edge
+ * 0: u = u0, 1: u = u1, 2: v = v0, 3: v = v1).  Returns the candidate count. */
+int orc_project_cull(const orc_tree_node* tree, const unsigned char* built, const float* cone, const float* upts,
+                     const double* P, const double org[3], int* list) {
+    (void)tree;
+    const int nb = built[1] ? ORC_TREE_NODES : (built[0] ? 1 : 0);
+    const float Pf[3] = {(float)(P[0] - org[0]), (float)(P[1] - org[1]), (float)(P[2] - org[2])};
+    float ub2 = INFINITY;
+    for (int k = 0; k < nb; ++k)
+        for (int a = 1; a < PTS; a += 3)   /* the 3x3 sub-lattice (1, 4, 7)^2 of each node */
+            for (int b = 1; b < PTS; b += 3) {
+                const float* x = upts + 3 * (ORC_UPTS * k + PTS * a + b);
+                const float d[3] = {x[0] - Pf[0], x[1] - Pf[1], x[2] - Pf[2]};
+                const float dd = fdot3(d, d);
+                ub2 = ub2 < dd ? ub2 : dd;
+            }
+    ub2 = ub2 * (1.0f + 0x1p-10f);
+    int n = 0;
+    for (int k = 0; k < nb; ++k) {
+        const float* rc = cone + ORC_CONE_STRIDE * k;
+        float g[3];
+        for (int c = 0; c < 3; ++c) {
+            const float lo = rc[9 + c] - Pf[c], hi = Pf[c] - rc[12 + c];
+            g[c] = lo > hi ? lo : hi;
+            g[c] = g[c] > 0.0f ? g[c] : 0.0f;
+        }
+        const int nearb = fdot3(g, g) <= ub2;
+        const float d[3] = {Pf[0] - rc[0], Pf[1] - rc[1], Pf[2] - rc[2]};
+        const float dd = fdot3(d, d), r = rc[3];
+        float e = dd - r * r;
+        e = e > 0.0f ? e : 0.0f;
+        const int seen = rc[7] * sqrtf(e) <= fabsf(fdot3(d, rc + 4)) + rc[8] * r;
+        if (nearb && seen) {
+            /* seed: the node's lattice point closest to P (first of equals) */
+            float best = INFINITY;
+            int bi = 0;
+            for (int j = 0; j < ORC_UPTS; ++j) {
+                const float* x = upts + 3 * (ORC_UPTS * k + j);
+                const float e3[3] = {x[0] - Pf[0], x[1] - Pf[1], x[2] - Pf[2]};
+                const float ee = fdot3(e3, e3);
+                if (ee < best) { best = ee; bi = j; }
+            }
+            list[n++] = 128 * k + bi;
+        }
+    }
+    return n;
+}
+
+/* Seed of projection candidate c = 128 * node + j: the node's lattice point j = 9 tx + ty (the
+ * same arithmetic as the samples). */
+static void projection_seed(int c, double C[2]) {
+    const int k = c >> 7, j = c & 127;
+    const unsigned g = k == 0 ? 1u : GAP, bx = k == 0 ? 0u : (unsigned)(k - 1) / GAP, by = k == 0 ? 0u : (unsigned)(k - 1) % GAP;
+    const double base_unit = 1.0 / g, unit = base_unit / GAP;
+    const int tx = j / PTS, ty = j % PTS;
+    C[0] = base_unit * bx + tx * unit;
+    C[1] = base_unit * by + ty * unit;
+}
+
 /* ------------------------------------------- inversion: the oracle's definition of the answer
  *
  * The reference stops Gauss-Newton when |S - P| < max_edge (kernel.cu:178), which cannot reach
@@ -735,20 +993,108 @@ static int run_trajectory(const orc_surface* s, const double* M, const double P[
     return 0;
 }
 
+/* One projection trajectory from C (the definition above): projected Newton with a line search,
+ * C stays in the domain.  Returns 1 when it converged; *iters counts the iterations. */
+static void ders2_at(const orc_surface* s, const double* M, const double C[2], d3* S, d3* Su, d3* Sv, d3* Suu,
+                     d3* Suv, d3* Svv) {
+    const int p = s->degree_u, q = s->degree_v;
+    span_loc L = locate(s, M, C[0], C[1]);
+    d4 R = R_of(L.middle, p, q, L.u, L.v);
+    *S = cart(R);
+    *Su = der_u(L.middle, p, q, L.u, L.v, R, L.spanU);
+    *Sv = der_v(L.middle, p, q, L.u, L.v, R, L.spanV);
+    *Suu = der_uu(L.middle, p, q, L.u, L.v, R, L.spanU);
+    *Suv = der_uv(L.middle, p, q, L.u, L.v, R, L.spanU, L.spanV);
+    *Svv = der_vv(L.middle, p, q, L.u, L.v, R, L.spanV);
+}
+
+static double dot3d(d3 a, d3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+static double clampd(double x, double lo, double hi) { return x < lo ? lo : (x > hi ? hi : x); }
+
+static int project_trajectory(const orc_surface* s, const double* M, const double P[3], double C[2],
+                              const double dom[4], int max_iter, int* iters) {
+    d3 S, Su, Sv, Suu, Suv, Svv;
+    C[0] = clampd(C[0], dom[0], dom[1]);
+    C[1] = clampd(C[1], dom[2], dom[3]);
+    ders2_at(s, M, C, &S, &Su, &Sv, &Suu, &Suv, &Svv);
+    for (int it = 0; it < max_iter; ++it) {
+        const d3 r = {S.x - P[0], S.y - P[1], S.z - P[2]};
+        const double f = dot3d(r, r);
+        const double g0 = dot3d(Su, r), g1 = dot3d(Sv, r);
+        const double a00 = dot3d(Su, Su), a01 = dot3d(Su, Sv), a11 = dot3d(Sv, Sv);
+        const double n00 = a00 + dot3d(r, Suu), n01 = a01 + dot3d(r, Suv), n11 = a11 + dot3d(r, Svv);
+        /* a coordinate at a bound whose descent direction -g points out of the domain stays */
+        const int fu = !((C[0] <= dom[0] && g0 > 0) || (C[0] >= dom[1] && g0 < 0));
+        const int fv = !((C[1] <= dom[2] && g1 > 0) || (C[1] >= dom[3] && g1 < 0));
+        double d0 = 0, d1 = 0;
+        int newton;
+        if (fu && fv) {
+            newton = n00 > 0 && n00 * n11 - n01 * n01 > 0;
+            const double h00 = newton ? n00 : a00, h01 = newton ? n01 : a01, h11 = newton ? n11 : a11;
+            const double det = h00 * h11 - h01 * h01;
+            if (!(det > 0)) { *iters = it + 1; return 0; }
+            d0 = (h11 * g0 - h01 * g1) / det;
+            d1 = (h00 * g1 - h01 * g0) / det;
+        } else if (fu) {   /* the 1-D Newton step along u where its curvature is positive */
+            newton = n00 > 0;
+            const double h = newton ? n00 : a00;
+            if (!(h > 0)) { *iters = it + 1; return 0; }
+            d0 = g0 / h;
+        } else if (fv) {
+            newton = n11 > 0;
+            const double h = newton ? n11 : a11;
+            if (!(h > 0)) { *iters = it + 1; return 0; }
+            d1 = g1 / h;
+        } else {
+            *iters = it + 1;   /* a corner where the distance grows into the domain */
+            return 1;
+        }
+        if (!(isfinite(d0) && isfinite(d1))) { *iters = it + 1; return 0; }
+        /* line search: halve the step until the distance does not grow (at most 30 times) */
+        double alpha = 1, Cn[2];
+        d3 Sn, Snu, Snv, Snuu, Snuv, Snvv;
+        for (int ls = 0;; ++ls) {
+            Cn[0] = clampd(C[0] - alpha * d0, dom[0], dom[1]);
+            Cn[1] = clampd(C[1] - alpha * d1, dom[2], dom[3]);
+            ders2_at(s, M, Cn, &Sn, &Snu, &Snv, &Snuu, &Snuv, &Snvv);
+            const d3 rn = {Sn.x - P[0], Sn.y - P[1], Sn.z - P[2]};
+            if (dot3d(rn, rn) <= f || ls == 30) break;
+            alpha *= 0.5;
+        }
+        const double moved = fmax(fabs(Cn[0] - C[0]), fabs(Cn[1] - C[1]));
+        C[0] = Cn[0];
+        C[1] = Cn[1];
+        S = Sn; Su = Snu; Sv = Snv; Suu = Snuu; Suv = Snuv; Svv = Snvv;
+        if (moved <= 1e-14 || (newton && moved <= 1e-10)) { *iters = it + 1; return 1; }
+    }
+    *iters = max_iter;
+    return 0;
+}
+
+
+/* cone == NULL: the inversion; else the projection (candidates, seeds and trajectories above). */
 static void invert_one(const orc_surface* s, const double* M, const orc_tree_node* tree, const unsigned char* built,
-                       const double* Pk, int max_iter, const double dom[4], double* uv, int* status, double* residual,
-                       int* iters) {
+                       const float* cone, const double org[3], const double* Pk, int max_iter, const double dom[4],
+                       double* uv, int* status, double* residual, int* iters) {
     int list[ORC_TREE_NODES];
-    int nc = orc_candidates(tree, built, Pk, list);
+    int nc = cone ? orc_project_cull(tree, built, cone, cone + ORC_CONE_STRIDE * ORC_TREE_NODES, Pk, org, list)
+                  : orc_candidates(tree, built, Pk, list);
     double best_uv[2] = {NAN, NAN}, best_r = INFINITY;
     double sol_uv[ORC_TREE_NODES][2], sol_r[ORC_TREE_NODES];
     int nsol = 0, total = 0;
     for (int c = 0; c < nc; ++c) {
-        const orc_tree_node* T = &tree[list[c]];
-        /* seed = uv-centre of the node (kernel.cu:154) */
-        double C[2] = {(T->uv_lb[0] + T->uv_rt[0]) / 2, (T->uv_lb[1] + T->uv_rt[1]) / 2};
+        double C[2];
+        if (cone) {
+            projection_seed(list[c], C);
+        } else {
+            /* seed = uv-centre of the node (kernel.cu:154) */
+            const orc_tree_node* T = &tree[list[c]];
+            C[0] = (T->uv_lb[0] + T->uv_rt[0]) / 2;
+            C[1] = (T->uv_lb[1] + T->uv_rt[1]) / 2;
+        }
         int its = 0;
-        int converged = run_trajectory(s, M, Pk, C, max_iter, 0, &its);
+        int converged = cone ? project_trajectory(s, M, Pk, C, dom, max_iter, &its)
+                             : run_trajectory(s, M, Pk, C, max_iter, 0, &its);
         total += its;
         if (!converged) continue;
         if (!(C[0] >= dom[0] && C[0] <= dom[1] && C[1] >= dom[2] && C[1] <= dom[3])) continue;
@@ -784,18 +1130,31 @@ static void domain_of(const orc_surface* s, double dom[4]) {
     dom[3] = s->knots_v[s->cp_v];
 }
 
-void orc_invert(const orc_surface* s, const double* M, const orc_tree_node* tree, const unsigned char* built,
-                const double* P, int64_t n, int max_iter, double* uv, int* status, double* residual, int* iters,
-                int threads) {
-    double dom[4];
+static void invert_all(const orc_surface* s, const double* M, const orc_tree_node* tree, const unsigned char* built,
+                       const float* cone, const double* P, int64_t n, int max_iter, double* uv, int* status,
+                       double* residual, int* iters, int threads) {
+    double dom[4], org[3];
     domain_of(s, dom);
+    surface_origin(s, org);
 #ifdef _OPENMP
     if (threads <= 0) threads = omp_get_max_threads();
 #pragma omp parallel for schedule(dynamic, 64) num_threads(threads)
 #endif
     for (int64_t k = 0; k < n; ++k)
-        invert_one(s, M, tree, built, P + 3 * k, max_iter, dom, uv + 2 * k, status + k, residual + k,
+        invert_one(s, M, tree, built, cone, org, P + 3 * k, max_iter, dom, uv + 2 * k, status + k, residual + k,
                    iters ? iters + k : NULL);
+}
+
+void orc_invert(const orc_surface* s, const double* M, const orc_tree_node* tree, const unsigned char* built,
+                const double* P, int64_t n, int max_iter, double* uv, int* status, double* residual, int* iters,
+                int threads) {
+    invert_all(s, M, tree, built, NULL, P, n, max_iter, uv, status, residual, iters, threads);
+}
+
+void orc_project(const orc_surface* s, const double* M, const orc_tree_node* tree, const unsigned char* built,
+                 const float* cone, const double* P, int64_t n, int max_iter, double* uv, int* status,
+                 double* residual, int* iters, int threads) {
+    invert_all(s, M, tree, built, cone, P, n, max_iter, uv, status, residual, iters, threads);
 }
 
 /* ------------------------------------------------------ stability of the answer at FP32 resolution */
@@ -830,9 +1189,9 @@ static double perturbed(const double org[3], const double* P, int k, int64_t i, 
     return org[c] + (P[c] - org[c]) * (1.0 + e * perturb_sign(k, 3 * i + c));
 }
 
-void orc_invert_perturbed(const orc_surface* s, const double* M, const orc_tree_node* tree,
-                          const unsigned char* built, const double* P, int64_t n, int max_iter, int K, double eps,
-                          double* uv, int* found, double* residual, int threads) {
+static void perturbed_all(const orc_surface* s, const double* M, const orc_tree_node* tree,
+                          const unsigned char* built, const float* cone, const double* P, int64_t n, int max_iter,
+                          int K, double eps, double* uv, int* found, double* residual, int threads) {
     double dom[4], org[3];
     domain_of(s, dom);
     surface_origin(s, org);
@@ -848,19 +1207,34 @@ void orc_invert_perturbed(const orc_surface* s, const double* M, const orc_tree_
             double C[2];
             int st, its;
             double r;
-            invert_one(s, M, tree, built, Pp, max_iter, dom, C, &st, &r, NULL);
+            invert_one(s, M, tree, built, cone, org, Pp, max_iter, dom, C, &st, &r, NULL);
             const int64_t o = (int64_t)k * n + i;
             int ok = 0;
             if (st == ORC_FOUND_UNIQUE || st == ORC_FOUND_AMBIGUOUS) {
                 /* the minimum of the true point next to the perturbed answer */
-                ok = run_trajectory(s, M, Pk, C, max_iter, 1, &its) && C[0] >= dom[0] && C[0] <= dom[1] &&
-                     C[1] >= dom[2] && C[1] <= dom[3];
+                if (cone)
+                    ok = project_trajectory(s, M, Pk, C, dom, max_iter, &its);
+                else
+                    ok = run_trajectory(s, M, Pk, C, max_iter, 1, &its) && C[0] >= dom[0] && C[0] <= dom[1] &&
+                         C[1] >= dom[2] && C[1] <= dom[3];
             }
             uv[2 * o] = ok ? C[0] : NAN;
             uv[2 * o + 1] = ok ? C[1] : NAN;
             found[o] = ok;
             residual[o] = ok ? dist3(surface_point(s, M, C), Pk) : NAN;
         }
+}
+
+void orc_invert_perturbed(const orc_surface* s, const double* M, const orc_tree_node* tree,
+                          const unsigned char* built, const double* P, int64_t n, int max_iter, int K, double eps,
+                          double* uv, int* found, double* residual, int threads) {
+    perturbed_all(s, M, tree, built, NULL, P, n, max_iter, K, eps, uv, found, residual, threads);
+}
+
+void orc_project_perturbed(const orc_surface* s, const double* M, const orc_tree_node* tree,
+                           const unsigned char* built, const float* cone, const double* P, int64_t n, int max_iter,
+                           int K, double eps, double* uv, int* found, double* residual, int threads) {
+    perturbed_all(s, M, tree, built, cone, P, n, max_iter, K, eps, uv, found, residual, threads);
 }
 
 /* The same trajectories as invert_one computed in FP32 arithmetic (span matrices, local
@@ -974,9 +1348,9 @@ static int trajectory32(const orc_surface* s, const double* M, const double org[
     return 0;
 }
 
-void orc_invert_fp32_explore(const orc_surface* s, const double* M, const orc_tree_node* tree,
-                             const unsigned char* built, const double* P, int64_t n, int max_iter, int pk,
-                             double eps, double* uv, int* found, double* residual, int threads) {
+static void explore_all(const orc_surface* s, const double* M, const orc_tree_node* tree,
+                        const unsigned char* built, const double* P, int64_t n, int max_iter, int pk, double eps,
+                        double* uv, int* found, double* residual, int threads) {
     double dom[4], org[3];
     domain_of(s, dom);
     surface_origin(s, org);
@@ -1026,6 +1400,12 @@ void orc_invert_fp32_explore(const orc_surface* s, const double* M, const orc_tr
         uv[2 * k + 1] = bv;
         residual[k] = isfinite(br) ? br : NAN;
     }
+}
+
+void orc_invert_fp32_explore(const orc_surface* s, const double* M, const orc_tree_node* tree,
+                             const unsigned char* built, const double* P, int64_t n, int max_iter, int pk,
+                             double eps, double* uv, int* found, double* residual, int threads) {
+    explore_all(s, M, tree, built, P, n, max_iter, pk, eps, uv, found, residual, threads);
 }
 
 /* ------------------------------------------------------------------------------ p-curves

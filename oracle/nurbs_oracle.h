@@ -137,6 +137,32 @@ void orc_normals(const orc_surface* s, const double* matrix_n, double u, double 
 void orc_eval_normal(const orc_surface* s, const double* matrix_n, const double* uv, int64_t n, unsigned mask,
                      double* out, int threads);
 
+/* Normal cones of the built nodes (the oracle of the CUDA cone build; nurbs_oracle.c states the
+ * definition): nbox[6 * 65] = the normal boxes (lb xyz, rt xyz); cone[ORC_CONE_STRIDE * 65] =
+ * per node in FP32, relative to the control net's centre: the bound box's bounding-ball centre
+ * (0..2) and radius (3), cone axis (4..6), cos and sin of the half-angle (7, 8; 0 and 1 for
+ * every direction), the bound box rounded outward (lb 9..11, rt 12..14), zero (15..19);
+ * upts[3 * ORC_UPTS * 65] = the surface points of each node's 9x9 lattice (index 9 tx + ty), the
+ * same way. */
+#define ORC_CONE_STRIDE 20
+#define ORC_UPTS 81
+void orc_build_cones(const orc_surface* s, const double* matrix_n, const orc_tree_node* tree,
+                     const unsigned char* built, double* nbox, float* cone, float* upts);
+/* Projection candidates of one point P (128 * node + its seed's lattice index, ascending
+ * nodes); org = the control net's centre.  Returns the candidate count. */
+int orc_project_cull(const orc_tree_node* tree, const unsigned char* built, const float* cone, const float* upts,
+                     const double* P, const double org[3], int* list);
+/* cone arguments below: the cone records followed by upts (ORC_CONE_STRIDE * 65 + 3 * ORC_UPTS * 65
+ * floats). */
+/* Closest point of the surface over its closed domain (the oracle of nurbs_project), and the
+ * stability set of its answers (the counterpart of orc_invert_perturbed). */
+void orc_project(const orc_surface* s, const double* matrix_n, const orc_tree_node* tree,
+                 const unsigned char* built, const float* cone, const double* P, int64_t n, int max_iter,
+                 double* uv, int* status, double* residual, int* iters, int threads);
+void orc_project_perturbed(const orc_surface* s, const double* matrix_n, const orc_tree_node* tree,
+                           const unsigned char* built, const float* cone, const double* P, int64_t n, int max_iter,
+                           int K, double eps, double* uv, int* found, double* residual, int threads);
+
 /* The reference's GaussNewton exactly as shipped (kernel.cu:151-249): <= 10 steps,
  * success when |S-P| < max_edge before a step.  Returns 1 on success and writes uv. */
 int orc_gauss_newton_shipped(const orc_surface* s, const double* matrix_n, const double seed[2],

@@ -103,6 +103,14 @@ def oracle_parity(o, P, uv, st, res, res_abs=1e-14):
     return classify_inversion(uv, st, res, ouv, ost, ores, P, res_abs=res_abs, perturbed=o.stability_set(P))
 
 
+def project_parity(o, P, uv, st, res, res_abs=1e-14):
+    """Classifies a GPU projection against the oracle's (OracleSurface.project), with its K
+    perturbed answers deciding which FOUND_UNIQUE queries are UNSTABLE."""
+    ouv, ost, ores, _ = o.project(P)
+    return classify_inversion(uv, st, res, ouv, ost, ores, P, res_abs=res_abs,
+                              perturbed=o.stability_set(P, project=True))
+
+
 # Mixed precision only: FOUND_UNIQUE queries whose FP32 exploration ends elsewhere than the
 # oracle's FP64 trajectories although the oracle's own FP32-resolution variants agree.  Every
 # case examined is a trajectory that leaves the domain far (FP32 cannot evaluate the extrapolated

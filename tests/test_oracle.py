@@ -284,3 +284,85 @@ def test_oracle_third_derivatives_and_normals_against_differences(kind):
     # a mask selects blocks in order
     sel = o.eval_normal(uv, 0b101000)
     assert np.array_equal(sel, np.concatenate([N[3], N[5]]))
+
+
+def _projection_queries(o, n, seed, spread):
+    """Points off the surface along its normal by up to +-spread/2 of the control net's extent,
+    and points far from it (a box six extents wide)."""
+    rng = np.random.default_rng(seed)
+    uv = rng.random((n, 2))
+    E = o.eval(uv, 7)
+    N = np.cross(E[3:6].T, E[6:9].T)
+    N /= np.linalg.norm(N, axis=1)[:, None]
+    ext = np.ptp(o.cps, 0).max()
+    near = E[0:3].T + N * ((rng.random(n) - 0.5) * spread * ext)[:, None]
+    far = o.cps.mean(0) + (rng.random((n // 4, 3)) - 0.5) * 6 * ext
+    return np.concatenate([near, far])
+
+
+@pytest.mark.parametrize("kind", ["large", "small", "rational"])
+def test_oracle_projection_is_a_constrained_minimum_and_mostly_global(kind):
+    """The projection's answers: every query found; each answer a minimum of |S - P| over the
+    closed domain (interior: gradient J^T r zero to rounding and Hessian positive definite; on an
+    edge: the free derivative zero, the other pointing into the domain); and the global minimum
+    (a 401x401 parameter grid) for at least 95 % of the queries."""
+    from gpu_nurbs_gb300 import synth
+    surf = {"large": synth.surface_large(), "small": synth.surface_small(),
+            "rational": synth.surface_random(synth.Rng(77))}[kind]
+    o = O.OracleSurface(surf)
+    P = _projection_queries(o, 400, 5, 0.2)
+    uv, st, res, _ = o.project(P)
+    assert np.all(st <= O.FOUND_AMBIGUOUS)
+    E = o.eval(uv, 63).reshape(6, 3, -1)
+    r = E[0].T - P
+    g = np.stack([(E[1].T * r).sum(1), (E[2].T * r).sum(1)], 1)
+    scale = np.maximum(np.linalg.norm(r, axis=1), 1e-3) * np.maximum(np.linalg.norm(E[1], axis=0),
+                                                                    np.linalg.norm(E[2], axis=0))
+    ku = surf["knots_u"][surf["p"]], surf["knots_u"][surf["nu"]]
+    kv = surf["knots_v"][surf["q"]], surf["knots_v"][surf["nv"]]
+    for a, (lo, hi) in ((0, ku), (1, kv)):
+        inner = (uv[:, a] > lo) & (uv[:, a] < hi)
+        # 1e-6: a Newton step of 1e-10 ends the iteration, which leaves |g| ~ 1e-7 |r||J| in the
+        # flat valleys of nearly degenerate minima
+        assert np.all(np.abs(g[inner, a]) <= 1e-6 * scale[inner]), (a, np.abs(g[inner, a] / scale[inner]).max())
+        assert np.all(g[uv[:, a] == lo, a] >= -1e-6 * scale[uv[:, a] == lo])
+        assert np.all(g[uv[:, a] == hi, a] <= 1e-6 * scale[uv[:, a] == hi])
+    interior = np.all((uv > [ku[0], kv[0]]) & (uv < [ku[1], kv[1]]), axis=1)
+    h00 = (E[1] * E[1]).sum(0) + (r.T * E[3]).sum(0)
+    h01 = (E[1] * E[2]).sum(0) + (r.T * E[4]).sum(0)
+    h11 = (E[2] * E[2]).sum(0) + (r.T * E[5]).sum(0)
+    det = h00 * h11 - h01 * h01
+    assert np.all((h00[interior] > 0) & (det[interior] >= -1e-9 * (h00[interior] * h11[interior]))), kind
+    gg = np.linspace(0, 1, 401)
+    U, V = np.meshgrid(ku[0] + gg * (ku[1] - ku[0]), kv[0] + gg * (kv[1] - kv[0]), indexing="ij")
+    G = o.eval(np.stack([U.ravel(), V.ravel()], 1), 1).T
+    dmin = np.array([np.linalg.norm(G - x, axis=1).min() for x in P])
+    assert np.mean(res <= dmin + 1e-12) >= 0.95, np.mean(res <= dmin + 1e-12)
+
+
+def test_oracle_normal_cones_hold_the_sampled_normals():
+    """Cones and bound boxes of the built nodes hold the normals and points sampled densely over
+    each node's parameter rectangle (the lattice-plus-bound construction is not a proof); nodes
+    whose cone is not every direction exist on the smooth surface."""
+    from gpu_nurbs_gb300 import synth
+    for surf in (synth.surface_small(), synth.surface_large()):
+        o = O.OracleSurface(surf)
+        t, _, b = o.tree()
+        nb, cr, lat = o.cones()
+        org = o.origin()
+        g = (np.arange(17) + 0.5) / 17
+        for k in np.nonzero(b)[0]:
+            lo, hi = t[k, 0:2], t[k, 2:4]
+            U, V = np.meshgrid(lo[0] + g * (hi[0] - lo[0]), lo[1] + g * (hi[1] - lo[1]), indexing="ij")
+            uv = np.stack([U.ravel(), V.ravel()], 1)
+            N = o.eval_normal(uv, 1).T
+            S = o.eval(uv, 1).T - org
+            assert np.all(S >= cr[k, 9:12] - 1e-12) and np.all(S <= cr[k, 12:15] + 1e-12), k
+            assert np.all(N >= nb[k, :3] - 1e-9) and np.all(N <= nb[k, 3:] + 1e-9), k
+            if cr[k, 7] > 0:
+                c = (N @ cr[k, 4:7].astype(np.float64)) / np.linalg.norm(N, axis=1)
+                assert np.all(c >= cr[k, 7] - 1e-6), (k, c.min(), cr[k, 7])
+            Lk = o.eval(np.stack([np.repeat(lo[0] + np.arange(9) / 8 * (hi[0] - lo[0]), 9),
+                                  np.tile(lo[1] + np.arange(9) / 8 * (hi[1] - lo[1]), 9)], 1), 1).T - org
+            assert np.abs(lat[k] - Lk).max() <= 1e-6 * max(1.0, np.abs(Lk).max()), k
+    assert np.any(O.OracleSurface(synth.surface_small()).cones()[1][:, 7] > 0)
