@@ -28,6 +28,9 @@ using namespace inv;
 
 constexpr int kMaxIterProj = 40;  // projected Newton iterations per seed (the oracle's cap)
 constexpr int kMaxHalvings = 30;  // line-search halvings per iteration
+// a Newton move this small ends a seed (far points have flat minima, where Newton converges
+// slowly: the inversion's 1e-10 would leave the parameters ~1e-9 from the minimum)
+constexpr double kTolNewtonProj = 1e-12;
 constexpr int kLattice = kPts * kPts;
 
 struct ProjStaged {
@@ -102,7 +105,7 @@ __device__ __forceinline__ int project_iterate(const Ctx& c, double px, double p
   const double moved = fmax(fabs(un - sd.u), fabs(vn - sd.v));
   sd.u = un;
   sd.v = vn;
-  if (moved <= kTolAny64 || (newton && moved <= kTolNewton64)) return kConverged;
+  if (moved <= kTolAny64 || (newton && moved <= kTolNewtonProj)) return kConverged;
   if (++sd.it >= kMaxIterProj) return kFailed;
   return kContinue;
 }

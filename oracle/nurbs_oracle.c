@@ -709,7 +709,9 @@ int orc_gauss_newton_shipped(const orc_surface* s, const double* M, const double
  *    bound whose descent direction points out of the domain is held there and the other takes
  *    the 1-D step, Newton where its curvature is positive; the new point is clamped to the
  *    domain), each halved until the distance does
- *    not grow (at most 30 times); converged at a move <= 1e-10 after a Newton step or <= 1e-14,
+ *    not grow (at most 30 times); converged at a move <= 1e-12 after a Newton step or <= 1e-14
+ *    (1e-12, not the inversion's 1e-10: far points have flat minima, where Newton converges
+ *    slowly and a stop at 1e-10 leaves the parameters ~1e-9 apart),
  *    or at a corner where the distance grows into the domain; at most max_iter iterations;
  *  - the answer is the closest result; AMBIGUOUS as in the inversion. */
 
@@ -1065,7 +1067,7 @@ static int project_trajectory(const orc_surface* s, const double* M, const doubl
         C[0] = Cn[0];
         C[1] = Cn[1];
         S = Sn; Su = Snu; Sv = Snv; Suu = Snuu; Suv = Snuv; Svv = Snvv;
-        if (moved <= 1e-14 || (newton && moved <= 1e-10)) { *iters = it + 1; return 1; }
+        if (moved <= 1e-14 || (newton && moved <= 1e-12)) { *iters = it + 1; return 1; }
     }
     *iters = max_iter;
     return 0;
