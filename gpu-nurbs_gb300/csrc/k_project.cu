@@ -31,6 +31,7 @@ constexpr int kMaxHalvings = 30;  // line-search halvings per iteration
 // a Newton move this small ends a seed (far points have flat minima, where Newton converges
 // slowly: the inversion's 1e-10 would leave the parameters ~1e-9 from the minimum)
 constexpr double kTolNewtonProj = 1e-12;
+constexpr double kWholeStep = 1e-6;  // steps below this skip the line search
 constexpr int kLattice = kPts * kPts;
 
 struct ProjStaged {
@@ -92,15 +93,20 @@ __device__ __forceinline__ int project_iterate(const Ctx& c, double px, double p
     return kConverged;  // a corner where the distance grows into the domain
   }
   if (!(isfinite(d0) && isfinite(d1))) return kFailed;
-  double alpha = 1, un, vn;
-  for (int ls = 0;; ++ls) {
-    un = clampd(sd.u - alpha * d0, c.dom_u0, c.dom_u1);
-    vn = clampd(sd.v - alpha * d1, c.dom_v0, c.dom_v1);
-    int hu = sd.hu, hv = sd.hv;
-    fast::SDer<double> e = fast::eval_at<double, P, Q, 0>(c.L64, c.m64, c.p, c.q, un, vn, hu, hv);
-    const v3<double> rn = {e.S.x - px, e.S.y - py, e.S.z - pz};
-    if (dot3(rn, rn) <= f || ls == kMaxHalvings) break;
-    alpha *= 0.5;
+  // line search; a step below kWholeStep is taken whole (its decrease is below the rounding of
+  // the distance, so comparing distances would stop it at random near the minimum)
+  double un = clampd(sd.u - d0, c.dom_u0, c.dom_u1), vn = clampd(sd.v - d1, c.dom_v0, c.dom_v1);
+  if (fmax(fabs(d0), fabs(d1)) > kWholeStep) {
+    double alpha = 1;
+    for (int ls = 0;; ++ls) {
+      int hu = sd.hu, hv = sd.hv;
+      fast::SDer<double> e = fast::eval_at<double, P, Q, 0>(c.L64, c.m64, c.p, c.q, un, vn, hu, hv);
+      const v3<double> rn = {e.S.x - px, e.S.y - py, e.S.z - pz};
+      if (dot3(rn, rn) <= f || ls == kMaxHalvings) break;
+      alpha *= 0.5;
+      un = clampd(sd.u - alpha * d0, c.dom_u0, c.dom_u1);
+      vn = clampd(sd.v - alpha * d1, c.dom_v0, c.dom_v1);
+    }
   }
   const double moved = fmax(fabs(un - sd.u), fabs(vn - sd.v));
   sd.u = un;

@@ -708,8 +708,8 @@ int orc_gauss_newton_shipped(const orc_surface* s, const double* M, const double
  *    Hessian J^T J + r.d2S where it is positive definite, J^T J elsewhere; a coordinate at a
  *    bound whose descent direction points out of the domain is held there and the other takes
  *    the 1-D step, Newton where its curvature is positive; the new point is clamped to the
- *    domain), each halved until the distance does
- *    not grow (at most 30 times); converged at a move <= 1e-12 after a Newton step or <= 1e-14
+ *    domain), each halved until the distance does not grow (at most 30 times; steps below 1e-6
+ *    are taken whole, their decrease being below the rounding of the distance); converged at a move <= 1e-12 after a Newton step or <= 1e-14
  *    (1e-12, not the inversion's 1e-10: far points have flat minima, where Newton converges
  *    slowly and a stop at 1e-10 leaves the parameters ~1e-9 apart),
  *    or at a corner where the distance grows into the domain; at most max_iter iterations;
@@ -1052,7 +1052,10 @@ static int project_trajectory(const orc_surface* s, const double* M, const doubl
             return 1;
         }
         if (!(isfinite(d0) && isfinite(d1))) { *iters = it + 1; return 0; }
-        /* line search: halve the step until the distance does not grow (at most 30 times) */
+        /* line search: halve the step until the distance does not grow (at most 30 times); a step
+         * below 1e-6 is taken whole (the decrease it makes is below the rounding of the distance,
+         * so comparing distances would stop it at random near the minimum) */
+        const int search = fmax(fabs(d0), fabs(d1)) > 1e-6;
         double alpha = 1, Cn[2];
         d3 Sn, Snu, Snv, Snuu, Snuv, Snvv;
         for (int ls = 0;; ++ls) {
@@ -1060,7 +1063,7 @@ static int project_trajectory(const orc_surface* s, const double* M, const doubl
             Cn[1] = clampd(C[1] - alpha * d1, dom[2], dom[3]);
             ders2_at(s, M, Cn, &Sn, &Snu, &Snv, &Snuu, &Snuv, &Snvv);
             const d3 rn = {Sn.x - P[0], Sn.y - P[1], Sn.z - P[2]};
-            if (dot3d(rn, rn) <= f || ls == 30) break;
+            if (!search || dot3d(rn, rn) <= f || ls == 30) break;
             alpha *= 0.5;
         }
         const double moved = fmax(fabs(Cn[0] - C[0]), fabs(Cn[1] - C[1]));
