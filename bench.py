@@ -13,8 +13,10 @@ On one GPU the same line also carries sub-records of the other workloads, each w
 clock samples: "batched" (4096 uneven surfaces, one persistent launch from a CUDA graph, mixed vs
 FP64, oracle parity sample), "quintic" (degree 5, 256x256 net, 2^24 queries, per-query parameter
 error against the oracle), "eval_large" (2^26 evaluations of S..Svv, FP64 and FP32, with their
-rooflines) and "serving" (continuous batching over a pool of 10^4 surfaces: peak throughput,
-p50/p99 at half of peak, FP64 server at the top rate).  --headline-only leaves them out.
+rooflines), "project" (nurbs_project of 2^20 points near and far from the 64x64 surface, FP64,
+oracle parity sample) and "serving" (continuous batching over a pool of 10^4 surfaces: peak
+throughput, p50/p99 at half of peak, FP64 server at the top rate).  --headline-only leaves them
+out.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload ...]
 
@@ -351,7 +353,7 @@ def run_ours(a):
         line["cpu_baseline"], line["parity_sample"] = cpu_baseline(surf, P, a.cpu_sample, g_uv, g_st, res_mixed)
     if world == 1 and not a.headline_only and a.workload == "large":
         for name, fn in (("batched", batched_record), ("quintic", quintic_record), ("eval_large", eval_record),
-                         ("serving", serving_record)):
+                         ("project", project_record), ("serving", serving_record)):
             t0 = time.perf_counter()
             try:
                 line[name] = fn(a, compact=True)
@@ -562,6 +564,74 @@ def quintic_record(a, compact=False):
         rec["cpu_baseline"] = {"value": m / dt, "unit": "inversions/s", "cores": host_cores(), "kind": "port",
                                "sample": f"{m} queries of the workload, the oracle's inversion"}
     return rec
+
+
+def projection_queries(surf, s, gn, torch, n, seed):
+    """Projection workload: 80 % of the points off the surface along its normal by up to +-10 %
+    of the control net's extent, 20 % anywhere in a box six extents wide around it."""
+    r = np.random.default_rng(seed)
+    nf = n // 5
+    uv = r.random((n - nf, 2))
+    E = s.eval(torch.as_tensor(uv, device="cuda"), gn.S | gn.SU | gn.SV).cpu().numpy()
+    N = np.cross(E[3:6].T, E[6:9].T)
+    N /= np.linalg.norm(N, axis=1)[:, None]
+    cps = np.asarray(surf["cps"]).reshape(-1, 3)
+    ext = np.ptp(cps, 0).max()
+    near = E[0:3].T + N * ((r.random(n - nf) - 0.5) * 0.2 * ext)[:, None]
+    far = cps.mean(0) + (r.random((nf, 3)) - 0.5) * 6 * ext
+    return np.ascontiguousarray(np.concatenate([near, far]))
+
+
+def project_record(a, compact=False):
+    """Point projection (nurbs_project, FP64) on the 64x64 bicubic surface: 2^20 points, 80 %
+    within 10 % of the extent of the surface, 20 % far from it; projections/s, with parity and
+    the oracle's CPU time on a bounded sample."""
+    import torch
+    gn = load_pkg()
+    from gpu_nurbs_gb300 import synth
+    n = 1 << 20
+    steps = 5 if compact else a.steps
+    surf = synth.surface_large()
+    s = gn.Surface(surf)
+    P = projection_queries(surf, s, gn, torch, n, 2024)
+    Pd = torch.as_tensor(P, device="cuda")
+    out = (torch.empty((n, 2), dtype=torch.float64, device="cuda"), torch.empty(n, dtype=torch.int32, device="cuda"),
+           torch.empty(n, dtype=torch.float64, device="cuda"))
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    timed = event_timer(torch, flush)
+    run = lambda: s.project(Pd, out=out)
+    for _ in range(3):
+        run()
+    torch.cuda.synchronize()
+    clocks = Clocks(0)
+    t = timed(run, steps)
+    clk = clocks.stop()
+    g_uv, g_st, g_res = (x.cpu().numpy() for x in out)
+    ms = sum(t) / len(t)
+    rec = {"value": n / (ms / 1e3), "unit": "projections/s", "ms_per_step": ms, "steps": steps, "dtype": "f64",
+           "config": {"workload": "project-64x64-bicubic-2^20 (80 % within 10 % of the extent, 20 % far)",
+                      "l2": "flushed (512 MB write) before each step"},
+           "found_frac": float(np.mean(g_st <= 1)), "clocks": clk}
+    if not a.no_cpu:
+        import oracle as O
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+        from parity import project_parity
+        m = min(a.cpu_sample // 2, n)
+        idx = np.linspace(0, n - 1, m).astype(np.int64)  # near and far points both
+        o = O.OracleSurface(surf)
+        o.cones()
+        t0 = time.perf_counter()
+        o.project(P[idx], threads=host_cores())
+        dt = time.perf_counter() - t0
+        c = project_parity(o, P[idx], g_uv[idx], g_st[idx], g_res[idx])
+        rec["parity_sample"] = {k: v for k, v in c.items() if k != "fail_idx"}
+        rec["cpu_baseline"] = {"value": m / dt, "unit": "projections/s", "cores": host_cores(), "kind": "port",
+                               "sample": f"{m} points of the workload, evenly spaced, the oracle's projection"}
+    return rec
+
+
+def run_project(a):
+    print(json.dumps(project_record(a)))
 
 
 def measured_hbm_gbs():
@@ -821,7 +891,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="large",
-                    choices=["large", "small", "quintic", "batched", "eval-small", "eval-large", "serving"])
+                    choices=["large", "small", "quintic", "batched", "eval-small", "eval-large", "serving", "project"])
     ap.add_argument("--rates", default="1000,10000,30000,100000,300000,1000000")
     ap.add_argument("--serve-seconds", type=float, default=1.0)
     ap.add_argument("--max-requests", type=int, default=40000)
@@ -844,6 +914,8 @@ def main():
         run_eval(a)
     elif a.workload == "serving":
         run_serving(a)
+    elif a.workload == "project":
+        run_project(a)
     else:
         run_ours(a)
 
