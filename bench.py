@@ -671,15 +671,28 @@ def eval_record(a, compact=False, which="eval-large"):
     def ev32():
         gn.check(L.nurbs_eval_f32(s.h, uv32.data_ptr(), n, mask, out32.data_ptr(), gn._stream()), "eval")
 
+    # the same count of points on a row-major parameter grid (a tessellation: the 32 points of a
+    # warp lie in one or two spans, so the coefficient gathers are broadcasts)
+    side = int(round(n ** 0.5))
+    g = (torch.arange(side, device="cuda", dtype=torch.float32) + 0.5) / side
+    uvg = torch.stack([g.repeat_interleave(side), g.repeat(side)], 1).contiguous()
+    ng = side * side
+
+    def ev32g():
+        gn.check(L.nurbs_eval_f32(s.h, uvg.data_ptr(), ng, mask, out32.data_ptr(), gn._stream()), "eval")
+
     for _ in range(3):
         ev64()
         ev32()
+        ev32g()
     torch.cuda.synchronize()
     clocks = Clocks(0)
     t64 = timed(ev64, steps)
     t32 = timed(ev32, steps)
+    t32g = timed(ev32g, steps)
     clk = clocks.stop()
     ms64, ms32 = sum(t64) / len(t64), sum(t32) / len(t32)
+    ms32g = sum(t32g) / len(t32g)
     peak64, peak32 = fp64_peak_tflops(torch)
     hbm, hbm_src = measured_hbm_gbs()
     k1, k2 = surf["p"] + 1, surf["q"] + 1
@@ -702,9 +715,14 @@ def eval_record(a, compact=False, which="eval-large"):
                      "flop_per_point": flop, "bytes_per_point_fp64": bytes64, "bytes_per_point_fp32": bytes32,
                      "hbm_achieved_gbs": bytes64 * n / (ms64 / 1e3) / 1e9,
                      "fp32": {"bound": "hbm", "achieved": gbs32, "peak": hbm, "unit": "GB/s",
-                              "frac": gbs32 / hbm if hbm else None, "peak_source": hbm_src},
+                              "frac": gbs32 / hbm if hbm else None, "peak_source": hbm_src,
+                              "note": "random (u,v): bound by the L1 wavefronts of per-lane span gathers"},
+                     "fp32_grid": {"points_per_step": ng, "value": ng / (ms32g / 1e3), "ms_per_step": ms32g,
+                                   "bound": "hbm", "achieved": bytes32 * ng / (ms32g / 1e3) / 1e9, "peak": hbm,
+                                   "unit": "GB/s", "frac": bytes32 * ng / (ms32g / 1e3) / 1e9 / hbm if hbm else None,
+                                   "uv": "row-major parameter grid (tessellation order)"},
                      "fp32_achieved_tflops": flop * n / (ms32 / 1e3) / 1e12, "fp32_peak": peak32},
-        "clocks": clk, "gpu_launches": 2 * steps,
+        "clocks": clk, "gpu_launches": 3 * steps,
     }
 
 
