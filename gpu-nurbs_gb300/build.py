@@ -27,9 +27,9 @@ LIB = os.path.join(HERE, "libgpunurbs.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-I" + INCLUDE, "-I" + CSRC,
           "--expt-relaxed-constexpr", "-Wno-deprecated-gpu-targets"]
-EXACT_TUS = {"k_convert.cu", "k_tree.cu", "k_legacy.cu"}
+EXACT_TUS = {"k_convert.cu", "k_tree.cu", "k_legacy.cu", "k_quadtree.cu"}
 EXPLICIT_FMA_TUS = {"k_eval.cu", "k_invert.cu", "k_pool.cu", "k_pcurve.cu", "k_project.cu"}
-SOURCES = ["k_convert.cu", "k_tree.cu", "k_legacy.cu", "k_eval.cu", "k_invert.cu", "api.cpp", "nu_io.cpp", "k_probe.cu", "k_static.cu", "k_pool.cu", "pool.cpp", "server.cpp", "k_pcurve.cu", "k_project.cu"]
+SOURCES = ["k_convert.cu", "k_tree.cu", "k_legacy.cu", "k_eval.cu", "k_invert.cu", "api.cpp", "nu_io.cpp", "k_probe.cu", "k_static.cu", "k_pool.cu", "pool.cpp", "server.cpp", "k_pcurve.cu", "k_project.cu", "k_quadtree.cu"]
 
 
 def nvcc() -> str:

@@ -1,0 +1,266 @@
+// Adaptive quadtree inversion (nurbs_invert_quadtree): the reference's first inversion, which
+// needs no tree build — per query a breadth-first quadtree over the parameter domain, culled by
+// control-net boxes (Inverse, src/kernel/kernel.cu:4-104; BoundingBoxCheck :106-149;
+// getSplitType :251-298; NODE_MAX_SIZE 64, src/kernel/kernel.cuh:13).
+//
+// One warp per query (a persistent grid; warps take queries from a counter):
+//   * a layer's nodes live in shared memory; each node's control-point box is reduced by the
+//     whole warp (lanes stride over the node's control-point rows and columns, min/max by
+//     shuffles: exact, so the pass/fail decisions equal the oracle's);
+//   * the passing nodes' trajectories run one per lane (the inversion's FP64 iteration from the
+//     node centre); a result counts when it converged inside the domain within max_edge of P;
+//   * the first layer with a result answers (its closest result; AMBIGUOUS as in the inversion);
+//     otherwise each passing node is split by the reference's getSplitType, evaluated with the
+//     reference-order FP64 functions (this translation unit is compiled with --fmad=false, so
+//     the split decisions, and with them the tree, are the oracle's bit for bit; the v-length
+//     uses the v-derivative, which the reference takes with MatrixSurfaceDerivativeU), and the
+//     children are compacted into the next layer in the reference's order by a warp prefix sum.
+// Culled nodes are not split (their control-point box does not hold P, so neither does their
+// surface); a layer of more than 64 nodes or 60 layers ends the query unanswered.
+#include "invert_core.cuh"
+
+namespace gnurbs {
+namespace {
+
+using namespace inv;
+
+constexpr int kQtMax = 64;     // nodes per layer (NODE_MAX_SIZE)
+constexpr int kQtLayers = 60;
+
+struct QtWarp {
+  double node[2][kQtMax + 4][4];  // two layers: lb.u, lb.v, rt.u, rt.v
+  double su[kQtMax], sv[kQtMax], sr[kQtMax];
+  unsigned char pass[kQtMax], ok[kQtMax];
+};
+
+__device__ __forceinline__ int knot_span(const int* knot_idx, const double* b, int ns, double x) {
+  return knot_idx[exact::find_seg(b, ns, x)];  // findSpan (Evaluate.cu:504-533) over the breakpoints
+}
+
+// getSplitType: 0 NOT_SPLIT, 1 SPLIT_V, 2 SPLIT_U, 3 SPLIT_UV
+__device__ int split_type(const SurfDev& s, const double* nd, double max_edge) {
+  const int p = s.p, q = s.q, k2 = q + 1, k12 = (p + 1) * (q + 1);
+  const double iu = (nd[2] - nd[0]) / 4, iv = (nd[3] - nd[1]) / 4;
+  double ul = 0, vl = 0;
+  for (int i = 0; i < 4; ++i) {
+    const double x = nd[0] + i * iu, y = nd[1] + i * iv;
+    const int su = exact::find_seg(s.bu, s.ns_u, x), sv = exact::find_seg(s.bv, s.ns_v, y);
+    const double du = s.bu[su + 1] - s.bu[su], dv = s.bv[sv + 1] - s.bv[sv];
+    const double u = (x - s.bu[su]) / du, v = (y - s.bv[sv]) / dv;
+    exact::DenseSpan M{s.m64 + (size_t)(su * s.ns_v + sv) * k12 * 4, k2};
+    const v4<double> R = exact::point_r(M, p, q, u, v);
+    const v3<double> a = exact::der_u(M, p, q, u, v, R, s.range_u / du);
+    const v3<double> b = exact::der_v(M, p, q, u, v, R, s.range_v / dv);
+    ul += sqrt(a.x * a.x + a.y * a.y + a.z * a.z);
+    vl += sqrt(b.x * b.x + b.y * b.y + b.z * b.z);
+  }
+  ul *= (nd[2] - nd[0]) * 0.25;
+  vl *= (nd[3] - nd[1]) * 0.25;
+  if (ul < max_edge && vl < max_edge) return 0;
+  if (nd[2] - nd[0] > 0.25 || nd[3] - nd[1] > 0.25) return 3;
+  if (ul < max_edge) return 1;
+  if (vl < max_edge) return 2;
+  return 3;
+}
+
+__device__ __forceinline__ void put_node(double* o, double a, double b, double c, double d) {
+  o[0] = a;
+  o[1] = b;
+  o[2] = c;
+  o[3] = d;
+}
+
+template <int P, int Q>
+__device__ void quadtree_query(const SurfDev& s, const Ctx& cx, QtWarp& w, const double* __restrict__ Pq, int64_t qi,
+                               double max_edge, double* __restrict__ uv_out, int* __restrict__ st_out,
+                               double* __restrict__ res_out) {
+  const int lane = threadIdx.x & 31;
+  const unsigned FULL = 0xffffffffu;
+  const double px = Pq[3 * qi], py = Pq[3 * qi + 1], pz = Pq[3 * qi + 2];
+  int cur = 0, size = 1, status = 3;
+  bool passed_any = false;
+  double ou = __longlong_as_double(0x7ff8000000000000ll), ov = ou, orr = ou;
+  if (lane == 0) put_node(w.node[0][0], s.dom_u0, s.dom_v0, s.dom_u1, s.dom_v1);
+  __syncwarp();
+  for (int layer = 0; layer < kQtLayers && size > 0; ++layer) {
+    // ---- control-point boxes (BoundingBoxCheck), one node at a time, the warp striding over it
+    for (int i = 0; i < size; ++i) {
+      const double* nd = w.node[cur][i];
+      const int i0 = knot_span(s.knot_u, s.bu, s.ns_u, nd[0]) - s.p, i1 = knot_span(s.knot_u, s.bu, s.ns_u, nd[2]);
+      const int j0 = knot_span(s.knot_v, s.bv, s.ns_v, nd[1]) - s.q, j1 = knot_span(s.knot_v, s.bv, s.ns_v, nd[3]);
+      const int nb = j1 - j0 + 1, cnt = (i1 - i0 + 1) * nb;
+      double mn[3], mx[3];
+      for (int c = 0; c < 3; ++c) {
+        mn[c] = s.cps[3 * ((size_t)i0 * s.nv + j0) + c];
+        mx[c] = mn[c];
+      }
+      for (int e = lane; e < cnt; e += 32) {
+        const double* x = s.cps + 3 * ((size_t)(i0 + e / nb) * s.nv + (j0 + e % nb));
+        for (int c = 0; c < 3; ++c) {
+          mn[c] = mn[c] > x[c] ? x[c] : mn[c];
+          mx[c] = mx[c] < x[c] ? x[c] : mx[c];
+        }
+      }
+      for (int o = 16; o > 0; o >>= 1)
+        for (int c = 0; c < 3; ++c) {
+          mn[c] = fmin(mn[c], __shfl_xor_sync(FULL, mn[c], o));
+          mx[c] = fmax(mx[c], __shfl_xor_sync(FULL, mx[c], o));
+        }
+      const bool pass = px >= mn[0] - max_edge && px <= mx[0] + max_edge && py >= mn[1] - max_edge &&
+                        py <= mx[1] + max_edge && pz >= mn[2] - max_edge && pz <= mx[2] + max_edge;
+      if (lane == 0) w.pass[i] = pass ? 1 : 0;
+      passed_any = passed_any || pass;
+    }
+    __syncwarp();
+    // ---- trajectories of the passing nodes, one per lane
+    for (int i = lane; i < size; i += 32) {
+      w.ok[i] = 0;
+      if (!w.pass[i]) continue;
+      const double* nd = w.node[cur][i];
+      Seed<double> sd;
+      sd.u = (nd[0] + nd[2]) / 2;
+      sd.v = (nd[1] + nd[3]) / 2;
+      sd.prev = INFINITY;
+      sd.it = 0;
+      sd.hu = 0;
+      sd.hv = 0;
+      sd.newton = false;
+      int r = kContinue;
+      while (r == kContinue) r = iterate64<P, Q>(cx, px, py, pz, sd);
+      double rr;
+      if (r == kConverged && finish64<P, Q>(cx, px, py, pz, sd.u, sd.v, sd.hu, sd.hv, rr) && rr < max_edge) {
+        w.ok[i] = 1;
+        w.su[i] = sd.u;
+        w.sv[i] = sd.v;
+        w.sr[i] = rr;
+      }
+    }
+    __syncwarp();
+    // ---- the layer's closest result (ties: the lower node), if any
+    int best = -1;
+    for (int i = 0; i < size; ++i)
+      if (w.ok[i] && (best < 0 || w.sr[i] < w.sr[best])) best = i;
+    if (best >= 0) {
+      status = 0;
+      for (int i = 0; i < size; ++i)
+        if (w.ok[i] && i != best && w.sr[i] <= w.sr[best] * (1 + 1e-6) + 1e-12 &&
+            (fabs(w.su[i] - w.su[best]) > 1e-7 || fabs(w.sv[i] - w.sv[best]) > 1e-7))
+          status = 1;
+      ou = w.su[best];
+      ov = w.sv[best];
+      orr = w.sr[best];
+      break;
+    }
+    // ---- split the passing nodes (getSplitType) and compact their children in node order
+    int nch[2] = {0, 0}, typ[2] = {0, 0};
+    for (int r = 0; r < 2; ++r) {
+      const int i = lane + 32 * r;
+      if (i < size && w.pass[i]) {
+        typ[r] = split_type(s, w.node[cur][i], max_edge);
+        nch[r] = typ[r] == 3 ? 4 : (typ[r] == 0 ? 0 : 2);
+      }
+    }
+    int total = 0, off[2];
+    for (int r = 0; r < 2; ++r) {
+      int incl = nch[r];
+      for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(FULL, incl, o);
+        if (lane >= o) incl += t;
+      }
+      off[r] = total + incl - nch[r];
+      total += __shfl_sync(FULL, incl, 31);
+    }
+    if (total > kQtMax) break;  // layer overflow: unanswered
+    if (total == 0) {
+      status = passed_any ? 3 : 2;
+      break;
+    }
+    for (int r = 0; r < 2; ++r) {
+      const int i = lane + 32 * r;
+      if (nch[r] == 0) continue;
+      const double* nd = w.node[cur][i];
+      const double lx = nd[0], ly = nd[1], rx = nd[2], ry = nd[3];
+      const double mxu = (lx + rx) / 2, myv = (ly + ry) / 2;
+      double* o = w.node[cur ^ 1][off[r]];
+      if (typ[r] == 3) {
+        put_node(o, lx, ly, mxu, myv);
+        put_node(o + 4, lx, myv, mxu, ry);
+        put_node(o + 8, mxu, myv, rx, ry);
+        put_node(o + 12, mxu, ly, rx, myv);
+      } else if (typ[r] == 2) {
+        put_node(o, lx, ly, mxu, ry);
+        put_node(o + 4, mxu, ly, rx, ry);
+      } else {
+        put_node(o, lx, ly, rx, myv);
+        put_node(o + 4, lx, myv, rx, ry);
+      }
+    }
+    __syncwarp();
+    cur ^= 1;
+    size = total;
+  }
+  if (lane == 0) {
+    uv_out[2 * qi] = ou;
+    uv_out[2 * qi + 1] = ov;
+    st_out[qi] = status;
+    res_out[qi] = orr;
+  }
+  __syncwarp();
+}
+
+template <int P, int Q>
+__global__ void __launch_bounds__(kThreads)
+    k_invert_quadtree(SurfDev s, const double* __restrict__ Pq, int64_t n, double max_edge, double* __restrict__ uv_out,
+                      int* __restrict__ st_out, double* __restrict__ res_out, unsigned* __restrict__ counter) {
+  __shared__ QtWarp ww[kWarps];
+  Ctx cx;
+  cx.L32 = fast::global_locator<float>(s);
+  cx.L64 = fast::global_locator<double>(s);
+  cx.m32 = s.m32;
+  cx.m64 = s.m64;
+  cx.p = s.p;
+  cx.q = s.q;
+  cx.dom_u0 = s.dom_u0;
+  cx.dom_u1 = s.dom_u1;
+  cx.dom_v0 = s.dom_v0;
+  cx.dom_v1 = s.dom_v1;
+  QtWarp& w = ww[threadIdx.x >> 5];
+  for (;;) {
+    unsigned qi = 0;
+    if ((threadIdx.x & 31) == 0) qi = atomicAdd(counter, 1u);
+    qi = __shfl_sync(0xffffffffu, qi, 0);
+    if ((int64_t)qi >= n) break;
+    quadtree_query<P, Q>(s, cx, w, Pq, (int64_t)qi, max_edge, uv_out, st_out, res_out);
+  }
+}
+
+template <int P, int Q>
+cudaError_t launch_quadtree_pq(const SurfDev& s, const double* P_, int64_t n, double max_edge, double* uv, int* st_,
+                               double* res, unsigned* counter, cudaStream_t st) {
+  if (n > 0xffffffffLL) return cudaErrorInvalidValue;  // query ids are 32-bit
+  static int cached[64] = {0};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) dev = 0;
+  if (!cached[dev]) {
+    int sms = 0, per_sm = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_invert_quadtree<P, Q>, kThreads, 0);
+    cached[dev] = (sms > 0 ? sms : 1) * (per_sm > 0 ? per_sm : 1);
+  }
+  int64_t blocks = (n + kWarps - 1) / kWarps;
+  if (blocks > cached[dev]) blocks = cached[dev];
+  k_invert_quadtree<P, Q><<<(unsigned)blocks, kThreads, 0, st>>>(s, P_, n, max_edge, uv, st_, res, counter);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_invert_quadtree(const SurfDev& s, const double* P, int64_t n, double max_edge, double* uv,
+                                   int* status, double* residual, unsigned* counter, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  if (s.p == 3 && s.q == 3) return launch_quadtree_pq<3, 3>(s, P, n, max_edge, uv, status, residual, counter, st);
+  return launch_quadtree_pq<0, 0>(s, P, n, max_edge, uv, status, residual, counter, st);
+}
+
+}  // namespace gnurbs

@@ -213,6 +213,17 @@ int nurbs_invert(nurbs_surface_t s, const double* P_dev, int64_t n, double* uv_d
  * (nurbs_surface_create, nurbs_build_tree); single surfaces only (not the pool). */
 int nurbs_project(nurbs_surface_t s, const double* P_dev, int64_t n, double* uv_dev, int* status_dev,
                   double* residual_dev, void* stream);
+/* Adaptive quadtree inversion, the reference's first inversion (Inverse, BoundingBoxCheck,
+ * getSplitType; src/kernel/kernel.cu:4-149, 251-298), which needs no tree: per query a
+ * breadth-first quadtree over the domain; a node passes when P lies in the box of the control
+ * points of its span range widened by max_edge, and seeds an FP64 trajectory at its centre
+ * (nurbs_invert's iteration) that counts when it converges inside the domain within max_edge of
+ * P; the first layer with such a result answers with its closest one.  Nodes that pass are split
+ * by getSplitType (the v-length from the v-derivative); a layer of more than 64 nodes
+ * (NODE_MAX_SIZE) ends the query unanswered.  For points on the surface or within max_edge of
+ * it.  Outputs as nurbs_invert; n < 2^32. */
+int nurbs_invert_quadtree(nurbs_surface_t s, const double* P_dev, int64_t n, double max_edge, double* uv_dev,
+                          int* status_dev, double* residual_dev, void* stream);
 /* Copies the projection's culling data to host memory: nbox[65*6] normal boxes (lb xyz, rt xyz),
  * cone[65*20] FP32 records relative to the control net's centre (bound-box ball centre and radius,
  * cone axis, cos and sin of its half-angle (0 and 1: every direction), bound box rounded outward,

@@ -87,6 +87,9 @@ def lib():
         L.orc_project_perturbed.restype = None
         L.orc_project_perturbed.argtypes = [C.POINTER(_Surf), _dp, _dp, _bp, _fp, _dp, C.c_int64, C.c_int, C.c_int,
                                             C.c_double, _dp, _ip, _dp, C.c_int]
+        L.orc_invert_quadtree.restype = None
+        L.orc_invert_quadtree.argtypes = [C.POINTER(_Surf), _dp, _dp, C.c_int64, C.c_double, C.c_int, _dp, _ip, _dp,
+                                          C.c_void_p, C.c_int]
         L.orc_eval_normal.restype = None
         L.orc_eval_normal.argtypes = [C.POINTER(_Surf), _dp, _dp, C.c_int64, C.c_uint, _dp, C.c_int]
         L.orc_gauss_newton_shipped.restype = C.c_int
@@ -289,6 +292,18 @@ class OracleSurface:
         lib().orc_pcurve(C.byref(self._s), self.matrix_n, np.ascontiguousarray(t.reshape(-1)), b, Cs, n, max_iter,
                          uv, st, res, fl, threads)
         return uv.reshape(n, 2), st, res, fl
+
+    def invert_quadtree(self, P: np.ndarray, max_edge: float, max_iter: int = MAX_ITER, threads: int = 0):
+        """Adaptive quadtree inversion (orc_invert_quadtree): uv (n,2), status, residual, layers."""
+        P = np.ascontiguousarray(P, dtype=np.float64).reshape(-1, 3)
+        n = P.shape[0]
+        uv = np.empty(2 * n, dtype=np.float64)
+        st = np.empty(n, dtype=np.int32)
+        res = np.empty(n, dtype=np.float64)
+        ly = np.empty(n, dtype=np.int32)
+        lib().orc_invert_quadtree(C.byref(self._s), self.matrix_n, P, n, max_edge, max_iter, uv, st, res,
+                                  ly.ctypes.data, threads)
+        return uv.reshape(n, 2), st, res, ly
 
     def gauss_newton_shipped(self, seed, P, max_edge):
         uv = np.zeros(2)

@@ -1480,3 +1480,164 @@ void orc_pcurve(const orc_surface* s, const double* M, const orc_tree_node* tree
     free(st0);
     free(r0);
 }
+
+/* --------------------------------------------------- adaptive quadtree inversion (v1 seeding)
+ * The reference's first inversion (Inverse, src/kernel/kernel.cu:4-104; BoundingBoxCheck
+ * :106-149; getSplitType :251-298; Node, NODE_MAX_SIZE 64, src/kernel/kernel.cuh:13, 30-33)
+ * needs no tree: per query, a breadth-first quadtree over the parameter domain.  The oracle's
+ * definition, with a decision on each defect:
+ *  - the root is the knot domain (the reference starts from [0,1]^2);
+ *  - a node passes when P lies in the box of the control points of its span range, widened by
+ *    max_edge (BoundingBoxCheck: rows findSpan(lb.u) - p .. findSpan(rt.u), the same in v);
+ *  - every passing node seeds one trajectory at its centre (the inversion's trajectory: GN
+ *    update, Newton below a 1e-2 step, converged at 1e-10 / 1e-14, 40 iterations); it succeeds
+ *    when it converged inside the domain with |S - P| < max_edge (the reference's success test);
+ *  - the first layer with a success ends the query: its closest success is the answer (the
+ *    reference returns the first success in node order), AMBIGUOUS as in the inversion;
+ *  - otherwise every passing node is split by getSplitType (4 samples on its diagonal, the
+ *    u- and v-lengths sum |S_u| and |S_v| times a quarter of the side; the reference takes the
+ *    v-derivative with MatrixSurfaceDerivativeU) and its children, in the reference's order,
+ *    form the next layer; nodes that do not pass are not split (the hull is a bound, so their
+ *    subtrees cannot hold an answer; the reference splits every node and overflows its 64-node
+ *    layer at depth 4); NOT_SPLIT nodes end there;
+ *  - a layer of more than 64 nodes, or 60 layers, ends the query unanswered (NOT_CONVERGED); an
+ *    empty layer ends it with NO_CANDIDATE when no node ever passed, else NOT_CONVERGED. */
+
+#define ORC_QT_MAX 64
+#define ORC_QT_LAYERS 60
+
+typedef struct { double lb[2], rt[2]; } qt_node;
+
+static int qt_hull_check(const orc_surface* s, const qt_node* nd, const double* P, double max_edge) {
+    const int p = s->degree_u, q = s->degree_v;
+    const int i0 = orc_find_span(p, s->cp_u, s->knots_u, nd->lb[0]) - p;
+    const int j0 = orc_find_span(q, s->cp_v, s->knots_v, nd->lb[1]) - q;
+    const int i1 = orc_find_span(p, s->cp_u, s->knots_u, nd->rt[0]);
+    const int j1 = orc_find_span(q, s->cp_v, s->knots_v, nd->rt[1]);
+    double mn[3], mx[3];
+    for (int c = 0; c < 3; ++c) mn[c] = mx[c] = s->cps[3 * ((int64_t)i0 * s->cp_v + j0) + c];
+    for (int i = i0; i <= i1; ++i)
+        for (int j = j0; j <= j1; ++j) {
+            const double* x = s->cps + 3 * ((int64_t)i * s->cp_v + j);
+            for (int c = 0; c < 3; ++c) {
+                if (mn[c] > x[c]) mn[c] = x[c];
+                if (mx[c] < x[c]) mx[c] = x[c];
+            }
+        }
+    return P[0] >= mn[0] - max_edge && P[0] <= mx[0] + max_edge && P[1] >= mn[1] - max_edge &&
+           P[1] <= mx[1] + max_edge && P[2] >= mn[2] - max_edge && P[2] <= mx[2] + max_edge;
+}
+
+/* 0 NOT_SPLIT, 1 SPLIT_V, 2 SPLIT_U, 3 SPLIT_UV (getSplitType) */
+static int qt_split_type(const orc_surface* s, const double* M, const qt_node* nd, double max_edge) {
+    const int p = s->degree_u, q = s->degree_v;
+    const double iu = (nd->rt[0] - nd->lb[0]) / 4, iv = (nd->rt[1] - nd->lb[1]) / 4;
+    double ul = 0, vl = 0;
+    for (int i = 0; i < 4; ++i) {
+        span_loc L = locate(s, M, nd->lb[0] + i * iu, nd->lb[1] + i * iv);
+        d4 R = R_of(L.middle, p, q, L.u, L.v);
+        d3 a = der_u(L.middle, p, q, L.u, L.v, R, L.spanU);
+        d3 b = der_v(L.middle, p, q, L.u, L.v, R, L.spanV);
+        ul += sqrt(a.x * a.x + a.y * a.y + a.z * a.z);
+        vl += sqrt(b.x * b.x + b.y * b.y + b.z * b.z);
+    }
+    ul *= (nd->rt[0] - nd->lb[0]) * 0.25;
+    vl *= (nd->rt[1] - nd->lb[1]) * 0.25;
+    if (ul < max_edge && vl < max_edge) return 0;
+    if (nd->rt[0] - nd->lb[0] > 0.25 || nd->rt[1] - nd->lb[1] > 0.25) return 3;
+    if (ul < max_edge) return 1;
+    if (vl < max_edge) return 2;
+    return 3;
+}
+
+/* children of nd by split type t, appended to out (the reference's order) */
+static int qt_children(const qt_node* nd, int t, qt_node* out) {
+    const double lx = nd->lb[0], ly = nd->lb[1], rx = nd->rt[0], ry = nd->rt[1];
+    const double mx = (lx + rx) / 2, my = (ly + ry) / 2;
+    if (t == 3) {
+        qt_node c[4] = {{{lx, ly}, {mx, my}}, {{lx, my}, {mx, ry}}, {{mx, my}, {rx, ry}}, {{mx, ly}, {rx, my}}};
+        memcpy(out, c, sizeof c);
+        return 4;
+    }
+    if (t == 2) {
+        qt_node c[2] = {{{lx, ly}, {mx, ry}}, {{mx, ly}, {rx, ry}}};
+        memcpy(out, c, sizeof c);
+        return 2;
+    }
+    if (t == 1) {
+        qt_node c[2] = {{{lx, ly}, {rx, my}}, {{lx, my}, {rx, ry}}};
+        memcpy(out, c, sizeof c);
+        return 2;
+    }
+    return 0;
+}
+
+void orc_invert_quadtree(const orc_surface* s, const double* M, const double* P, int64_t n, double max_edge,
+                         int max_iter, double* uv, int* status, double* residual, int* layers, int threads) {
+    double dom[4];
+    domain_of(s, dom);
+#ifdef _OPENMP
+    if (threads <= 0) threads = omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 16) num_threads(threads)
+#endif
+    for (int64_t k = 0; k < n; ++k) {
+        const double* Pk = P + 3 * k;
+        qt_node cur[ORC_QT_MAX], nxt[ORC_QT_MAX + 4];
+        int size = 1, passed_any = 0, st = ORC_NOT_CONVERGED, layer = 0;
+        double bu = NAN, bv = NAN, br = NAN;
+        cur[0].lb[0] = dom[0]; cur[0].lb[1] = dom[2]; cur[0].rt[0] = dom[1]; cur[0].rt[1] = dom[3];
+        for (; layer < ORC_QT_LAYERS && size > 0; ++layer) {
+            unsigned char pass[ORC_QT_MAX];
+            double su[ORC_QT_MAX][2], sr[ORC_QT_MAX];
+            int ns = 0;
+            for (int i = 0; i < size; ++i) {
+                pass[i] = (unsigned char)qt_hull_check(s, &cur[i], Pk, max_edge);
+                if (!pass[i]) continue;
+                passed_any = 1;
+                double C[2] = {(cur[i].lb[0] + cur[i].rt[0]) / 2, (cur[i].lb[1] + cur[i].rt[1]) / 2};
+                int its;
+                if (!run_trajectory(s, M, Pk, C, max_iter, 0, &its)) continue;
+                if (!(C[0] >= dom[0] && C[0] <= dom[1] && C[1] >= dom[2] && C[1] <= dom[3])) continue;
+                const double r = dist3(surface_point(s, M, C), Pk);
+                if (!(r < max_edge)) continue;
+                su[ns][0] = C[0];
+                su[ns][1] = C[1];
+                sr[ns] = r;
+                ++ns;
+            }
+            if (ns > 0) {
+                int b = 0;
+                for (int t = 1; t < ns; ++t)
+                    if (sr[t] < sr[b]) b = t;
+                st = ORC_FOUND_UNIQUE;
+                for (int t = 0; t < ns; ++t) {
+                    const int same = fabs(su[t][0] - su[b][0]) <= 1e-7 && fabs(su[t][1] - su[b][1]) <= 1e-7;
+                    if (!same && sr[t] <= sr[b] * (1 + 1e-6) + 1e-12) st = ORC_FOUND_AMBIGUOUS;
+                }
+                bu = su[b][0];
+                bv = su[b][1];
+                br = sr[b];
+                break;
+            }
+            int nn = 0, overflow = 0;
+            for (int i = 0; i < size && !overflow; ++i) {
+                if (!pass[i]) continue;
+                nn += qt_children(&cur[i], qt_split_type(s, M, &cur[i], max_edge), nxt + nn);
+                overflow = nn > ORC_QT_MAX;
+            }
+            if (overflow) { ++layer; break; }
+            if (nn == 0) {
+                st = passed_any ? ORC_NOT_CONVERGED : ORC_NO_CANDIDATE;
+                ++layer;
+                break;
+            }
+            memcpy(cur, nxt, sizeof(qt_node) * nn);
+            size = nn;
+        }
+        uv[2 * k] = bu;
+        uv[2 * k + 1] = bv;
+        status[k] = st;
+        residual[k] = br;
+        if (layers) layers[k] = layer;
+    }
+}

@@ -163,6 +163,14 @@ void orc_project_perturbed(const orc_surface* s, const double* matrix_n, const o
                            const unsigned char* built, const float* cone, const double* P, int64_t n, int max_iter,
                            int K, double eps, double* uv, int* found, double* residual, int threads);
 
+/* Adaptive quadtree inversion (the reference's v1 Inverse with its control-net culling; the
+ * oracle of nurbs_invert_quadtree, definition in nurbs_oracle.c): per query a breadth-first
+ * quadtree over the domain, a trajectory from every node whose widened control-net box holds P,
+ * the first layer with a result within max_edge answers.  uv[2n], status[n], residual[n],
+ * layers[n] (layers visited; may be NULL). */
+void orc_invert_quadtree(const orc_surface* s, const double* matrix_n, const double* P, int64_t n, double max_edge,
+                         int max_iter, double* uv, int* status, double* residual, int* layers, int threads);
+
 /* The reference's GaussNewton exactly as shipped (kernel.cu:151-249): <= 10 steps,
  * success when |S-P| < max_edge before a step.  Returns 1 on success and writes uv. */
 int orc_gauss_newton_shipped(const orc_surface* s, const double* matrix_n, const double seed[2],

@@ -1,0 +1,56 @@
+"""GPU tests of nurbs_invert_quadtree (the adaptive quadtree inversion) against the oracle's
+restatement (oracle.OracleSurface.invert_quadtree)."""
+import numpy as np
+import pytest
+
+import oracle as O
+from test_oracle import tube
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+
+def T(x):
+    return torch.as_tensor(np.ascontiguousarray(x), dtype=torch.float64, device="cuda")
+
+
+def cases():
+    from gpu_nurbs_gb300 import synth
+    return {"small": synth.surface_small(), "large": synth.surface_large(), "tube": tube(24, 8),
+            "rational": synth.surface_random(synth.Rng(77)), "quintic": synth.surface_quintic(n=32)}
+
+
+@pytest.mark.parametrize("which", ["small", "large", "tube", "rational", "quintic"])
+@pytest.mark.parametrize("max_edge", [1e-2, 1e-4])
+def test_quadtree_matches_the_oracle(nurbs, which, max_edge):
+    """Points on the surface, within max_edge of it, and far from it: the same status, the same
+    answer to 1e-9, the same residual to rounding."""
+    sf = cases()[which]
+    s, o = nurbs.Surface(sf), O.OracleSurface(sf)
+    rng = np.random.default_rng(7)
+    uv0 = rng.random((4096, 2))
+    E = o.eval(uv0, 7)
+    N = np.cross(E[3:6].T, E[6:9].T)
+    N /= np.linalg.norm(N, axis=1)[:, None]
+    near = E[0:3].T + N * ((rng.random(4096) - 0.5) * max_edge)[:, None]
+    far = o.cps.mean(0) + (rng.random((256, 3)) - 0.5) * 6 * np.ptp(o.cps, 0).max()
+    P = np.concatenate([E[0:3].T, near, far])
+    uv, st, res = (x.cpu().numpy() for x in s.invert_quadtree(T(P), max_edge))
+    ouv, ost, ores, _ = o.invert_quadtree(P, max_edge)
+    assert np.array_equal(st, ost)
+    f = st <= 1
+    assert np.abs(uv[f] - ouv[f]).max() <= 1e-9
+    assert np.all(np.abs(res[f] - ores[f]) <= 1e-12 * ores[f] + 1e-14)
+    assert np.mean(st[:4096] <= 1) == 1.0
+
+
+def test_quadtree_arguments(nurbs):
+    from gpu_nurbs_gb300 import synth
+    s = nurbs.Surface(synth.surface_small())
+    P = T(np.zeros((4, 3)))
+    with pytest.raises(nurbs.NurbsError):
+        s.invert_quadtree(P, 0.0)
+    with pytest.raises(nurbs.NurbsError):
+        s.invert_quadtree(P, float("nan"))
+    s.invert_quadtree(P[:0], 1e-3)

@@ -366,3 +366,25 @@ def test_oracle_normal_cones_hold_the_sampled_normals():
                                   np.tile(lo[1] + np.arange(9) / 8 * (hi[1] - lo[1]), 9)], 1), 1).T - org
             assert np.abs(lat[k] - Lk).max() <= 1e-6 * max(1.0, np.abs(Lk).max()), k
     assert np.any(O.OracleSurface(synth.surface_small()).cones()[1][:, 7] > 0)
+
+
+def test_oracle_quadtree_inversion():
+    """The adaptive quadtree inversion: points on the surface come back to 1e-12; points within
+    max_edge of it are answered within max_edge; points far from the control net have no
+    passing node (NO_CANDIDATE)."""
+    from gpu_nurbs_gb300 import synth
+    for surf in (synth.surface_small(), synth.surface_large(), tube(24, 8)):
+        o = O.OracleSurface(surf)
+        rng = np.random.default_rng(2)
+        uv0 = rng.random((1000, 2))
+        E = o.eval(uv0, 7)
+        uv, st, res, _ = o.invert_quadtree(E[0:3].T, 1e-3)
+        assert np.all(st <= O.FOUND_AMBIGUOUS)
+        assert np.abs(res).max() <= 1e-12
+        N = np.cross(E[3:6].T, E[6:9].T)
+        N /= np.linalg.norm(N, axis=1)[:, None]
+        P = E[0:3].T + N * ((rng.random(1000) - 0.5) * 1e-3)[:, None]
+        uv, st, res, _ = o.invert_quadtree(P, 1e-3)
+        assert np.mean(st <= O.FOUND_AMBIGUOUS) >= 0.99 and np.all(res[st <= 1] < 1e-3)
+        far = o.cps.max(0) + 1.0 + rng.random((50, 3))
+        assert np.all(o.invert_quadtree(far, 1e-3)[1] == O.NO_CANDIDATE)
