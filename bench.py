@@ -14,7 +14,8 @@ clock samples: "batched" (4096 uneven surfaces, one persistent launch from a CUD
 FP64, oracle parity sample), "quintic" (degree 5, 256x256 net, 2^24 queries, per-query parameter
 error against the oracle), "eval_large" (2^26 evaluations of S..Svv, FP64 and FP32, with their
 rooflines), "project" (nurbs_project of 2^20 points near and far from the 64x64 surface, FP64,
-oracle parity sample) and "serving" (continuous batching over a pool of 10^4 surfaces: peak
+oracle parity sample), "quadtree" (nurbs_invert_quadtree of 2^20 points on that surface, no
+tree build) and "serving" (continuous batching over a pool of 10^4 surfaces: peak
 throughput, p50/p99 at half of peak, FP64 server at the top rate).  --headline-only leaves them
 out.
 
@@ -353,7 +354,7 @@ def run_ours(a):
         line["cpu_baseline"], line["parity_sample"] = cpu_baseline(surf, P, a.cpu_sample, g_uv, g_st, res_mixed)
     if world == 1 and not a.headline_only and a.workload == "large":
         for name, fn in (("batched", batched_record), ("quintic", quintic_record), ("eval_large", eval_record),
-                         ("project", project_record), ("serving", serving_record)):
+                         ("project", project_record), ("quadtree", quadtree_record), ("serving", serving_record)):
             t0 = time.perf_counter()
             try:
                 line[name] = fn(a, compact=True)
@@ -628,6 +629,58 @@ def project_record(a, compact=False):
         rec["cpu_baseline"] = {"value": m / dt, "unit": "projections/s", "cores": host_cores(), "kind": "port",
                                "sample": f"{m} points of the workload, evenly spaced, the oracle's projection"}
     return rec
+
+
+def quadtree_record(a, compact=False):
+    """Adaptive quadtree inversion (nurbs_invert_quadtree, FP64; the reference's first inversion
+    with max_edge 1e-4 as its driver calls it) of 2^20 points on the 64x64 bicubic surface; no
+    tree build.  Inversions/s, parity with the oracle on a bounded sample and its CPU time."""
+    import torch
+    gn = load_pkg()
+    from gpu_nurbs_gb300 import synth
+    n = 1 << 20
+    max_edge = 1e-4
+    steps = 5 if compact else a.steps
+    surf = synth.surface_large()
+    s = gn.Surface(surf)
+    uv0 = np.random.default_rng(99).random((n, 2))
+    P = np.ascontiguousarray(s.eval(torch.as_tensor(uv0, device="cuda"), gn.S).cpu().numpy().T)
+    Pd = torch.as_tensor(P, device="cuda")
+    out = (torch.empty((n, 2), dtype=torch.float64, device="cuda"), torch.empty(n, dtype=torch.int32, device="cuda"),
+           torch.empty(n, dtype=torch.float64, device="cuda"))
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    timed = event_timer(torch, flush)
+    run = lambda: s.invert_quadtree(Pd, max_edge, out=out)
+    for _ in range(3):
+        run()
+    torch.cuda.synchronize()
+    clocks = Clocks(0)
+    t = timed(run, steps)
+    clk = clocks.stop()
+    g_uv, g_st, g_res = (x.cpu().numpy() for x in out)
+    ms = sum(t) / len(t)
+    rec = {"value": n / (ms / 1e3), "unit": "inversions/s", "ms_per_step": ms, "steps": steps, "dtype": "f64",
+           "config": {"workload": "quadtree-64x64-bicubic-2^20 on-surface points, max_edge 1e-4",
+                      "l2": "flushed (512 MB write) before each step"},
+           "found_frac": float(np.mean(g_st <= 1)), "max_uv_err": float(np.abs(g_uv - uv0)[g_st <= 1].max()),
+           "clocks": clk}
+    if not a.no_cpu:
+        import oracle as O
+        m = min(a.cpu_sample, n)
+        o = O.OracleSurface(surf)
+        t0 = time.perf_counter()
+        ouv, ost, ores, _ = o.invert_quadtree(P[:m], max_edge, threads=host_cores())
+        dt = time.perf_counter() - t0
+        f = ost <= 1
+        rec["parity_sample"] = {"n": m, "status_equal": int(np.sum(g_st[:m] == ost)),
+                                "max_uv_diff": float(np.abs(g_uv[:m][f] - ouv[f]).max()) if f.any() else 0.0}
+        rec["cpu_baseline"] = {"value": m / dt, "unit": "inversions/s", "cores": host_cores(), "kind": "port",
+                               "sample": f"first {m} points of the workload, the oracle's quadtree inversion"}
+    return rec
+
+
+def run_quadtree(a):
+    print(json.dumps(quadtree_record(a)))
 
 
 def run_project(a):
@@ -909,7 +962,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="large",
-                    choices=["large", "small", "quintic", "batched", "eval-small", "eval-large", "serving", "project"])
+                    choices=["large", "small", "quintic", "batched", "eval-small", "eval-large", "serving", "project", "quadtree"])
     ap.add_argument("--rates", default="1000,10000,30000,100000,300000,1000000")
     ap.add_argument("--serve-seconds", type=float, default=1.0)
     ap.add_argument("--max-requests", type=int, default=40000)
@@ -934,6 +987,8 @@ def main():
         run_serving(a)
     elif a.workload == "project":
         run_project(a)
+    elif a.workload == "quadtree":
+        run_quadtree(a)
     else:
         run_ours(a)
 
