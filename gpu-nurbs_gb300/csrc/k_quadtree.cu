@@ -29,6 +29,7 @@ constexpr int kQtLayers = 60;
 
 struct QtWarp {
   double node[2][kQtMax + 4][4];  // two layers: lb.u, lb.v, rt.u, rt.v
+  int code[2][kQtMax + 4];        // index of the node's precomputed box, -1 when it has none
   double su[kQtMax], sv[kQtMax], sr[kQtMax];
   unsigned char pass[kQtMax], ok[kQtMax];
 };
@@ -70,42 +71,108 @@ __device__ __forceinline__ void put_node(double* o, double a, double b, double c
   o[3] = d;
 }
 
+// Precomputed boxes of the top kQtDepth levels of square children (depth d, u index a, v index b:
+// code = base(d) + a * 2^d + b; base = 0, 1, 5).  Deeper nodes, and the halves of U / V splits,
+// scan their control points.
+constexpr int kQtDepth = 3;
+constexpr int kQtBoxes = 1 + 4 + 16;
+__device__ __forceinline__ int code_depth(int c) { return c == 0 ? 0 : (c < 5 ? 1 : 2); }
+__device__ __forceinline__ int child_code(int pc, int hu, int hv) {
+  if (pc < 0) return -1;
+  const int d = code_depth(pc);
+  if (d + 1 >= kQtDepth) return -1;
+  const int base = d == 0 ? 0 : 1, side = 1 << d, idx = pc - base;
+  const int a = idx / side, b = idx % side;
+  return (d == 0 ? 1 : 5) + (2 * a + hu) * (2 * side) + (2 * b + hv);
+}
+
+// Partial box over a node's control points (the rows findSpan(lb.u) - p .. findSpan(rt.u), the
+// same in v: BoundingBoxCheck's range), over elements t, t + stride, ...; starts from the first
+// control point of the range, as the reference does.
+__device__ void node_box(const SurfDev& s, const double* nd, int t, int stride, double* mn, double* mx) {
+  const int i0 = knot_span(s.knot_u, s.bu, s.ns_u, nd[0]) - s.p, i1 = knot_span(s.knot_u, s.bu, s.ns_u, nd[2]);
+  const int j0 = knot_span(s.knot_v, s.bv, s.ns_v, nd[1]) - s.q, j1 = knot_span(s.knot_v, s.bv, s.ns_v, nd[3]);
+  const int nb = j1 - j0 + 1, cnt = (i1 - i0 + 1) * nb;
+  for (int c = 0; c < 3; ++c) {
+    mn[c] = s.cps[3 * ((size_t)i0 * s.nv + j0) + c];
+    mx[c] = mn[c];
+  }
+  for (int e = t; e < cnt; e += stride) {
+    const double* x = s.cps + 3 * ((size_t)(i0 + e / nb) * s.nv + (j0 + e % nb));
+    for (int c = 0; c < 3; ++c) {
+      mn[c] = mn[c] > x[c] ? x[c] : mn[c];
+      mx[c] = mx[c] < x[c] ? x[c] : mx[c];
+    }
+  }
+}
+
+// One CTA per precomputed box: the node's rectangle by the same midpoint splits as the search.
+__global__ void __launch_bounds__(256) k_quadtree_boxes(SurfDev s, double* __restrict__ qtbox) {
+  const int code = blockIdx.x;
+  const int d = code_depth(code), side = 1 << d, idx = code - (d == 0 ? 0 : (d == 1 ? 1 : 5));
+  const int a = idx / side, b = idx % side;
+  double nd[4] = {s.dom_u0, s.dom_v0, s.dom_u1, s.dom_v1};
+  for (int l = d - 1; l >= 0; --l) {
+    const int hu = (a >> l) & 1, hv = (b >> l) & 1;
+    const double mu = (nd[0] + nd[2]) / 2, mv = (nd[1] + nd[3]) / 2;
+    if (hu) nd[0] = mu; else nd[2] = mu;
+    if (hv) nd[1] = mv; else nd[3] = mv;
+  }
+  double mn[3], mx[3];
+  node_box(s, nd, threadIdx.x, blockDim.x, mn, mx);
+  __shared__ double red[256][6];
+  for (int c = 0; c < 3; ++c) {
+    red[threadIdx.x][c] = mn[c];
+    red[threadIdx.x][3 + c] = mx[c];
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int j = 1; j < (int)blockDim.x; ++j)
+      for (int c = 0; c < 3; ++c) {
+        mn[c] = fmin(mn[c], red[j][c]);
+        mx[c] = fmax(mx[c], red[j][3 + c]);
+      }
+    for (int c = 0; c < 3; ++c) {
+      qtbox[6 * code + c] = mn[c];
+      qtbox[6 * code + 3 + c] = mx[c];
+    }
+  }
+}
+
 template <int P, int Q>
-__device__ void quadtree_query(const SurfDev& s, const Ctx& cx, QtWarp& w, const double* __restrict__ Pq, int64_t qi,
-                               double max_edge, double* __restrict__ uv_out, int* __restrict__ st_out,
-                               double* __restrict__ res_out) {
+__device__ void quadtree_query(const SurfDev& s, const Ctx& cx, QtWarp& w, const double* __restrict__ qtbox,
+                               const double* __restrict__ Pq, int64_t qi, double max_edge,
+                               double* __restrict__ uv_out, int* __restrict__ st_out, double* __restrict__ res_out) {
   const int lane = threadIdx.x & 31;
   const unsigned FULL = 0xffffffffu;
   const double px = Pq[3 * qi], py = Pq[3 * qi + 1], pz = Pq[3 * qi + 2];
   int cur = 0, size = 1, status = 3;
   bool passed_any = false;
   double ou = __longlong_as_double(0x7ff8000000000000ll), ov = ou, orr = ou;
-  if (lane == 0) put_node(w.node[0][0], s.dom_u0, s.dom_v0, s.dom_u1, s.dom_v1);
+  if (lane == 0) {
+    put_node(w.node[0][0], s.dom_u0, s.dom_v0, s.dom_u1, s.dom_v1);
+    w.code[0][0] = 0;
+  }
   __syncwarp();
   for (int layer = 0; layer < kQtLayers && size > 0; ++layer) {
     // ---- control-point boxes (BoundingBoxCheck), one node at a time, the warp striding over it
     for (int i = 0; i < size; ++i) {
       const double* nd = w.node[cur][i];
-      const int i0 = knot_span(s.knot_u, s.bu, s.ns_u, nd[0]) - s.p, i1 = knot_span(s.knot_u, s.bu, s.ns_u, nd[2]);
-      const int j0 = knot_span(s.knot_v, s.bv, s.ns_v, nd[1]) - s.q, j1 = knot_span(s.knot_v, s.bv, s.ns_v, nd[3]);
-      const int nb = j1 - j0 + 1, cnt = (i1 - i0 + 1) * nb;
       double mn[3], mx[3];
-      for (int c = 0; c < 3; ++c) {
-        mn[c] = s.cps[3 * ((size_t)i0 * s.nv + j0) + c];
-        mx[c] = mn[c];
-      }
-      for (int e = lane; e < cnt; e += 32) {
-        const double* x = s.cps + 3 * ((size_t)(i0 + e / nb) * s.nv + (j0 + e % nb));
+      if (w.code[cur][i] >= 0) {  // the top levels' boxes, computed once per launch
+        const double* b = qtbox + 6 * w.code[cur][i];
         for (int c = 0; c < 3; ++c) {
-          mn[c] = mn[c] > x[c] ? x[c] : mn[c];
-          mx[c] = mx[c] < x[c] ? x[c] : mx[c];
+          mn[c] = b[c];
+          mx[c] = b[3 + c];
         }
+      } else {
+        node_box(s, nd, lane, 32, mn, mx);
+        for (int o = 16; o > 0; o >>= 1)
+          for (int c = 0; c < 3; ++c) {
+            mn[c] = fmin(mn[c], __shfl_xor_sync(FULL, mn[c], o));
+            mx[c] = fmax(mx[c], __shfl_xor_sync(FULL, mx[c], o));
+          }
       }
-      for (int o = 16; o > 0; o >>= 1)
-        for (int c = 0; c < 3; ++c) {
-          mn[c] = fmin(mn[c], __shfl_xor_sync(FULL, mn[c], o));
-          mx[c] = fmax(mx[c], __shfl_xor_sync(FULL, mx[c], o));
-        }
       const bool pass = px >= mn[0] - max_edge && px <= mx[0] + max_edge && py >= mn[1] - max_edge &&
                         py <= mx[1] + max_edge && pz >= mn[2] - max_edge && pz <= mx[2] + max_edge;
       if (lane == 0) w.pass[i] = pass ? 1 : 0;
@@ -182,17 +249,24 @@ __device__ void quadtree_query(const SurfDev& s, const Ctx& cx, QtWarp& w, const
       const double lx = nd[0], ly = nd[1], rx = nd[2], ry = nd[3];
       const double mxu = (lx + rx) / 2, myv = (ly + ry) / 2;
       double* o = w.node[cur ^ 1][off[r]];
+      int* oc = w.code[cur ^ 1] + off[r];
+      const int pc = w.code[cur][i];
       if (typ[r] == 3) {
         put_node(o, lx, ly, mxu, myv);
         put_node(o + 4, lx, myv, mxu, ry);
         put_node(o + 8, mxu, myv, rx, ry);
         put_node(o + 12, mxu, ly, rx, myv);
-      } else if (typ[r] == 2) {
-        put_node(o, lx, ly, mxu, ry);
-        put_node(o + 4, mxu, ly, rx, ry);
+        const int hu[4] = {0, 0, 1, 1}, hv[4] = {0, 1, 1, 0};
+        for (int c = 0; c < 4; ++c) oc[c] = child_code(pc, hu[c], hv[c]);
       } else {
-        put_node(o, lx, ly, rx, myv);
-        put_node(o + 4, lx, myv, rx, ry);
+        if (typ[r] == 2) {
+          put_node(o, lx, ly, mxu, ry);
+          put_node(o + 4, mxu, ly, rx, ry);
+        } else {
+          put_node(o, lx, ly, rx, myv);
+          put_node(o + 4, lx, myv, rx, ry);
+        }
+        oc[0] = oc[1] = -1;
       }
     }
     __syncwarp();
@@ -210,8 +284,9 @@ __device__ void quadtree_query(const SurfDev& s, const Ctx& cx, QtWarp& w, const
 
 template <int P, int Q>
 __global__ void __launch_bounds__(kThreads)
-    k_invert_quadtree(SurfDev s, const double* __restrict__ Pq, int64_t n, double max_edge, double* __restrict__ uv_out,
-                      int* __restrict__ st_out, double* __restrict__ res_out, unsigned* __restrict__ counter) {
+    k_invert_quadtree(SurfDev s, const double* __restrict__ qtbox, const double* __restrict__ Pq, int64_t n,
+                      double max_edge, double* __restrict__ uv_out, int* __restrict__ st_out,
+                      double* __restrict__ res_out, unsigned* __restrict__ counter) {
   __shared__ QtWarp ww[kWarps];
   Ctx cx;
   cx.L32 = fast::global_locator<float>(s);
@@ -230,7 +305,7 @@ __global__ void __launch_bounds__(kThreads)
     if ((threadIdx.x & 31) == 0) qi = atomicAdd(counter, 1u);
     qi = __shfl_sync(0xffffffffu, qi, 0);
     if ((int64_t)qi >= n) break;
-    quadtree_query<P, Q>(s, cx, w, Pq, (int64_t)qi, max_edge, uv_out, st_out, res_out);
+    quadtree_query<P, Q>(s, cx, w, qtbox, Pq, (int64_t)qi, max_edge, uv_out, st_out, res_out);
   }
 }
 
@@ -250,7 +325,8 @@ cudaError_t launch_quadtree_pq(const SurfDev& s, const double* P_, int64_t n, do
   }
   int64_t blocks = (n + kWarps - 1) / kWarps;
   if (blocks > cached[dev]) blocks = cached[dev];
-  k_invert_quadtree<P, Q><<<(unsigned)blocks, kThreads, 0, st>>>(s, P_, n, max_edge, uv, st_, res, counter);
+  k_quadtree_boxes<<<kQtBoxes, 256, 0, st>>>(s, s.qtbox);
+  k_invert_quadtree<P, Q><<<(unsigned)blocks, kThreads, 0, st>>>(s, s.qtbox, P_, n, max_edge, uv, st_, res, counter);
   return cudaGetLastError();
 }
 

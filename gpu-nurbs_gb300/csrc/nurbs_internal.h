@@ -42,6 +42,8 @@ constexpr int kConeStride = 20;   // floats per normal-cone record
 //                                    rt 12..14), zero (15..19)
 //   lattice[65][81][3]               surface points of each node's 9x9 lattice (index 9 tx + ty),
 //                                    FP32 relative to org: distance bounds and projection seeds
+//   qtbox[21][6]                     control-point boxes of the quadtree inversion's square nodes of
+//                                    depth 0..2, written by each quadtree launch
 struct SurfDev {
   int p, q, nu, nv;
   int ns_u, ns_v;
@@ -76,6 +78,7 @@ struct SurfDev {
   double* nbox;           // normal cones (see above)
   float* cone;
   float* lattice;
+  double* qtbox;          // control-point boxes of the quadtree inversion's top levels (21 x 6)
 };
 
 // Tree node in the reference TreeNode order (src/kernel/kernel.cuh:30-39), 80 bytes.

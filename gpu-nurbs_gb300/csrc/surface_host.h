@@ -42,7 +42,7 @@ struct SurfaceHost {
   size_t o_bu, o_bv, o_idu, o_idv, o_bu32, o_bv32, o_idu32, o_idv32, o_iu, o_iv, o_ku, o_kv, o_cps, o_w, o_tree,
       o_div, o_built, in_bytes;
   // offsets inside the computed part
-  size_t o_m64, o_m32, o_bas_u, o_bas_v, o_cd32, o_cd64, o_nbox, o_cone, o_lat, out_bytes;
+  size_t o_m64, o_m32, o_bas_u, o_bas_v, o_cd32, o_cd64, o_nbox, o_cone, o_lat, o_qtb, out_bytes;
 };
 
 // Validates and prepares a surface given by host arrays.  Returns NURBS_OK or an error code,
@@ -118,6 +118,7 @@ inline int prepare_surface(int p, int q, int nu, int nv, const double* ku, const
   S.o_nbox = take(kTreeNodes * 6 * 8);
   S.o_cone = take(kTreeNodes * kConeStride * 4);
   S.o_lat = take(kTreeNodes * kPts * kPts * 3 * 4);
+  S.o_qtb = take(21 * 6 * 8);
   S.out_bytes = off;
   return NURBS_OK;
 }
@@ -177,6 +178,7 @@ inline void fill_surface(const SurfaceHost& S, char* img, char* in_dev, char* ou
   d.nbox = (double*)(out_dev + S.o_nbox);
   d.cone = (float*)(out_dev + S.o_cone);
   d.lattice = (float*)(out_dev + S.o_lat);
+  d.qtbox = (double*)(out_dev + S.o_qtb);
 }
 
 }  // namespace gnurbs
