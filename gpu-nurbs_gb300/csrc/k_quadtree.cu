@@ -3,7 +3,9 @@
 // control-net boxes (Inverse, src/kernel/kernel.cu:4-104; BoundingBoxCheck :106-149;
 // getSplitType :251-298; NODE_MAX_SIZE 64, src/kernel/kernel.cuh:13).
 //
-// One warp per query (a persistent grid; warps take queries from a counter):
+// A persistent grid whose warps take chunks of 32 queries from a counter.  The first layer (the
+// root: its precomputed box and one trajectory from the domain's centre) runs lane per query and
+// answers most queries; a query it leaves open is then searched by the whole warp:
 //   * a layer's nodes live in shared memory; each node's control-point box is reduced by the
 //     whole warp (lanes stride over the node's control-point rows and columns, min/max by
 //     shuffles: exact, so the pass/fail decisions equal the oracle's);
@@ -139,9 +141,12 @@ __global__ void __launch_bounds__(256) k_quadtree_boxes(SurfDev s, double* __res
   }
 }
 
+// The whole warp searches one query's tree.  root_failed: the root passed and its trajectory had
+// no result (the chunk's lane-per-query first layer found that), so layer 0 goes straight to the
+// split.
 template <int P, int Q>
 __device__ void quadtree_query(const SurfDev& s, const Ctx& cx, QtWarp& w, const double* __restrict__ qtbox,
-                               const double* __restrict__ Pq, int64_t qi, double max_edge,
+                               const double* __restrict__ Pq, int64_t qi, double max_edge, bool root_failed,
                                double* __restrict__ uv_out, int* __restrict__ st_out, double* __restrict__ res_out) {
   const int lane = threadIdx.x & 31;
   const unsigned FULL = 0xffffffffu;
@@ -155,8 +160,16 @@ __device__ void quadtree_query(const SurfDev& s, const Ctx& cx, QtWarp& w, const
   }
   __syncwarp();
   for (int layer = 0; layer < kQtLayers && size > 0; ++layer) {
+    const bool known = layer == 0 && root_failed;
+    if (known) {
+      if (lane == 0) {
+        w.pass[0] = 1;
+        w.ok[0] = 0;
+      }
+      passed_any = true;
+    }
     // ---- control-point boxes (BoundingBoxCheck), one node at a time, the warp striding over it
-    for (int i = 0; i < size; ++i) {
+    for (int i = 0; i < (known ? 0 : size); ++i) {
       const double* nd = w.node[cur][i];
       double mn[3], mx[3];
       if (w.code[cur][i] >= 0) {  // the top levels' boxes, computed once per launch
@@ -180,7 +193,7 @@ __device__ void quadtree_query(const SurfDev& s, const Ctx& cx, QtWarp& w, const
     }
     __syncwarp();
     // ---- trajectories of the passing nodes, one per lane
-    for (int i = lane; i < size; i += 32) {
+    for (int i = lane; i < (known ? 0 : size); i += 32) {
       w.ok[i] = 0;
       if (!w.pass[i]) continue;
       const double* nd = w.node[cur][i];
@@ -300,19 +313,65 @@ __global__ void __launch_bounds__(kThreads)
   cx.dom_v0 = s.dom_v0;
   cx.dom_v1 = s.dom_v1;
   QtWarp& w = ww[threadIdx.x >> 5];
+  const int lane = threadIdx.x & 31;
+  const unsigned FULL = 0xffffffffu;
+  // chunks of 32 queries: the first layer (the root, one node) lane per query, which answers most
+  // queries; the warp then searches the rest one by one from the root's split
+  const int64_t chunks = (n + 31) / 32;
   for (;;) {
-    unsigned qi = 0;
-    if ((threadIdx.x & 31) == 0) qi = atomicAdd(counter, 1u);
-    qi = __shfl_sync(0xffffffffu, qi, 0);
-    if ((int64_t)qi >= n) break;
-    quadtree_query<P, Q>(s, cx, w, qtbox, Pq, (int64_t)qi, max_edge, uv_out, st_out, res_out);
+    unsigned ch = 0;
+    if (lane == 0) ch = atomicAdd(counter, 1u);
+    ch = __shfl_sync(FULL, ch, 0);
+    if ((int64_t)ch >= chunks) break;
+    const int64_t qi = (int64_t)ch * 32 + lane;
+    bool rest = false;
+    if (qi < n) {
+      const double px = Pq[3 * qi], py = Pq[3 * qi + 1], pz = Pq[3 * qi + 2];
+      const bool pass = px >= qtbox[0] - max_edge && px <= qtbox[3] + max_edge && py >= qtbox[1] - max_edge &&
+                        py <= qtbox[4] + max_edge && pz >= qtbox[2] - max_edge && pz <= qtbox[5] + max_edge;
+      int status = 2;  // the root alone does not pass: no node ever passes
+      double ou = __longlong_as_double(0x7ff8000000000000ll), ov = ou, orr = ou;
+      if (pass) {
+        Seed<double> sd;
+        sd.u = (s.dom_u0 + s.dom_u1) / 2;
+        sd.v = (s.dom_v0 + s.dom_v1) / 2;
+        sd.prev = INFINITY;
+        sd.it = 0;
+        sd.hu = 0;
+        sd.hv = 0;
+        sd.newton = false;
+        int r = kContinue;
+        while (r == kContinue) r = iterate64<P, Q>(cx, px, py, pz, sd);
+        double rr;
+        if (r == kConverged && finish64<P, Q>(cx, px, py, pz, sd.u, sd.v, sd.hu, sd.hv, rr) && rr < max_edge) {
+          status = 0;
+          ou = sd.u;
+          ov = sd.v;
+          orr = rr;
+        } else {
+          rest = true;
+        }
+      }
+      if (!rest) {
+        uv_out[2 * qi] = ou;
+        uv_out[2 * qi + 1] = ov;
+        st_out[qi] = status;
+        res_out[qi] = orr;
+      }
+    }
+    unsigned m = __ballot_sync(FULL, rest);
+    while (m) {
+      const int j = __ffs(m) - 1;
+      m &= m - 1;
+      quadtree_query<P, Q>(s, cx, w, qtbox, Pq, (int64_t)ch * 32 + j, max_edge, true, uv_out, st_out, res_out);
+    }
   }
 }
 
 template <int P, int Q>
 cudaError_t launch_quadtree_pq(const SurfDev& s, const double* P_, int64_t n, double max_edge, double* uv, int* st_,
                                double* res, unsigned* counter, cudaStream_t st) {
-  if (n > 0xffffffffLL) return cudaErrorInvalidValue;  // query ids are 32-bit
+  if ((n + 31) / 32 > 0xffffffffLL) return cudaErrorInvalidValue;  // chunk ids are 32-bit
   static int cached[64] = {0};
   int dev = 0;
   cudaGetDevice(&dev);
@@ -323,7 +382,7 @@ cudaError_t launch_quadtree_pq(const SurfDev& s, const double* P_, int64_t n, do
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_invert_quadtree<P, Q>, kThreads, 0);
     cached[dev] = (sms > 0 ? sms : 1) * (per_sm > 0 ? per_sm : 1);
   }
-  int64_t blocks = (n + kWarps - 1) / kWarps;
+  int64_t blocks = ((n + 31) / 32 + kWarps - 1) / kWarps;
   if (blocks > cached[dev]) blocks = cached[dev];
   k_quadtree_boxes<<<kQtBoxes, 256, 0, st>>>(s, s.qtbox);
   k_invert_quadtree<P, Q><<<(unsigned)blocks, kThreads, 0, st>>>(s, s.qtbox, P_, n, max_edge, uv, st_, res, counter);
