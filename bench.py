@@ -13,8 +13,8 @@ On one GPU the same line also carries sub-records of the other workloads, each w
 clock samples: "batched" (4096 uneven surfaces, one persistent launch from a CUDA graph, mixed vs
 FP64, oracle parity sample), "quintic" (degree 5, 256x256 net, 2^24 queries, per-query parameter
 error against the oracle), "eval_large" (2^26 evaluations of S..Svv, FP64 and FP32, with their
-rooflines), "project" (nurbs_project of 2^20 points near and far from the 64x64 surface, FP64,
-oracle parity sample), "quadtree" (nurbs_invert_quadtree of 2^20 points on that surface, no
+rooflines), "project" (nurbs_project of 2^20 points near and far from the 64x64 surface, mixed and
+FP64, oracle parity sample), "quadtree" (nurbs_invert_quadtree of 2^20 points on that surface, no
 tree build) and "serving" (continuous batching over a pool of 10^4 surfaces: peak
 throughput, p50/p99 at half of peak, FP64 server at the top rate).  --headline-only leaves them
 out.
@@ -584,9 +584,9 @@ def projection_queries(surf, s, gn, torch, n, seed):
 
 
 def project_record(a, compact=False):
-    """Point projection (nurbs_project, FP64) on the 64x64 bicubic surface: 2^20 points, 80 %
-    within 10 % of the extent of the surface, 20 % far from it; projections/s, with parity and
-    the oracle's CPU time on a bounded sample."""
+    """Point projection (nurbs_project, mixed and FP64) on the 64x64 bicubic surface: 2^20 points,
+    80 % within 10 % of the extent of the surface, 20 % far from it; projections/s, with parity of
+    the mixed results and the oracle's CPU time on a bounded sample."""
     import torch
     gn = load_pkg()
     from gpu_nurbs_gb300 import synth
@@ -600,16 +600,21 @@ def project_record(a, compact=False):
            torch.empty(n, dtype=torch.float64, device="cuda"))
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     timed = event_timer(torch, flush)
-    run = lambda: s.project(Pd, out=out)
+    run = lambda: s.project(Pd, gn.PREC_MIXED, out=out)
+    run64 = lambda: s.project(Pd, gn.PREC_FP64, out=out)
     for _ in range(3):
         run()
+    run64()
     torch.cuda.synchronize()
     clocks = Clocks(0)
     t = timed(run, steps)
+    t64 = timed(run64, max(2, steps // 2))
     clk = clocks.stop()
+    run()
     g_uv, g_st, g_res = (x.cpu().numpy() for x in out)
-    ms = sum(t) / len(t)
-    rec = {"value": n / (ms / 1e3), "unit": "projections/s", "ms_per_step": ms, "steps": steps, "dtype": "f64",
+    ms, ms64 = sum(t) / len(t), sum(t64) / len(t64)
+    rec = {"value": n / (ms / 1e3), "unit": "projections/s", "ms_per_step": ms, "steps": steps, "dtype": "f32+f64",
+           "fp64_value": n / (ms64 / 1e3), "fp64_ms_per_step": ms64, "mixed_vs_fp64": ms64 / ms,
            "config": {"workload": "project-64x64-bicubic-2^20 (80 % within 10 % of the extent, 20 % far)",
                       "l2": "flushed (512 MB write) before each step"},
            "found_frac": float(np.mean(g_st <= 1)), "clocks": clk}

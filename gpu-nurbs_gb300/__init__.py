@@ -92,7 +92,7 @@ SIGNATURES = {
     "nurbs_invert_host": (C.c_int, [_vp, _vp, _i64, _vp, _vp, _vp, C.c_int, _vp]),
     "nurbs_invert_count": (C.c_int, [_vp, _vp, _i64, C.c_int, _vp, _vp]),
     "nurbs_pcurve": (C.c_int, [_vp, _vp, _i64, _vp, _vp, _vp, _vp, C.c_int, _vp]),
-    "nurbs_project": (C.c_int, [_vp, _vp, _i64, _vp, _vp, _vp, _vp]),
+    "nurbs_project": (C.c_int, [_vp, _vp, _i64, _vp, _vp, _vp, C.c_int, _vp]),
     "nurbs_invert_quadtree": (C.c_int, [_vp, _vp, _i64, C.c_double, _vp, _vp, _vp, _vp]),
     "nurbs_normal_cones_export": (C.c_int, [_vp, _vp, _vp, _vp]),
     "nurbs_eval_normal": (C.c_int, [_vp, _vp, _i64, C.c_uint, _vp, _vp]),
@@ -315,9 +315,9 @@ class Surface:
               "nurbs_invert")
         return uv, st, res
 
-    def project(self, P, stream=None, out=None):
-        """Closest point over the closed domain (nurbs_project, FP64): P (n,3) float64 CUDA
-        tensor -> (uv (n,2), status (n,), residual (n,))."""
+    def project(self, P, precision: int = PREC_FP64, stream=None, out=None):
+        """Closest point over the closed domain (nurbs_project): P (n,3) float64 CUDA tensor ->
+        (uv (n,2), status (n,), residual (n,))."""
         torch = _torch()
         P = P.contiguous()
         n = P.shape[0]
@@ -327,7 +327,7 @@ class Surface:
             res = torch.empty(n, dtype=torch.float64, device=P.device)
         else:
             uv, st, res = out
-        check(lib().nurbs_project(self.h, _ptr(P), n, _ptr(uv), _ptr(st), _ptr(res), _stream(stream)),
+        check(lib().nurbs_project(self.h, _ptr(P), n, _ptr(uv), _ptr(st), _ptr(res), precision, _stream(stream)),
               "nurbs_project")
         return uv, st, res
 

@@ -103,8 +103,8 @@ struct nurbs_surface_s {
 // Enqueues one inversion on `st`: waits for the previous user of the counter slot, zeroes the
 // counter, launches, marks the slot.  Inside a stream capture the slot is used without the
 // event handshake (capture cannot wait on work recorded outside it).
-// precision: NURBS_PREC_FP64 / MIXED for the inversion, -1 for the projection (FP64), -2 for the
-// adaptive quadtree inversion (FP64, max_edge)
+// precision: NURBS_PREC_FP64 / MIXED for the inversion, -1 / -3 for the projection (FP64 / mixed),
+// -2 for the adaptive quadtree inversion (FP64, max_edge)
 static cudaError_t invert_on(nurbs_surface_s* s, const double* P, int64_t n, double* uv, int* status, double* res,
                              int precision, cudaStream_t st, double max_edge = 0) {
   std::lock_guard<std::mutex> lk(s->mu);
@@ -126,8 +126,9 @@ static cudaError_t invert_on(nurbs_surface_s* s, const double* P, int64_t n, dou
   if (e == cudaSuccess) {
     if (precision == -2)
       e = launch_invert_quadtree(s->dev, P, n, max_edge, uv, status, res, s->counters + slot, st);
-    else if (precision == -1)
-      e = launch_project(s->dev, P, n, uv, status, res, s->counters + slot, st);
+    else if (precision == -1 || precision == -3)
+      e = launch_project(s->dev, P, n, uv, status, res, precision == -3 ? NURBS_PREC_MIXED : NURBS_PREC_FP64,
+                         s->counters + slot, st);
     else
       e = launch_invert(s->dev, P, n, uv, status, res, precision, s->counters + slot, st);
   }
@@ -383,12 +384,16 @@ int nurbs_normal_cones_export(nurbs_surface_t s, double* nbox_host, float* cone_
 }
 
 int nurbs_project(nurbs_surface_t s, const double* P_dev, int64_t n, double* uv_dev, int* status_dev,
-                  double* residual_dev, void* stream) {
+                  double* residual_dev, int precision, void* stream) {
   if (!s) return fail(NURBS_E_INVALID, "NULL surface");
   if (n < 0) return fail(NURBS_E_INVALID, "negative count");
+  if (precision != NURBS_PREC_FP64 && precision != NURBS_PREC_MIXED)
+    return fail(NURBS_E_INVALID, "precision %d is not FP64 or MIXED", precision);
   if (n == 0) return NURBS_OK;
   if (!P_dev || !uv_dev || !status_dev || !residual_dev) return fail(NURBS_E_INVALID, "NULL buffer");
-  CUDA_TRY(invert_on(s, P_dev, n, uv_dev, status_dev, residual_dev, -1, (cudaStream_t)stream), "project launch");
+  CUDA_TRY(invert_on(s, P_dev, n, uv_dev, status_dev, residual_dev, precision == NURBS_PREC_MIXED ? -3 : -1,
+                     (cudaStream_t)stream),
+           "project launch");
   return NURBS_OK;
 }
 

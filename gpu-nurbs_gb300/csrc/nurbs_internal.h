@@ -151,7 +151,7 @@ cudaError_t launch_pcurve_passes(const SurfDev& s, const double* C, int64_t n, c
 cudaError_t launch_cones(const SurfDev& s, cudaStream_t st);
 // the projection: closest point over the closed domain (k_project.cu)
 cudaError_t launch_project(const SurfDev& s, const double* P, int64_t n, double* uv, int* status,
-                           double* residual, unsigned* counter, cudaStream_t st);
+                           double* residual, int precision, unsigned* counter, cudaStream_t st);
 // adaptive quadtree inversion (k_quadtree.cu)
 cudaError_t launch_invert_quadtree(const SurfDev& s, const double* P, int64_t n, double max_edge, double* uv,
                                    int* status, double* residual, unsigned* counter, cudaStream_t st);

@@ -208,11 +208,13 @@ int nurbs_invert(nurbs_surface_t s, const double* P_dev, int64_t n, double* uv_d
  * built nodes whose bound box (the node's box intersected with its control points' box) is within
  * a distance bound from lattice points and whose normal cone can face P (both signs); each is
  * seeded at its 9x9 lattice point closest to P and runs projected Newton steps with a line search
- * inside the domain, so minima on the domain's boundary are found too.  FP64.  Outputs as
+ * inside the domain, so minima on the domain's boundary are found too.  precision:
+ * NURBS_PREC_FP64, or NURBS_PREC_MIXED (the trajectories in FP32, then FP64 projected Newton
+ * steps from the best result, and from the best of another grid cell within 5 %).  Outputs as
  * nurbs_invert (NURBS_INV_NO_CANDIDATE only for non-finite P).  The cones are built with the tree
  * (nurbs_surface_create, nurbs_build_tree); single surfaces only (not the pool). */
 int nurbs_project(nurbs_surface_t s, const double* P_dev, int64_t n, double* uv_dev, int* status_dev,
-                  double* residual_dev, void* stream);
+                  double* residual_dev, int precision, void* stream);
 /* Adaptive quadtree inversion, the reference's first inversion (Inverse, BoundingBoxCheck,
  * getSplitType; src/kernel/kernel.cu:4-149, 251-298), which needs no tree: per query a
  * breadth-first quadtree over the domain; a node passes when P lies in the box of the control

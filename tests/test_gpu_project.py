@@ -44,18 +44,20 @@ def test_normal_cones_bit_exact(nurbs, which):
     assert np.array_equal(gl[b].view(np.int32), ol[b].view(np.int32))
 
 
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "mixed"])
 @pytest.mark.parametrize("which", ["large", "small", "rational", "quintic"])
-def test_project_parity(nurbs, which):
+def test_project_parity(nurbs, which, precision):
     """Points up to 10 % of the extent off the surface along its normal and points far from it
     (a box six extents wide): every answer the oracle's, UNSTABLE queries (the oracle's own
     answer changes for perturbations at FP32 resolution) no farther than the farthest of its
-    answers."""
+    answers.  Mixed precision: FOUND_UNIQUE failures within the chaos bound of the mixed
+    inversion."""
     sf = surfaces()[which]
     s, o = nurbs.Surface(sf), O.OracleSurface(sf)
     P = _projection_queries(o, 4096, 11, 0.2)
-    uv, st, res = (x.cpu().numpy() for x in s.project(T(P)))
+    uv, st, res = (x.cpu().numpy() for x in s.project(T(P), precision))
     c = project_parity(o, P, uv, st, res)
-    assert_exact(c, which, 0)
+    assert_exact(c, which, precision)
     assert np.all(st <= 1)
 
 
@@ -68,7 +70,7 @@ def test_project_on_the_surface_recovers_the_parameters(nurbs):
     o = O.OracleSurface(sf)
     uv0 = np.random.default_rng(4).random((8192, 2))
     P = o.eval(uv0, 1).T.copy()
-    uv, st, res = (x.cpu().numpy() for x in s.project(T(P)))
+    uv, st, res = (x.cpu().numpy() for x in s.project(T(P), nurbs.PREC_MIXED))
     assert np.all(st <= 1)
     assert res.max() <= 1e-12
     assert np.abs(uv - uv0)[st == 0].max() <= 1e-9
@@ -94,4 +96,9 @@ def test_project_edge_cases(nurbs):
     ouv, ost, ores, _ = o.project(P[:-1])
     assert np.abs(uv[:-1] - ouv).max() <= 1e-9
     assert np.all(np.abs(res[:-1] - ores) <= 1e-12 * ores + 1e-14)
-    assert nurbs.lib().nurbs_project(s.h, None, 4, None, None, None, None) == nurbs.E_INVALID
+    assert nurbs.lib().nurbs_project(s.h, None, 4, None, None, None, 0, None) == nurbs.E_INVALID
+    assert nurbs.lib().nurbs_project(s.h, None, 0, None, None, None, 7, None) == nurbs.E_INVALID
+    for prec in (0, 1):
+        uv, st, res = (x.cpu().numpy() for x in s.project(T(P), prec))
+        assert st[-1] == nurbs.INV_NO_CANDIDATE
+        assert np.abs(uv[:-1] - ouv).max() <= 1e-9

@@ -125,6 +125,44 @@ def test_uploads_evict_least_recently_used(nurbs, request):
     srv.close()
 
 
+def test_queries_while_uploads_evict(nurbs, request):
+    """Queries submitted while uploads force evictions: a query against a surface that is no longer
+    resident is refused at submission; every accepted query completes with the results the same
+    surface gives alone (an evicted surface is never released while a queued request uses it)."""
+    from gpu_nurbs_gb300 import synth
+    surfs, _ = synth.batched_surfaces(32, seed=13)
+    sizes = [nurbs.surface_bytes(s) for s in surfs]
+    slot_bytes = 4 * (4096 * 52 + 1024)
+    pool = nurbs.Pool(int(sum(sorted(sizes)[-4:]) + 4 * slot_bytes + (4 << 20)), max_surfaces=64)
+    srv = nurbs.Server(pool, slots=2, max_batch_queries=4096)
+    request.addfinalizer(srv.close)
+    rng = np.random.default_rng(5)
+    ids, accepted, refused = [], [], 0
+    for k, sf in enumerate(surfs):
+        t, sid = srv.submit_upload(sf)
+        for j in range(3):  # queries against recent surfaces while this upload may evict them
+            if not ids:
+                break
+            pick = int(rng.integers(max(0, len(ids) - 4), len(ids)))
+            P = queries(surfs[pick], int(rng.integers(16, 512)), rng)
+            try:
+                tq, out = srv.submit_invert(ids[pick], P)
+                accepted.append((tq, pick, P, out))
+            except nurbs.NurbsError:
+                refused += 1
+        assert srv.wait(t) == 0
+        ids.append(int(sid[0]))
+    for tq, pick, P, out in accepted:
+        assert srv.wait(tq) == 0
+        ref = [x.cpu().numpy() for x in nurbs.Surface(surfs[pick]).invert(torch.as_tensor(P, device="cuda"),
+                                                                           nurbs.PREC_MIXED)]
+        assert same_within_tolerance(out[:3], ref, P)
+    assert len(accepted) > 0
+    info = pool.info()
+    assert info.surfaces < len(surfs)
+    srv.close()
+
+
 def test_replay_trace(nurbs, served, request):
     surfs, pool, ids = served
     rng = np.random.default_rng(6)
