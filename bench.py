@@ -590,7 +590,7 @@ def project_record(a, compact=False):
     import torch
     gn = load_pkg()
     from gpu_nurbs_gb300 import synth
-    n = 1 << 20
+    n = (1 << 20) if compact else a.queries
     steps = 5 if compact else a.steps
     surf = synth.surface_large()
     s = gn.Surface(surf)
@@ -615,7 +615,7 @@ def project_record(a, compact=False):
     ms, ms64 = sum(t) / len(t), sum(t64) / len(t64)
     rec = {"value": n / (ms / 1e3), "unit": "projections/s", "ms_per_step": ms, "steps": steps, "dtype": "f32+f64",
            "fp64_value": n / (ms64 / 1e3), "fp64_ms_per_step": ms64, "mixed_vs_fp64": ms64 / ms,
-           "config": {"workload": "project-64x64-bicubic-2^20 (80 % within 10 % of the extent, 20 % far)",
+           "config": {"workload": f"project-64x64-bicubic-{n} points (80 % within 10 % of the extent, 20 % far)",
                       "l2": "flushed (512 MB write) before each step"},
            "found_frac": float(np.mean(g_st <= 1)), "clocks": clk}
     if not a.no_cpu:
@@ -643,7 +643,7 @@ def quadtree_record(a, compact=False):
     import torch
     gn = load_pkg()
     from gpu_nurbs_gb300 import synth
-    n = 1 << 20
+    n = (1 << 20) if compact else a.queries
     max_edge = 1e-4
     steps = 5 if compact else a.steps
     surf = synth.surface_large()
@@ -665,7 +665,7 @@ def quadtree_record(a, compact=False):
     g_uv, g_st, g_res = (x.cpu().numpy() for x in out)
     ms = sum(t) / len(t)
     rec = {"value": n / (ms / 1e3), "unit": "inversions/s", "ms_per_step": ms, "steps": steps, "dtype": "f64",
-           "config": {"workload": "quadtree-64x64-bicubic-2^20 on-surface points, max_edge 1e-4",
+           "config": {"workload": f"quadtree-64x64-bicubic-{n} on-surface points, max_edge 1e-4",
                       "l2": "flushed (512 MB write) before each step"},
            "found_frac": float(np.mean(g_st <= 1)), "max_uv_err": float(np.abs(g_uv - uv0)[g_st <= 1].max()),
            "clocks": clk}
