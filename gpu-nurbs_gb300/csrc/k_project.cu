@@ -457,8 +457,11 @@ struct ProjSmem {
   static constexpr size_t bytes = ww + sizeof(ProjWarp<MODE>) * kWarps;
 };
 
+// Register budget: the FP64 schedule keeps 168 registers (3 CTAs per SM); the mixed one of a
+// specialised degree is held to 5 CTAs per SM, its FP32 exploration latency-bound at 3 (the
+// generic-degree variant would spill 18 KB at that budget and keeps 3).
 template <int P, int Q, int MODE>
-__global__ void __launch_bounds__(kThreads, 3)
+__global__ void __launch_bounds__(kThreads, (MODE == kModeMixed && P != 0) ? 5 : 3)
     k_project(SurfDev s, const double* __restrict__ Pq, int64_t n, double* __restrict__ uv_out,
               int* __restrict__ st_out, double* __restrict__ res_out, unsigned* __restrict__ counter) {
   extern __shared__ __align__(16) unsigned char smem[];
