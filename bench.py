@@ -232,9 +232,7 @@ def run_ours(a):
     if world > 1:
         dist.init_process_group("nccl")
     gn = load_pkg()
-    n = a.queries
-    if a.workload == "quintic" and n == (1 << 20):
-        n = 1 << 24   # the quintic workload's query count
+    n = a.queries or ((1 << 24) if a.workload == "quintic" else (1 << 20))
     surf, s, uv_true, P = make_workload(gn, torch, a.workload, n, 1000 + rank)
     Pd = torch.as_tensor(P, device="cuda")
     uv = torch.empty((n, 2), dtype=torch.float64, device="cuda")
@@ -590,7 +588,7 @@ def project_record(a, compact=False):
     import torch
     gn = load_pkg()
     from gpu_nurbs_gb300 import synth
-    n = (1 << 20) if compact else a.queries
+    n = (1 << 20) if compact or not a.queries else a.queries
     steps = 5 if compact else a.steps
     surf = synth.surface_large()
     s = gn.Surface(surf)
@@ -643,7 +641,7 @@ def quadtree_record(a, compact=False):
     import torch
     gn = load_pkg()
     from gpu_nurbs_gb300 import synth
-    n = (1 << 20) if compact else a.queries
+    n = (1 << 20) if compact or not a.queries else a.queries
     max_edge = 1e-4
     steps = 5 if compact else a.steps
     surf = synth.surface_large()
@@ -710,7 +708,7 @@ def eval_record(a, compact=False, which="eval-large"):
     small = which == "eval-small"
     surf = synth.surface_small() if small else synth.surface_large()
     mask = 7 if small else 63
-    n = (1 << 20) if small else (1 << 26)
+    n = ((1 << 20) if small else (1 << 26)) if compact or not a.queries else a.queries
     steps = 8 if compact else a.steps
     s = gn.Surface(surf)
     r = synth.Rng(synth.SEED_BASE + 77)
@@ -952,7 +950,7 @@ def run_reference(a):
         "steps": a.steps, "warmup": a.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "fp64", "data": "synthetic (seeded)",
         "config": {"workload": workload_label(a.workload if a.workload in ("large", "small", "quintic") else "small",
-                                              (1 << 24) if a.workload == "quintic" else a.queries),
+                                              a.queries or ((1 << 24) if a.workload == "quintic" else (1 << 20))),
                    "queries_per_step": len(P), "note": "each step inverts a bounded sample of the workload"},
         "cpu_baseline": {"value": v, "unit": "inversions/s", "cores": cores, "kind": kind,
                          "sample": f"{len(P)} queries per step (bounded sample of the workload), all host cores"},
@@ -976,7 +974,8 @@ def main():
     ap.add_argument("--serve-chunk", type=int, default=16, help="queries per warp chunk when serving")
     ap.add_argument("--surfaces", type=int, default=4096)
     ap.add_argument("--tune-queries", type=int, default=4 << 20)
-    ap.add_argument("--queries", type=int, default=1 << 20)
+    ap.add_argument("--queries", type=int, default=None,
+                    help="points per step (default: 2^20; quintic 2^24; eval-large 2^26)")
     ap.add_argument("--cpu-sample", type=int, default=1 << 14)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--headline-only", action="store_true",
