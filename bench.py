@@ -108,7 +108,7 @@ class Clocks:
 # same kernel on the same workload, per unit of work so that they scale to the launch size:
 # traffic grows with the number of queries or points.
 TRAFFIC_PER_UNIT = {
-    "large": (33.88e6 + 16.49e6) / (1 << 20),   # mixed k_invert, bytes per query (2^20-query capture)
+    "large": (38.02e6 + 27.69e6) / (1 << 20),   # mixed k_invert, bytes per query (2^20-query capture)
     "eval-large": (69.05e6 + 542.67e6) / (1 << 22),  # FP64 k_eval S..Svv, bytes per point (2^22 points)
 }
 
