@@ -27,7 +27,7 @@ E_INVALID, E_CUDA, E_NOMEM, E_IO, E_PARSE, E_UNSUPPORTED, E_BUDGET, E_TIMEOUT, E
 S, SU, SV, SUU, SUV, SVV = 1, 2, 4, 8, 16, 32
 SUUU, SUUV, SUVV, SVVV = 64, 128, 256, 512
 N, NU, NV, NUU, NUV, NVV = 1, 2, 4, 8, 16, 32
-PREC_FP64, PREC_MIXED, PREC_FP32 = 0, 1, 2
+PREC_FP64, PREC_MIXED, PREC_FP32, PREC_EXACT = 0, 1, 2, 3
 PCURVE_JUMP, PCURVE_AMBIGUOUS, PCURVE_NOT_FOUND = 1, 2, 4
 INV_FOUND, INV_AMBIGUOUS, INV_NO_CANDIDATE, INV_NOT_CONVERGED = 0, 1, 2, 3
 PTR_HOST, PTR_DEVICE = 0, 1
@@ -253,14 +253,15 @@ class Surface:
         check(lib().nurbs_get_matrix_n(self.h, _ptr(out), _stream(stream)), "nurbs_get_matrix_n")
         return out
 
-    def eval(self, uv, mask: int = S, stream=None):
-        """uv: (n,2) float64 CUDA tensor -> (3*nblocks, n) float64 SoA tensor."""
+    def eval(self, uv, mask: int = S, stream=None, precision: int = PREC_FP64):
+        """uv: (n,2) float64 CUDA tensor -> (3*nblocks, n) float64 SoA tensor.  precision
+        PREC_EXACT: the reference's FP64 expressions term by term (mask <= 63)."""
         torch = _torch()
         uv = uv.contiguous()
         n = uv.shape[0]
         nb = bin(mask & 1023).count("1")
         out = torch.empty((3 * nb, n), dtype=torch.float64, device=uv.device)
-        check(lib().nurbs_eval(self.h, _ptr(uv), n, mask, _ptr(out), PREC_FP64, _stream(stream)), "nurbs_eval")
+        check(lib().nurbs_eval(self.h, _ptr(uv), n, mask, _ptr(out), precision, _stream(stream)), "nurbs_eval")
         return out
 
     def eval_normal(self, uv, mask: int = N, stream=None):

@@ -310,10 +310,16 @@ int nurbs_eval(nurbs_surface_t s, const double* uv_dev, int64_t n, unsigned mask
   if (!s) return fail(NURBS_E_INVALID, "NULL surface");
   if (n < 0) return fail(NURBS_E_INVALID, "negative count");
   if (mask == 0 || mask > 1023u) return fail(NURBS_E_INVALID, "mask 0x%x outside 1..1023", mask);
-  if (precision != NURBS_PREC_FP64) return fail(NURBS_E_INVALID, "nurbs_eval computes in FP64; use nurbs_eval_f32");
+  if (precision != NURBS_PREC_FP64 && precision != NURBS_PREC_EXACT)
+    return fail(NURBS_E_INVALID, "nurbs_eval computes in FP64 (NURBS_PREC_FP64 or NURBS_PREC_EXACT); use nurbs_eval_f32");
+  if (precision == NURBS_PREC_EXACT && mask > 63u)
+    return fail(NURBS_E_INVALID, "NURBS_PREC_EXACT evaluates to second order (mask <= 63)");
   if (n == 0) return NURBS_OK;
   if (!uv_dev || !out_dev) return fail(NURBS_E_INVALID, "NULL buffer");
-  CUDA_TRY(launch_eval_f64(s->dev, uv_dev, n, mask, out_dev, (cudaStream_t)stream), "eval launch");
+  if (precision == NURBS_PREC_EXACT)
+    CUDA_TRY(launch_eval_exact(s->dev, uv_dev, n, mask, out_dev, (cudaStream_t)stream), "eval launch");
+  else
+    CUDA_TRY(launch_eval_f64(s->dev, uv_dev, n, mask, out_dev, (cudaStream_t)stream), "eval launch");
   return NURBS_OK;
 }
 

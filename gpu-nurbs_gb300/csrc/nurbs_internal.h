@@ -104,6 +104,8 @@ cudaError_t launch_eval_f64(const SurfDev& s, const double* uv, int64_t n, unsig
                             cudaStream_t st);
 cudaError_t launch_eval_f32(const SurfDev& s, const float* uv, int64_t n, unsigned mask, float* out,
                             cudaStream_t st);
+cudaError_t launch_eval_exact(const SurfDev& s, const double* uv, int64_t n, unsigned mask, double* out,
+                              cudaStream_t st);
 cudaError_t launch_eval_normal(const SurfDev& s, const double* uv, int64_t n, unsigned mask, double* out,
                                cudaStream_t st);
 cudaError_t launch_evaluate_random(const double* uv, double* xyz, int64_t n, const double* matrix_n, int p,

@@ -68,6 +68,8 @@ extern "C" {
 #define NURBS_PREC_FP64   0   /* every iteration and contraction in FP64 */
 #define NURBS_PREC_MIXED  1   /* FP32 seeding/early iterations, FP64 final 2 steps + residual */
 #define NURBS_PREC_FP32   2   /* evaluation only: FP32 contraction of the FP32 span matrices */
+#define NURBS_PREC_EXACT  3   /* nurbs_eval only: the reference's FP64 expressions term by term
+                                 (bit-identical to its functions at every degree; mask <= 63) */
 
 /* inversion status per query */
 #define NURBS_INV_FOUND        0   /* converged, in-domain, best candidate unique */

@@ -72,6 +72,45 @@ def test_eval_within_1e12(nurbs, cuda, path):
     assert max(errs) <= 1e-12, errs
 
 
+@pytest.mark.parametrize("path", MODEL_FILES, ids=ids)
+def test_eval_exact_bit_exact(nurbs, cuda, path):
+    """NURBS_PREC_EXACT evaluation equals the reference's own FP64 functions bit for bit (the
+    golden fixtures), degree 5 models included."""
+    g = load_golden(path)
+    s = nurbs.Surface(surf_of(g))
+    ev = s.eval(T(g["uv"], cuda), 63, precision=nurbs.PREC_EXACT).cpu().numpy()
+    ref = g["eval"]
+    ok = np.isfinite(ref)
+    assert np.array_equal(ev[ok].view(np.int64), ref[ok].view(np.int64))
+
+
+@pytest.mark.parametrize("which", ["quintic", "deg7"])
+def test_eval_exact_high_degree_matches_the_oracle(nurbs, cuda, which):
+    """At degrees 5 and 7, where the Horner path differs from the reference's formulation by the
+    power basis's conditioning, NURBS_PREC_EXACT equals the oracle (the reference's expressions)
+    bit for bit, also at span boundaries and domain corners."""
+    from gpu_nurbs_gb300 import synth
+    if which == "quintic":
+        surf = synth.surface_quintic(n=32)
+    else:
+        r = np.random.default_rng(3)
+        nu = nv = 12
+        surf = dict(p=7, q=7, nu=nu, nv=nv, knots_u=synth.uniform_knots(7, nu), knots_v=synth.uniform_knots(7, nv),
+                    cps=np.stack([np.repeat(np.linspace(0, 1, nu), nv), np.tile(np.linspace(0, 1, nv), nu),
+                                  0.1 * r.standard_normal(nu * nv)], 1), weights=r.uniform(0.5, 2, nu * nv))
+    o = O.OracleSurface(surf)
+    rng = np.random.default_rng(4)
+    uv = rng.random((4096, 2))
+    ku = np.unique(surf["knots_u"])
+    uv[:64, 0] = rng.choice(ku, 64)
+    uv[64:68] = [[0, 0], [0, 1], [1, 0], [1, 1]]
+    s = nurbs.Surface(surf)
+    ev = s.eval(T(uv, cuda), 63, precision=nurbs.PREC_EXACT).cpu().numpy()
+    assert np.array_equal(ev.view(np.int64), o.eval(uv, 63).view(np.int64))
+    with pytest.raises(nurbs.NurbsError):
+        s.eval(T(uv, cuda), 64, precision=nurbs.PREC_EXACT)
+
+
 @pytest.mark.parametrize("mask", [1, 7, 2, 9, 32, 63])
 def test_eval_masks(nurbs, cuda, mask):
     g = load_golden(MODEL_FILES[-1])
