@@ -201,6 +201,8 @@ bool dispatch(nurbs_server_s* S, Slot& sl, std::deque<Request*>& pending) {
   return true;
 }
 
+constexpr int kPollUs = 20;  // the scheduler's sleep between polls of the in-flight batches
+
 void scheduler_main(nurbs_server_s* S) {
   std::deque<Request*> pending;
   while (!S->stop.load()) {
@@ -230,7 +232,14 @@ void scheduler_main(nurbs_server_s* S) {
     if (!S->paused.load())
       for (auto& sl : S->slots)
         if (!sl.busy && !pending.empty()) progress |= dispatch(S, sl, pending);
-    if (!progress) std::this_thread::yield();
+    if (!progress) {
+      // Batches in flight and nothing to start: sleep until a request arrives (submit notifies
+      // cv_work) or kPollUs passes, then poll the slots' events again.  A bounded wait: the
+      // thread does not spin on a host core, and a completion is seen within kPollUs (plus the
+      // timer's slack) of the GPU finishing.
+      std::unique_lock<std::mutex> lock(S->mu);
+      if (S->incoming.empty() && !S->stop.load()) S->cv_work.wait_for(lock, std::chrono::microseconds(kPollUs));
+    }
   }
   // shutdown: finish what is in flight, fail what never started
   for (auto& sl : S->slots)
