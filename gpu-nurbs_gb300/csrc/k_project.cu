@@ -17,8 +17,12 @@
 //   3. the converged results are merged into per-query records (grid cells of the domain, as in
 //      the inversion) and the closest wins; AMBIGUOUS when another minimum is as close.
 // The warp's (query, seed) pairs are flattened into a task list as in the FP64 inversion
-// (round-major), every lane pulling the next task when its seed ends.  FP64 throughout: the
-// iteration count per seed is small and its line search needs distances at full precision.
+// (round-major), every lane pulling the next task when its seed ends.  Two schedules (template
+// MODE): FP64 — every trajectory in FP64; MIXED — the trajectories in FP32 (tables relative to
+// the control net's centre; steps below kWholeStep32 skip the line search, whose distance
+// comparisons are rounding noise there), each query's best result and best of another grid cell
+// kept, then FP64 projected Newton steps from the best, and from the other when it is within
+// kPolishMargin of it or the best fails.
 #include "invert_core.cuh"
 
 namespace gnurbs {
