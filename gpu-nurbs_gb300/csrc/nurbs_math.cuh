@@ -225,6 +225,13 @@ GN_HD v4<double> rd(const Acc& M, int k1, int k2, const double* vu, const double
   mv(M, k1, k2, vv, tmp);
   return dot4(vu, tmp, k1);
 }
+// the same contracting u first (MatrixSurfaceRdVV, Evaluate.cu:384-405)
+template <class Acc>
+GN_HD v4<double> rd_ufirst(const Acc& M, int k1, int k2, const double* vu, const double* vv) {
+  double tmp[4][kMaxDegree + 1];
+  vm(M, k1, k2, vu, tmp);
+  return dot4(vv, tmp, k2);
+}
 GN_HD v4<double> scale4(v4<double> a, double s) { return {a.x * s, a.y * s, a.z * s, a.w * s}; }
 GN_HD v3<double> cross(v3<double> a, v3<double> b) {  // cross_product, src/util/Matrix.cu:62-64
   return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
@@ -244,7 +251,7 @@ GN_HD void ders3(const Acc& M, int p, int q, double u, double v, double su, doub
   const v4<double> Rv = scale4(rd(M, k1, k2, U[0], V[1]), sv);
   const v4<double> Ruu = scale4(scale4(rd(M, k1, k2, U[2], V[0]), su), su);
   const v4<double> Ruv = scale4(scale4(rd(M, k1, k2, U[1], V[1]), su), sv);
-  const v4<double> Rvv = scale4(scale4(rd(M, k1, k2, U[0], V[2]), sv), sv);
+  const v4<double> Rvv = scale4(scale4(rd_ufirst(M, k1, k2, U[0], V[2]), sv), sv);
   const v4<double> Ruuu = scale4(scale4(scale4(rd(M, k1, k2, U[3], V[0]), su), su), su);
   const v4<double> Ruuv = scale4(scale4(scale4(rd(M, k1, k2, U[2], V[1]), su), su), sv);
   const v4<double> Ruvv = scale4(scale4(scale4(rd(M, k1, k2, U[1], V[2]), su), sv), sv);

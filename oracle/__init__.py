@@ -90,6 +90,14 @@ def lib():
         L.orc_invert_quadtree.restype = None
         L.orc_invert_quadtree.argtypes = [C.POINTER(_Surf), _dp, _dp, C.c_int64, C.c_double, C.c_int, _dp, _ip, _dp,
                                           C.c_void_p, C.c_int]
+        L.orc_qt_hull_check.restype = C.c_int
+        L.orc_qt_hull_check.argtypes = [C.POINTER(_Surf), _dp, _dp, C.c_double]
+        L.orc_qt_split_type.restype = C.c_int
+        L.orc_qt_split_type.argtypes = [C.POINTER(_Surf), _dp, _dp, C.c_double, C.c_int]
+        L.orc_ders3.restype = None
+        L.orc_ders3.argtypes = [C.POINTER(_Surf), _dp, C.c_double, C.c_double, _dp]
+        L.orc_normals.restype = None
+        L.orc_normals.argtypes = [C.POINTER(_Surf), _dp, C.c_double, C.c_double, _dp]
         L.orc_eval_normal.restype = None
         L.orc_eval_normal.argtypes = [C.POINTER(_Surf), _dp, _dp, C.c_int64, C.c_uint, _dp, C.c_int]
         L.orc_gauss_newton_shipped.restype = C.c_int
@@ -305,6 +313,22 @@ class OracleSurface:
                                   ly.ctypes.data, threads)
         return uv.reshape(n, 2), st, res, ly
 
+    def qt_hull_check(self, node4, P, max_edge):
+        return int(lib().orc_qt_hull_check(C.byref(self._s), np.ascontiguousarray(node4, np.float64),
+                                           np.ascontiguousarray(P, np.float64), max_edge))
+
+    def qt_split_type(self, node4, max_edge, as_reference=False):
+        return int(lib().orc_qt_split_type(C.byref(self._s), self.matrix_n, np.ascontiguousarray(node4, np.float64),
+                                           max_edge, 1 if as_reference else 0))
+
+    def ders3(self, u, v):
+        """S..Svvv (10, 3) and N, Nu, Nv, Nuu, Nuv, Nvv (6, 3) at one parameter pair."""
+        d = np.zeros(30)
+        nrm = np.zeros(18)
+        lib().orc_ders3(C.byref(self._s), self.matrix_n, float(u), float(v), d)
+        lib().orc_normals(C.byref(self._s), self.matrix_n, float(u), float(v), nrm)
+        return d.reshape(10, 3), nrm.reshape(6, 3)
+
     def gauss_newton_shipped(self, seed, P, max_edge):
         uv = np.zeros(2)
         ok = lib().orc_gauss_newton_shipped(C.byref(self._s), self.matrix_n, np.asarray(seed, np.float64),
@@ -336,6 +360,12 @@ def ref_lib():
         R.ref_gauss_newton.argtypes = [C.c_int] * 4 + [_dp, _dp, _dp, _dp, _dp, C.c_double, _dp]
         R.ref_find_span.restype = C.c_int
         R.ref_find_span.argtypes = [C.c_int, C.c_int, _dp, C.c_double]
+        R.ref_ders3.restype = None
+        R.ref_ders3.argtypes = [C.c_int] * 4 + [_dp, _dp, _dp, C.c_double, C.c_double, _dp]
+        R.ref_qt_box_check.restype = C.c_int
+        R.ref_qt_box_check.argtypes = [C.c_int] * 4 + [_dp, _dp, _dp, _dp, _dp, C.c_double]
+        R.ref_qt_split_type.restype = C.c_int
+        R.ref_qt_split_type.argtypes = [C.c_int] * 4 + [_dp, _dp, _dp, _dp, C.c_double]
         _ref = R
     return _ref
 
@@ -390,6 +420,22 @@ class RefSurface:
             out.append(np.array([i for i in range(TREE_NODES)
                                  if b[i] and self.R.ref_box_check(np.ascontiguousarray(t[i]), pk)], dtype=np.int32))
         return out
+
+    def ders3(self, u, v):
+        """The reference's new-style derivatives (14, 3): S..Svvv, N, Nuu, Nuv, Nvv."""
+        out = np.zeros(42)
+        self.R.ref_ders3(*self._dims(), self.o.ku, self.o.kv, self.matrix_n, float(u), float(v), out)
+        return out.reshape(14, 3)
+
+    def qt_box_check(self, node4, P, max_edge):
+        return int(self.R.ref_qt_box_check(*self._dims(), self.o.ku, self.o.kv,
+                                           np.ascontiguousarray(self.o.cps.reshape(-1)),
+                                           np.ascontiguousarray(node4, np.float64),
+                                           np.ascontiguousarray(P, np.float64), max_edge))
+
+    def qt_split_type(self, node4, max_edge):
+        return int(self.R.ref_qt_split_type(*self._dims(), self.o.ku, self.o.kv, self.matrix_n,
+                                            np.ascontiguousarray(node4, np.float64), max_edge))
 
     def gauss_newton_shipped(self, node_uv4, P, max_edge):
         uv = np.zeros(2)

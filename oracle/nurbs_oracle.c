@@ -424,6 +424,17 @@ static d4 rd(const double* middle, int k1, int k2, const double* vu, const doubl
     mv4(middle, k1, k2, vv, tmp);
     return dot4(vu, k1, tmp);
 }
+/* the same contracting u first (MatrixSurfaceRdVV, Evaluate.cu:384-405) */
+static d4 rd_ufirst(const double* middle, int k1, int k2, const double* vu, const double* vv) {
+    double tmp[4][8];
+    d4 r;
+    for (int c = 0; c < 4; ++c) mat_mult(vu, middle + c * k1 * k2, tmp[c], 1, k1, k2);
+    mat_mult(tmp[0], vv, &r.x, 1, k2, 1);
+    mat_mult(tmp[1], vv, &r.y, 1, k2, 1);
+    mat_mult(tmp[2], vv, &r.z, 1, k2, 1);
+    mat_mult(tmp[3], vv, &r.w, 1, k2, 1);
+    return r;
+}
 static d4 d4s(d4 a, double s) { d4 o = {a.x * s, a.y * s, a.z * s, a.w * s}; return o; }
 static d3 cross3(d3 a, d3 b) {   /* cross_product, src/util/Matrix.cu:62-64 */
     d3 o = {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
@@ -444,7 +455,7 @@ void orc_ders3(const orc_surface* s, const double* M, double uu, double vv, doub
     d4 Rv = d4s(rd(L.middle, k1, k2, U[0], V[1]), sv);
     d4 Ruu = d4s(d4s(rd(L.middle, k1, k2, U[2], V[0]), su), su);
     d4 Ruv = d4s(d4s(rd(L.middle, k1, k2, U[1], V[1]), su), sv);
-    d4 Rvv = d4s(d4s(rd(L.middle, k1, k2, U[0], V[2]), sv), sv);
+    d4 Rvv = d4s(d4s(rd_ufirst(L.middle, k1, k2, U[0], V[2]), sv), sv);
     d4 Ruuu = d4s(d4s(d4s(rd(L.middle, k1, k2, U[3], V[0]), su), su), su);
     d4 Ruuv = d4s(d4s(d4s(rd(L.middle, k1, k2, U[2], V[1]), su), su), sv);
     d4 Ruvv = d4s(d4s(d4s(rd(L.middle, k1, k2, U[1], V[2]), su), sv), sv);
@@ -1528,8 +1539,10 @@ static int qt_hull_check(const orc_surface* s, const qt_node* nd, const double* 
            P[1] <= mx[1] + max_edge && P[2] >= mn[2] - max_edge && P[2] <= mx[2] + max_edge;
 }
 
-/* 0 NOT_SPLIT, 1 SPLIT_V, 2 SPLIT_U, 3 SPLIT_UV (getSplitType) */
-static int qt_split_type(const orc_surface* s, const double* M, const qt_node* nd, double max_edge) {
+/* 0 NOT_SPLIT, 1 SPLIT_V, 2 SPLIT_U, 3 SPLIT_UV (getSplitType); as_reference: the v-length from
+ * MatrixSurfaceDerivativeU with spanV, as the reference computes it (for pinning only). */
+static int qt_split_type_x(const orc_surface* s, const double* M, const qt_node* nd, double max_edge,
+                           int as_reference) {
     const int p = s->degree_u, q = s->degree_v;
     const double iu = (nd->rt[0] - nd->lb[0]) / 4, iv = (nd->rt[1] - nd->lb[1]) / 4;
     double ul = 0, vl = 0;
@@ -1537,7 +1550,7 @@ static int qt_split_type(const orc_surface* s, const double* M, const qt_node* n
         span_loc L = locate(s, M, nd->lb[0] + i * iu, nd->lb[1] + i * iv);
         d4 R = R_of(L.middle, p, q, L.u, L.v);
         d3 a = der_u(L.middle, p, q, L.u, L.v, R, L.spanU);
-        d3 b = der_v(L.middle, p, q, L.u, L.v, R, L.spanV);
+        d3 b = as_reference ? der_u(L.middle, p, q, L.u, L.v, R, L.spanV) : der_v(L.middle, p, q, L.u, L.v, R, L.spanV);
         ul += sqrt(a.x * a.x + a.y * a.y + a.z * a.z);
         vl += sqrt(b.x * b.x + b.y * b.y + b.z * b.z);
     }
@@ -1548,6 +1561,20 @@ static int qt_split_type(const orc_surface* s, const double* M, const qt_node* n
     if (ul < max_edge) return 1;
     if (vl < max_edge) return 2;
     return 3;
+}
+
+static int qt_split_type(const orc_surface* s, const double* M, const qt_node* nd, double max_edge) {
+    return qt_split_type_x(s, M, nd, max_edge, 0);
+}
+
+int orc_qt_hull_check(const orc_surface* s, const double node4[4], const double P[3], double max_edge) {
+    qt_node nd = {{node4[0], node4[1]}, {node4[2], node4[3]}};
+    return qt_hull_check(s, &nd, P, max_edge);
+}
+
+int orc_qt_split_type(const orc_surface* s, const double* M, const double node4[4], double max_edge, int as_reference) {
+    qt_node nd = {{node4[0], node4[1]}, {node4[2], node4[3]}};
+    return qt_split_type_x(s, M, &nd, max_edge, as_reference);
 }
 
 /* children of nd by split type t, appended to out (the reference's order) */

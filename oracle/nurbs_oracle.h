@@ -171,6 +171,13 @@ void orc_project_perturbed(const orc_surface* s, const double* matrix_n, const o
 void orc_invert_quadtree(const orc_surface* s, const double* matrix_n, const double* P, int64_t n, double max_edge,
                          int max_iter, double* uv, int* status, double* residual, int* layers, int threads);
 
+/* One node (lb.u, lb.v, rt.u, rt.v) of the quadtree inversion: its control-point box check and
+ * its split type (as_reference = 1: the reference's v-length from MatrixSurfaceDerivativeU, for
+ * pinning the definition against the reference's own getSplitType). */
+int orc_qt_hull_check(const orc_surface* s, const double node4[4], const double P[3], double max_edge);
+int orc_qt_split_type(const orc_surface* s, const double* matrix_n, const double node4[4], double max_edge,
+                      int as_reference);
+
 /* The reference's GaussNewton exactly as shipped (kernel.cu:151-249): <= 10 steps,
  * success when |S-P| < max_edge before a step.  Returns 1 on success and writes uv. */
 int orc_gauss_newton_shipped(const orc_surface* s, const double* matrix_n, const double seed[2],

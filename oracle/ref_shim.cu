@@ -226,4 +226,89 @@ int ref_find_span(int degree, int cp, const double* knots, double u) {
   return findSpan(degree, cp, const_cast<double*>(knots), u);
 }
 
+// The projection path's derivatives at (uu, vv): GetVector's power vectors (kernel.cu:1386-1450,
+// restated for one point), MatrixSurfaceRd* (Evaluate.cu:288-502), the new-style quotient forms
+// (:932-1020) and SurfaceNormalDerivative{UU,UV,VV} (:1125-1135).  out[42]: S, Su, Sv, Suu, Suv,
+// Svv, Suuu, Suuv, Suvv, Svvv, N = Su x Sv, Nuu, Nuv, Nvv (xyz each).
+void ref_ders3(int p, int q, int nu, int nv, const double* ku_c, const double* kv_c, const double* MN_c, double uu,
+               double vv, double* out) {
+  double* knots_u = const_cast<double*>(ku_c);
+  double* knots_v = const_cast<double*>(kv_c);
+  double* MatrixN = const_cast<double*>(MN_c);
+  int m = findSpan(p, nu, knots_u, uu);
+  int n = findSpan(q, nv, knots_v, vv);
+  double u = (uu - knots_u[m]) / (knots_u[m + 1] - knots_u[m]);
+  double v = (vv - knots_v[n]) / (knots_v[n + 1] - knots_v[n]);
+  double spanU = (knots_u[p + nu] - knots_u[0]) / (knots_u[m + 1] - knots_u[m]);
+  double spanV = (knots_v[q + nv] - knots_v[0]) / (knots_v[n + 1] - knots_v[n]);
+  double* middle = MatrixN + MatrixNPosition(m, n, p, q, nu, nv, 0);
+  const int k1 = p + 1, k2 = q + 1;
+  double U[4][MAX_DEGREE], V[4][MAX_DEGREE];
+  for (int d = 0; d < 2; ++d) {
+    double* W = d == 0 ? U[0] : V[0];
+    double* W1 = d == 0 ? U[1] : V[1];
+    double* W2 = d == 0 ? U[2] : V[2];
+    double* W3 = d == 0 ? U[3] : V[3];
+    const int k = d == 0 ? k1 : k2;
+    const double t = d == 0 ? u : v;
+    double now = 1;
+    for (int i = 0; i < k; i++) { W[i] = now; now *= t; }
+    W1[0] = 0;
+    for (int i = 0; i < k - 1; i++) W1[i + 1] = (i + 1) * W[i];
+    W2[0] = W2[1] = 0;
+    for (int i = 0; i < k - 2; i++) W2[i + 2] = (i + 2) * (i + 1) * W[i];
+    W3[0] = W3[1] = W3[2] = 0;
+    for (int i = 0; i < k - 3; i++) W3[i + 3] = (i + 3) * (i + 2) * (i + 1) * W[i];
+  }
+  double4 R = MatrixSurfacePoint(middle, p, q, nu, nv, knots_u, knots_v, u, v);
+  double4 RdU = MatrixSurfaceRdU(middle, p, q, nu, nv, knots_u, knots_v, u, v, U[1], V[0], spanU);
+  double4 RdV = MatrixSurfaceRdV(middle, p, q, nu, nv, knots_u, knots_v, u, v, U[0], V[1], spanV);
+  double4 RdUU = MatrixSurfaceRdUU(middle, p, q, nu, nv, knots_u, knots_v, u, v, U[2], V[0], spanU);
+  double4 RdUV = MatrixSurfaceRdUV(middle, p, q, nu, nv, knots_u, knots_v, u, v, U[1], V[1], spanU, spanV);
+  double4 RdVV = MatrixSurfaceRdVV(middle, p, q, nu, nv, knots_u, knots_v, u, v, U[0], V[2], spanV);
+  double4 RdUUU = MatrixSurfaceRdUUU(middle, p, q, nu, nv, knots_u, knots_v, u, v, U[3], V[0], spanU);
+  double4 RdUUV = MatrixSurfaceRdUUV(middle, p, q, nu, nv, knots_u, knots_v, u, v, U[2], V[1], spanU, spanV);
+  double4 RdUVV = MatrixSurfaceRdUVV(middle, p, q, nu, nv, knots_u, knots_v, u, v, U[1], V[2], spanU, spanV);
+  double4 RdVVV = MatrixSurfaceRdVVV(middle, p, q, nu, nv, knots_u, knots_v, u, v, U[0], V[3], spanV);
+  const double h = R.w;
+  double3 P = homogenousToCartesian(R);
+  double3 PdU = MatrixSurfaceDerivativeU(RdU, P, h);
+  double3 PdV = MatrixSurfaceDerivativeV(RdV, P, h);
+  double3 PdUU = MatrixSurfaceDerivativeUU(RdUU, PdU, P, h, RdU.w);
+  double3 PdUV = MatrixSurfaceDerivativeUV(RdUV, PdU, PdV, P, h, RdU.w, RdV.w);
+  double3 PdVV = MatrixSurfaceDerivativeVV(RdVV, PdV, P, h, RdV.w);
+  double3 PdUUU = MatrixSurfaceDerivativeUUU(RdUUU, PdUU, PdU, P, h, RdU.w, RdUU.w);
+  double3 PdUUV = MatrixSurfaceDerivativeUUV(RdUUV, PdUU, PdUV, PdU, PdV, P, h, RdU.w, RdV.w, RdUU.w, RdUV.w);
+  double3 PdUVV = MatrixSurfaceDerivativeUVV(RdUVV, PdUV, PdVV, PdU, PdV, P, h, RdU.w, RdV.w, RdUV.w, RdVV.w);
+  double3 PdVVV = MatrixSurfaceDerivativeVVV(RdVVV, PdVV, PdV, P, h, RdV.w, RdVV.w);
+  const double3 blk[14] = {P, PdU, PdV, PdUU, PdUV, PdVV, PdUUU, PdUUV, PdUVV, PdVVV, cross_product(PdU, PdV),
+                           SurfaceNormalDerivativeUU(PdU, PdV, PdUU, PdUV, PdUUU, PdUUV),
+                           SurfaceNormalDerivativeUV(PdU, PdV, PdUU, PdUV, PdVV, PdUUV, PdUVV),
+                           SurfaceNormalDerivativeVV(PdU, PdV, PdUV, PdVV, PdUVV, PdVVV)};
+  for (int b = 0; b < 14; ++b) {
+    out[3 * b] = blk[b].x;
+    out[3 * b + 1] = blk[b].y;
+    out[3 * b + 2] = blk[b].z;
+  }
+}
+
+// BoundingBoxCheck (kernel.cu:106-149) and getSplitType (:251-298) of the first inversion for one
+// node given as 4 doubles (lb.u, lb.v, rt.u, rt.v).
+int ref_qt_box_check(int p, int q, int nu, int nv, const double* ku_c, const double* kv_c, const double* cps,
+                     const double* node4, const double* P, double max_edge) {
+  double3* control_points = make_cps(cps, nu * nv);
+  Node nd = {{node4[0], node4[1]}, {node4[2], node4[3]}};
+  bool r = BoundingBoxCheck(nd, double3{P[0], P[1], P[2]}, max_edge, p, q, nu, nv, const_cast<double*>(ku_c),
+                            const_cast<double*>(kv_c), control_points);
+  delete[] control_points;
+  return r ? 1 : 0;
+}
+
+int ref_qt_split_type(int p, int q, int nu, int nv, const double* ku_c, const double* kv_c, const double* MN_c,
+                      const double* node4, double max_edge) {
+  Node nd = {{node4[0], node4[1]}, {node4[2], node4[3]}};
+  return (int)getSplitType(nd, max_edge, const_cast<double*>(MN_c), p, q, nu, nv, const_cast<double*>(ku_c),
+                           const_cast<double*>(kv_c), nullptr, nullptr);
+}
+
 }  // extern "C"

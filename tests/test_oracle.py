@@ -4,6 +4,7 @@ The fixtures (tests/golden/*.npz) were produced by the reference's FP64 function
 the host (oracle/_ref, see tests/golden/make_golden.py).  These tests pin the oracle: span
 matrices, evaluation, tree and candidate lists must agree bit for bit.
 """
+import glob
 import math
 import os
 from fractions import Fraction
@@ -388,3 +389,47 @@ def test_oracle_quadtree_inversion():
         assert np.mean(st <= O.FOUND_AMBIGUOUS) >= 0.99 and np.all(res[st <= 1] < 1e-3)
         far = o.cps.max(0) + 1.0 + rng.random((50, 3))
         assert np.all(o.invert_quadtree(far, 1e-3)[1] == O.NO_CANDIDATE)
+
+
+PIN_FILES = sorted(glob.glob(os.path.join(GOLDEN, "pin3_*.npz")))
+
+
+def _pin_surface(path):
+    g = load_golden(os.path.join(GOLDEN, os.path.basename(path)[len("pin3_"):]))
+    return surf_of(g), np.load(path)
+
+
+@pytest.mark.parametrize("path", PIN_FILES, ids=lambda p: os.path.basename(p)[5:-4])
+def test_oracle_third_order_pinned_to_reference(path):
+    """The oracle's third-order and normal derivatives against the reference's own
+    MatrixSurfaceRd* / new-style quotient forms / SurfaceNormalDerivative* (fixtures made by the
+    reference compiled for the host): bit-identical for S, Su, Sv, Suu, Svv, Suuu, Svvv and N
+    everywhere, and the mixed ones equal to rounding noise where the weights are constant; where
+    they are not,
+    the reference's S_uv, S_uuv, S_uvv carry its sign defect (the oracle's follow the quotient
+    rule, checked against central differences elsewhere)."""
+    surf, z = _pin_surface(path)
+    o = O.OracleSurface(surf)
+    mine = np.stack([np.concatenate([d, n[[0, 3, 4, 5]]]) for d, n in (o.ders3(u, v) for u, v in z["uv"])])
+    ref = z["ders3"]
+    exact_blocks = [0, 1, 2, 3, 5, 6, 9, 10]
+    assert np.array_equal(mine[:, exact_blocks].view(np.int64), ref[:, exact_blocks].view(np.int64))
+    if np.ptp(surf["weights"]) == 0:
+        # constant weights: h's derivatives are rounding noise (~1e-17), so the defect's terms
+        # change the mixed derivatives by ~1e-29 at most
+        assert np.abs(mine - ref).max() <= 1e-20 * max(1.0, np.abs(ref).max())
+
+
+@pytest.mark.parametrize("path", PIN_FILES, ids=lambda p: os.path.basename(p)[5:-4])
+def test_oracle_quadtree_pinned_to_reference(path):
+    """The quadtree inversion's node tests against the reference's BoundingBoxCheck and
+    getSplitType: box checks equal for every node and point; split types equal with the
+    reference's v-length (MatrixSurfaceDerivativeU) reproduced; the oracle's own definition
+    (the v-derivative) differs from it only where that length decides."""
+    surf, z = _pin_surface(path)
+    o = O.OracleSurface(surf)
+    for e, me in enumerate(z["max_edge"]):
+        for i, nd in enumerate(z["nodes"]):
+            assert o.qt_split_type(nd, me, as_reference=True) == z["split"][e, i]
+            for j, x in enumerate(z["P"]):
+                assert o.qt_hull_check(nd, x, me) == z["box"][e, i, j]
