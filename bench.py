@@ -635,9 +635,10 @@ def project_record(a, compact=False):
 
 
 def quadtree_record(a, compact=False):
-    """Adaptive quadtree inversion (nurbs_invert_quadtree, FP64; the reference's first inversion
-    with max_edge 1e-4 as its driver calls it) of 2^20 points on the 64x64 bicubic surface; no
-    tree build.  Inversions/s, parity with the oracle on a bounded sample and its CPU time."""
+    """Adaptive quadtree inversion (nurbs_invert_quadtree, mixed and FP64; the reference's first
+    inversion with max_edge 1e-4 as its driver calls it) of 2^20 points on the 64x64 bicubic
+    surface; no tree build.  Inversions/s, parity of the mixed results with the oracle on a
+    bounded sample and its CPU time."""
     import torch
     gn = load_pkg()
     from gpu_nurbs_gb300 import synth
@@ -653,16 +654,21 @@ def quadtree_record(a, compact=False):
            torch.empty(n, dtype=torch.float64, device="cuda"))
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     timed = event_timer(torch, flush)
-    run = lambda: s.invert_quadtree(Pd, max_edge, out=out)
+    run = lambda: s.invert_quadtree(Pd, max_edge, gn.PREC_MIXED, out=out)
+    run64 = lambda: s.invert_quadtree(Pd, max_edge, gn.PREC_FP64, out=out)
     for _ in range(3):
         run()
+    run64()
     torch.cuda.synchronize()
     clocks = Clocks(0)
     t = timed(run, steps)
+    t64 = timed(run64, max(2, steps // 2))
     clk = clocks.stop()
+    run()
     g_uv, g_st, g_res = (x.cpu().numpy() for x in out)
-    ms = sum(t) / len(t)
-    rec = {"value": n / (ms / 1e3), "unit": "inversions/s", "ms_per_step": ms, "steps": steps, "dtype": "f64",
+    ms, ms64 = sum(t) / len(t), sum(t64) / len(t64)
+    rec = {"value": n / (ms / 1e3), "unit": "inversions/s", "ms_per_step": ms, "steps": steps, "dtype": "f32+f64",
+           "fp64_value": n / (ms64 / 1e3), "fp64_ms_per_step": ms64, "mixed_vs_fp64": ms64 / ms,
            "config": {"workload": f"quadtree-64x64-bicubic-{n} on-surface points, max_edge 1e-4",
                       "l2": "flushed (512 MB write) before each step"},
            "found_frac": float(np.mean(g_st <= 1)), "max_uv_err": float(np.abs(g_uv - uv0)[g_st <= 1].max()),

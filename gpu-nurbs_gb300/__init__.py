@@ -93,7 +93,7 @@ SIGNATURES = {
     "nurbs_invert_count": (C.c_int, [_vp, _vp, _i64, C.c_int, _vp, _vp]),
     "nurbs_pcurve": (C.c_int, [_vp, _vp, _i64, _vp, _vp, _vp, _vp, C.c_int, _vp]),
     "nurbs_project": (C.c_int, [_vp, _vp, _i64, _vp, _vp, _vp, C.c_int, _vp]),
-    "nurbs_invert_quadtree": (C.c_int, [_vp, _vp, _i64, C.c_double, _vp, _vp, _vp, _vp]),
+    "nurbs_invert_quadtree": (C.c_int, [_vp, _vp, _i64, C.c_double, _vp, _vp, _vp, C.c_int, _vp]),
     "nurbs_normal_cones_export": (C.c_int, [_vp, _vp, _vp, _vp]),
     "nurbs_eval_normal": (C.c_int, [_vp, _vp, _i64, C.c_uint, _vp, _vp]),
     "nurbs_probe_fp_peak": (C.c_int, [C.c_int, C.POINTER(C.c_double), _vp]),
@@ -332,9 +332,9 @@ class Surface:
               "nurbs_project")
         return uv, st, res
 
-    def invert_quadtree(self, P, max_edge: float, stream=None, out=None):
-        """Adaptive quadtree inversion (nurbs_invert_quadtree, FP64): P (n,3) float64 CUDA tensor
-        -> (uv (n,2), status (n,), residual (n,))."""
+    def invert_quadtree(self, P, max_edge: float, precision: int = PREC_FP64, stream=None, out=None):
+        """Adaptive quadtree inversion (nurbs_invert_quadtree): P (n,3) float64 CUDA tensor ->
+        (uv (n,2), status (n,), residual (n,))."""
         torch = _torch()
         P = P.contiguous()
         n = P.shape[0]
@@ -345,7 +345,7 @@ class Surface:
         else:
             uv, st, res = out
         check(lib().nurbs_invert_quadtree(self.h, _ptr(P), n, float(max_edge), _ptr(uv), _ptr(st), _ptr(res),
-                                          _stream(stream)), "nurbs_invert_quadtree")
+                                          precision, _stream(stream)), "nurbs_invert_quadtree")
         return uv, st, res
 
     def normal_cones(self):

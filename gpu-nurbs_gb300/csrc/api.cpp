@@ -104,7 +104,7 @@ struct nurbs_surface_s {
 // counter, launches, marks the slot.  Inside a stream capture the slot is used without the
 // event handshake (capture cannot wait on work recorded outside it).
 // precision: NURBS_PREC_FP64 / MIXED for the inversion, -1 / -3 for the projection (FP64 / mixed),
-// -2 for the adaptive quadtree inversion (FP64, max_edge)
+// -2 / -4 for the adaptive quadtree inversion (FP64 / mixed, max_edge)
 static cudaError_t invert_on(nurbs_surface_s* s, const double* P, int64_t n, double* uv, int* status, double* res,
                              int precision, cudaStream_t st, double max_edge = 0) {
   std::lock_guard<std::mutex> lk(s->mu);
@@ -124,8 +124,9 @@ static cudaError_t invert_on(nurbs_surface_s* s, const double* P, int64_t n, dou
   }
   e = cudaMemsetAsync(s->counters + slot, 0, sizeof(unsigned), st);
   if (e == cudaSuccess) {
-    if (precision == -2)
-      e = launch_invert_quadtree(s->dev, P, n, max_edge, uv, status, res, s->counters + slot, st);
+    if (precision == -2 || precision == -4)
+      e = launch_invert_quadtree(s->dev, P, n, max_edge, uv, status, res,
+                                 precision == -4 ? NURBS_PREC_MIXED : NURBS_PREC_FP64, s->counters + slot, st);
     else if (precision == -1 || precision == -3)
       e = launch_project(s->dev, P, n, uv, status, res, precision == -3 ? NURBS_PREC_MIXED : NURBS_PREC_FP64,
                          s->counters + slot, st);
@@ -404,14 +405,17 @@ int nurbs_project(nurbs_surface_t s, const double* P_dev, int64_t n, double* uv_
 }
 
 int nurbs_invert_quadtree(nurbs_surface_t s, const double* P_dev, int64_t n, double max_edge, double* uv_dev,
-                          int* status_dev, double* residual_dev, void* stream) {
+                          int* status_dev, double* residual_dev, int precision, void* stream) {
   if (!s) return fail(NURBS_E_INVALID, "NULL surface");
   if (n < 0) return fail(NURBS_E_INVALID, "negative count");
+  if (precision != NURBS_PREC_FP64 && precision != NURBS_PREC_MIXED)
+    return fail(NURBS_E_INVALID, "precision %d is not FP64 or MIXED", precision);
   if (!(max_edge > 0) || !std::isfinite(max_edge)) return fail(NURBS_E_INVALID, "max_edge must be positive");
   if (n > 0xffffffffLL) return fail(NURBS_E_INVALID, "more than 2^32 - 1 queries");
   if (n == 0) return NURBS_OK;
   if (!P_dev || !uv_dev || !status_dev || !residual_dev) return fail(NURBS_E_INVALID, "NULL buffer");
-  CUDA_TRY(invert_on(s, P_dev, n, uv_dev, status_dev, residual_dev, -2, (cudaStream_t)stream, max_edge),
+  CUDA_TRY(invert_on(s, P_dev, n, uv_dev, status_dev, residual_dev, precision == NURBS_PREC_MIXED ? -4 : -2,
+                     (cudaStream_t)stream, max_edge),
            "quadtree inversion launch");
   return NURBS_OK;
 }

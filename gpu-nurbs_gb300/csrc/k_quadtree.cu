@@ -5,7 +5,9 @@
 //
 // A persistent grid whose warps take chunks of 32 queries from a counter.  The first layer (the
 // root: its precomputed box and one trajectory from the domain's centre) runs lane per query and
-// answers most queries; a query it leaves open is then searched by the whole warp:
+// answers most queries; with MODE mixed that trajectory runs in FP32 and its end takes FP64
+// Newton steps (the mixed inversion's final steps).  A query it leaves open is then searched by
+// the whole warp, in FP64:
 //   * a layer's nodes live in shared memory; each node's control-point box is reduced by the
 //     whole warp (lanes stride over the node's control-point rows and columns, min/max by
 //     shuffles: exact, so the pass/fail decisions equal the oracle's);
@@ -295,7 +297,7 @@ __device__ void quadtree_query(const SurfDev& s, const Ctx& cx, QtWarp& w, const
   __syncwarp();
 }
 
-template <int P, int Q>
+template <int P, int Q, int MODE>
 __global__ void __launch_bounds__(kThreads)
     k_invert_quadtree(SurfDev s, const double* __restrict__ qtbox, const double* __restrict__ Pq, int64_t n,
                       double max_edge, double* __restrict__ uv_out, int* __restrict__ st_out,
@@ -332,21 +334,52 @@ __global__ void __launch_bounds__(kThreads)
       int status = 2;  // the root alone does not pass: no node ever passes
       double ou = __longlong_as_double(0x7ff8000000000000ll), ov = ou, orr = ou;
       if (pass) {
-        Seed<double> sd;
-        sd.u = (s.dom_u0 + s.dom_u1) / 2;
-        sd.v = (s.dom_v0 + s.dom_v1) / 2;
-        sd.prev = INFINITY;
-        sd.it = 0;
-        sd.hu = 0;
-        sd.hv = 0;
-        sd.newton = false;
-        int r = kContinue;
-        while (r == kContinue) r = iterate64<P, Q>(cx, px, py, pz, sd);
-        double rr;
-        if (r == kConverged && finish64<P, Q>(cx, px, py, pz, sd.u, sd.v, sd.hu, sd.hv, rr) && rr < max_edge) {
+        bool ok = false;
+        double u = (s.dom_u0 + s.dom_u1) / 2, v = (s.dom_v0 + s.dom_v1) / 2, rr = 0;
+        if constexpr (MODE == kModeMixed) {
+          // the root's trajectory in FP32 (the mixed inversion's iteration, the point relative to
+          // the control net's centre), then its FP64 Newton steps and residual
+          Seed<float> sd;
+          sd.u = (float)u;
+          sd.v = (float)v;
+          sd.prev = INFINITY;
+          sd.it = 0;
+          sd.hu = 0;
+          sd.hv = 0;
+          sd.newton = false;
+          const float tx = (float)(px - s.org[0]), ty = (float)(py - s.org[1]), tz = (float)(pz - s.org[2]);
+          const float eu = 2.0f * (float)(s.dom_u1 - s.dom_u0), ev = 2.0f * (float)(s.dom_v1 - s.dom_v0);
+          const float far[4] = {(float)s.dom_u0 - eu, (float)s.dom_u1 + eu, (float)s.dom_v0 - ev, (float)s.dom_v1 + ev};
+          float dist;
+          int r = kContinue;
+          while (r == kContinue) {
+            r = iterate32<P, Q>(cx, tx, ty, tz, sd, dist);
+            if (r == kContinue && !(sd.u >= far[0] && sd.u <= far[1] && sd.v >= far[2] && sd.v <= far[3])) r = kFailed;
+          }
+          if (r == kConverged) {
+            u = sd.u;
+            v = sd.v;
+            ok = final64<P, Q>(cx, px, py, pz, u, v, rr) && rr < max_edge;
+          }
+        } else {
+          Seed<double> sd;
+          sd.u = u;
+          sd.v = v;
+          sd.prev = INFINITY;
+          sd.it = 0;
+          sd.hu = 0;
+          sd.hv = 0;
+          sd.newton = false;
+          int r = kContinue;
+          while (r == kContinue) r = iterate64<P, Q>(cx, px, py, pz, sd);
+          u = sd.u;
+          v = sd.v;
+          ok = r == kConverged && finish64<P, Q>(cx, px, py, pz, u, v, sd.hu, sd.hv, rr) && rr < max_edge;
+        }
+        if (ok) {
           status = 0;
-          ou = sd.u;
-          ov = sd.v;
+          ou = u;
+          ov = v;
           orr = rr;
         } else {
           rest = true;
@@ -368,9 +401,9 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
-template <int P, int Q>
-cudaError_t launch_quadtree_pq(const SurfDev& s, const double* P_, int64_t n, double max_edge, double* uv, int* st_,
-                               double* res, unsigned* counter, cudaStream_t st) {
+template <int P, int Q, int MODE>
+cudaError_t launch_quadtree_mode(const SurfDev& s, const double* P_, int64_t n, double max_edge, double* uv, int* st_,
+                                 double* res, unsigned* counter, cudaStream_t st) {
   if ((n + 31) / 32 > 0xffffffffLL) return cudaErrorInvalidValue;  // chunk ids are 32-bit
   static int cached[64] = {0};
   int dev = 0;
@@ -379,23 +412,33 @@ cudaError_t launch_quadtree_pq(const SurfDev& s, const double* P_, int64_t n, do
   if (!cached[dev]) {
     int sms = 0, per_sm = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_invert_quadtree<P, Q>, kThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_invert_quadtree<P, Q, MODE>, kThreads, 0);
     cached[dev] = (sms > 0 ? sms : 1) * (per_sm > 0 ? per_sm : 1);
   }
   int64_t blocks = ((n + 31) / 32 + kWarps - 1) / kWarps;
   if (blocks > cached[dev]) blocks = cached[dev];
   k_quadtree_boxes<<<kQtBoxes, 256, 0, st>>>(s, s.qtbox);
-  k_invert_quadtree<P, Q><<<(unsigned)blocks, kThreads, 0, st>>>(s, s.qtbox, P_, n, max_edge, uv, st_, res, counter);
+  k_invert_quadtree<P, Q, MODE><<<(unsigned)blocks, kThreads, 0, st>>>(s, s.qtbox, P_, n, max_edge, uv, st_, res,
+                                                                       counter);
   return cudaGetLastError();
+}
+
+template <int P, int Q>
+cudaError_t launch_quadtree_pq(const SurfDev& s, const double* P_, int64_t n, double max_edge, double* uv, int* st_,
+                               double* res, int precision, unsigned* counter, cudaStream_t st) {
+  if (precision == kModeMixed)
+    return launch_quadtree_mode<P, Q, kModeMixed>(s, P_, n, max_edge, uv, st_, res, counter, st);
+  return launch_quadtree_mode<P, Q, kModeFP64>(s, P_, n, max_edge, uv, st_, res, counter, st);
 }
 
 }  // namespace
 
 cudaError_t launch_invert_quadtree(const SurfDev& s, const double* P, int64_t n, double max_edge, double* uv,
-                                   int* status, double* residual, unsigned* counter, cudaStream_t st) {
+                                   int* status, double* residual, int precision, unsigned* counter, cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
-  if (s.p == 3 && s.q == 3) return launch_quadtree_pq<3, 3>(s, P, n, max_edge, uv, status, residual, counter, st);
-  return launch_quadtree_pq<0, 0>(s, P, n, max_edge, uv, status, residual, counter, st);
+  if (s.p == 3 && s.q == 3)
+    return launch_quadtree_pq<3, 3>(s, P, n, max_edge, uv, status, residual, precision, counter, st);
+  return launch_quadtree_pq<0, 0>(s, P, n, max_edge, uv, status, residual, precision, counter, st);
 }
 
 }  // namespace gnurbs

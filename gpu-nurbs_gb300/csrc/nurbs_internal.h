@@ -156,7 +156,7 @@ cudaError_t launch_project(const SurfDev& s, const double* P, int64_t n, double*
                            double* residual, int precision, unsigned* counter, cudaStream_t st);
 // adaptive quadtree inversion (k_quadtree.cu)
 cudaError_t launch_invert_quadtree(const SurfDev& s, const double* P, int64_t n, double max_edge, double* uv,
-                                   int* status, double* residual, unsigned* counter, cudaStream_t st);
+                                   int* status, double* residual, int precision, unsigned* counter, cudaStream_t st);
 // S, Su, Sv at the built nodes' uv-centres (cd32/cd64), after the tree is built
 cudaError_t launch_centre_ders(const SurfDev& s, cudaStream_t st);
 cudaError_t launch_centre_ders_batched(const SurfDev* table, const int* ids, int count, cudaStream_t st);

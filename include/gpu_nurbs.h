@@ -225,9 +225,11 @@ int nurbs_project(nurbs_surface_t s, const double* P_dev, int64_t n, double* uv_
  * P; the first layer with such a result answers with its closest one.  Nodes that pass are split
  * by getSplitType (the v-length from the v-derivative); a layer of more than 64 nodes
  * (NODE_MAX_SIZE) ends the query unanswered.  For points on the surface or within max_edge of
- * it.  Outputs as nurbs_invert; n < 2^32. */
+ * it.  precision: NURBS_PREC_FP64, or NURBS_PREC_MIXED (the root's trajectory, which answers most
+ * queries, in FP32 with FP64 final Newton steps and residual; the deeper layers in FP64).
+ * Outputs as nurbs_invert; n < 2^32 * 32. */
 int nurbs_invert_quadtree(nurbs_surface_t s, const double* P_dev, int64_t n, double max_edge, double* uv_dev,
-                          int* status_dev, double* residual_dev, void* stream);
+                          int* status_dev, double* residual_dev, int precision, void* stream);
 /* Copies the projection's culling data to host memory: nbox[65*6] normal boxes (lb xyz, rt xyz),
  * cone[65*20] FP32 records relative to the control net's centre (bound-box ball centre and radius,
  * cone axis, cos and sin of its half-angle (0 and 1: every direction), bound box rounded outward,

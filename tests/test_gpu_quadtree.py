@@ -21,11 +21,14 @@ def cases():
             "rational": synth.surface_random(synth.Rng(77)), "quintic": synth.surface_quintic(n=32)}
 
 
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "mixed"])
 @pytest.mark.parametrize("which", ["small", "large", "tube", "rational", "quintic"])
 @pytest.mark.parametrize("max_edge", [1e-2, 1e-4])
-def test_quadtree_matches_the_oracle(nurbs, which, max_edge):
+def test_quadtree_matches_the_oracle(nurbs, which, max_edge, precision):
     """Points on the surface, within max_edge of it, and far from it: the same status, the same
-    answer to 1e-9, the same residual to rounding."""
+    answer to 1e-9, the same residual to rounding (mixed: the root's FP32 trajectory may end in
+    another basin than the FP64 one for at most 1e-4 of the queries, the mixed inversion's
+    bound)."""
     sf = cases()[which]
     s, o = nurbs.Surface(sf), O.OracleSurface(sf)
     rng = np.random.default_rng(7)
@@ -36,10 +39,12 @@ def test_quadtree_matches_the_oracle(nurbs, which, max_edge):
     near = E[0:3].T + N * ((rng.random(4096) - 0.5) * max_edge)[:, None]
     far = o.cps.mean(0) + (rng.random((256, 3)) - 0.5) * 6 * np.ptp(o.cps, 0).max()
     P = np.concatenate([E[0:3].T, near, far])
-    uv, st, res = (x.cpu().numpy() for x in s.invert_quadtree(T(P), max_edge))
+    uv, st, res = (x.cpu().numpy() for x in s.invert_quadtree(T(P), max_edge, precision))
     ouv, ost, ores, _ = o.invert_quadtree(P, max_edge)
-    assert np.array_equal(st, ost)
-    f = st <= 1
+    same = (st == ost) & ((st > 1) | (np.abs(uv - ouv).max(1) <= 1e-9))
+    allowed = int(np.ceil(1e-4 * len(P))) if precision == 1 else 0
+    assert np.count_nonzero(~same) <= allowed, np.nonzero(~same)[0][:10]
+    f = (st <= 1) & same
     assert np.abs(uv[f] - ouv[f]).max() <= 1e-9
     assert np.all(np.abs(res[f] - ores[f]) <= 1e-12 * ores[f] + 1e-14)
     assert np.mean(st[:4096] <= 1) == 1.0
@@ -53,4 +58,6 @@ def test_quadtree_arguments(nurbs):
         s.invert_quadtree(P, 0.0)
     with pytest.raises(nurbs.NurbsError):
         s.invert_quadtree(P, float("nan"))
+    with pytest.raises(nurbs.NurbsError):
+        s.invert_quadtree(P, 1e-3, 5)
     s.invert_quadtree(P[:0], 1e-3)
