@@ -26,9 +26,10 @@ def cases():
 @pytest.mark.parametrize("max_edge", [1e-2, 1e-4])
 def test_quadtree_matches_the_oracle(nurbs, which, max_edge, precision):
     """Points on the surface, within max_edge of it, and far from it: the same status, the same
-    answer to 1e-9, the same residual to rounding (mixed: the root's FP32 trajectory may end in
-    another basin than the FP64 one for at most 1e-4 of the queries, the mixed inversion's
-    bound)."""
+    answer to 1e-9, the same residual to rounding.  Mixed: the root's FP32 trajectory can end in
+    another basin than the FP64 one (large GN steps over a wavy surface); its answer is then
+    another point within max_edge, which the reference's success test accepts as well: found /
+    not found differs for at most 1e-4 of the queries, the answer for at most 1e-3."""
     sf = cases()[which]
     s, o = nurbs.Surface(sf), O.OracleSurface(sf)
     rng = np.random.default_rng(7)
@@ -42,8 +43,12 @@ def test_quadtree_matches_the_oracle(nurbs, which, max_edge, precision):
     uv, st, res = (x.cpu().numpy() for x in s.invert_quadtree(T(P), max_edge, precision))
     ouv, ost, ores, _ = o.invert_quadtree(P, max_edge)
     same = (st == ost) & ((st > 1) | (np.abs(uv - ouv).max(1) <= 1e-9))
-    allowed = int(np.ceil(1e-4 * len(P))) if precision == 1 else 0
-    assert np.count_nonzero(~same) <= allowed, np.nonzero(~same)[0][:10]
+    if precision == 0:
+        assert np.all(same), np.nonzero(~same)[0][:10]
+    else:
+        assert np.count_nonzero((st <= 1) != (ost <= 1)) <= int(np.ceil(1e-4 * len(P)))
+        assert np.count_nonzero(~same) <= int(np.ceil(1e-3 * len(P))), np.nonzero(~same)[0][:10]
+        assert np.all(res[(st <= 1) & ~same] < max_edge)
     f = (st <= 1) & same
     assert np.abs(uv[f] - ouv[f]).max() <= 1e-9
     assert np.all(np.abs(res[f] - ores[f]) <= 1e-12 * ores[f] + 1e-14)
