@@ -66,3 +66,37 @@ def test_quadtree_arguments(nurbs):
     with pytest.raises(nurbs.NurbsError):
         s.invert_quadtree(P, 1e-3, 5)
     s.invert_quadtree(P[:0], 1e-3)
+
+
+def test_quadtree_and_projection_on_concurrent_streams(nurbs):
+    """The same surface on two streams at once (each launch rewrites the surface's top-level box
+    table with the same values; each call takes its own launch counter): the results equal those
+    of the calls one after the other."""
+    from gpu_nurbs_gb300 import synth
+    sf = synth.surface_large()
+    s, o = nurbs.Surface(sf), O.OracleSurface(sf)
+    uv0 = np.random.default_rng(12).random((50000, 2))
+    P = T(o.eval(uv0, 1).T)
+    ref_q = [x.cpu().numpy() for x in s.invert_quadtree(P, 1e-4, 1)]
+    ref_p = [x.cpu().numpy() for x in s.project(P, 1)]
+    torch.cuda.synchronize()
+    s1, s2 = torch.cuda.Stream(), torch.cuda.Stream()
+    outs = []
+    for _ in range(3):
+        s1.wait_stream(torch.cuda.current_stream())
+        s2.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(s1):
+            a = s.invert_quadtree(P, 1e-4, 1)
+        with torch.cuda.stream(s2):
+            b = s.project(P, 1)
+            c = s.invert_quadtree(P, 1e-4, 0)
+        outs.append((a, b, c))
+    torch.cuda.synchronize()
+    ref_q64 = [x.cpu().numpy() for x in s.invert_quadtree(P, 1e-4, 0)]
+    for a, b, c in outs:
+        for x, y in zip(a, ref_q):
+            assert np.array_equal(x.cpu().numpy(), y, equal_nan=True)
+        for x, y in zip(b, ref_p):
+            assert np.array_equal(x.cpu().numpy(), y, equal_nan=True)
+        for x, y in zip(c, ref_q64):
+            assert np.array_equal(x.cpu().numpy(), y, equal_nan=True)
