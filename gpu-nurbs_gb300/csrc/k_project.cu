@@ -22,7 +22,8 @@
 // the control net's centre; steps below kWholeStep32 skip the line search, whose distance
 // comparisons are rounding noise there), each query's best result and best of another grid cell
 // kept, then FP64 projected Newton steps from the best, and from the other when it is within
-// kPolishMargin of it or the best fails.
+// kPolishMargin of it or the best fails (project_polish64, the FP64 schedule's iteration where
+// those steps do not converge).
 #include "invert_core.cuh"
 
 namespace gnurbs {
@@ -183,6 +184,60 @@ __device__ __forceinline__ int project_iterate(const Ctx& c, double px, double p
   if (moved <= kTolAny64 || (newton && moved <= kTolNewtonProj)) return kConverged;
   if (++sd.it >= kMaxIterProj) return kFailed;
   return kContinue;
+}
+
+// MIXED: the final FP64 steps from an FP32 result, as the inversion's (final64): S, Su, Sv in FP64
+// and the Hessian's curvature term from FP32 second derivatives, projected onto the domain as the
+// trajectories are, without a line search (the FP32 result lies in its minimum's basin); at most
+// kPolishSteps, converged at a move <= kTolNewtonProj, the residual from the last step's S, Su, Sv.
+// False when it does not converge: the caller then runs the FP64 schedule's iteration.
+constexpr int kPolishSteps = 8;
+template <int P, int Q>
+__device__ bool project_polish64(const Ctx& c, double px, double py, double pz, double& u, double& v, double& res) {
+  int hu = fast::find_seg_hint(c.L32.bu, c.L32.ns_u, (float)u, 0);
+  int hv = fast::find_seg_hint(c.L32.bv, c.L32.ns_v, (float)v, 0);
+  int hu32 = hu, hv32 = hv;
+  for (int it = 0; it < kPolishSteps; ++it) {
+    const fast::SDer<double> d = fast::eval_at<double, P, Q, 1>(c.L64, c.m64, c.p, c.q, u, v, hu, hv);
+    const fast::SDer<float> e = fast::eval_at<float, P, Q, 2, true>(c.L32, c.m32, c.p, c.q, (float)u, (float)v, hu32,
+                                                                  hv32);
+    const v3<double> r = {d.S.x - px, d.S.y - py, d.S.z - pz};
+    const double g0 = dot3(d.Su, r), g1 = dot3(d.Sv, r);
+    const double a00 = dot3(d.Su, d.Su), a01 = dot3(d.Su, d.Sv), a11 = dot3(d.Sv, d.Sv);
+    const double n00 = a00 + dot3c(r, e.Suu), n01 = a01 + dot3c(r, e.Suv), n11 = a11 + dot3c(r, e.Svv);
+    const bool fu = !((u <= c.dom_u0 && g0 > 0) || (u >= c.dom_u1 && g0 < 0));
+    const bool fv = !((v <= c.dom_v0 && g1 > 0) || (v >= c.dom_v1 && g1 < 0));
+    double d0 = 0, d1 = 0;
+    if (fu && fv) {
+      const bool newton = n00 > 0 && det2(n00, n01, n11) > 0;
+      const double h00 = newton ? n00 : a00, h01 = newton ? n01 : a01, h11 = newton ? n11 : a11;
+      const double det = det2(h00, h01, h11);
+      if (!(det > 0)) return false;
+      d0 = fast::mad(h11, g0, -(h01 * g1)) / det;
+      d1 = fast::mad(h00, g1, -(h01 * g0)) / det;
+    } else if (fu) {
+      const double h = n00 > 0 ? n00 : a00;
+      if (!(h > 0)) return false;
+      d0 = g0 / h;
+    } else if (fv) {
+      const double h = n11 > 0 ? n11 : a11;
+      if (!(h > 0)) return false;
+      d1 = g1 / h;
+    }
+    if (!(isfinite(d0) && isfinite(d1))) return false;
+    const double un = clampd(u - d0, c.dom_u0, c.dom_u1), vn = clampd(v - d1, c.dom_v0, c.dom_v1);
+    const double du = u - un, dv = v - vn;
+    u = un;
+    v = vn;
+    if (fmax(fabs(du), fabs(dv)) <= kTolNewtonProj) {
+      const v3<double> r2 = {fast::mad(-d.Sv.x, dv, fast::mad(-d.Su.x, du, r.x)),
+                             fast::mad(-d.Sv.y, dv, fast::mad(-d.Su.y, du, r.y)),
+                             fast::mad(-d.Sv.z, dv, fast::mad(-d.Su.z, du, r.z))};
+      res = sqrt(dot3(r2, r2));
+      return isfinite(res);
+    }
+  }
+  return false;
 }
 
 // One warp projects the queries [q0, min(q0+32, qend)).
@@ -417,10 +472,14 @@ __device__ __forceinline__ void project_chunk(const Staged<kSmemSpans, MODE>& sm
       sd.it = 0;
       sd.hu = 0;
       sd.hv = 0;
-      int r = kContinue;
-      while (r == kContinue) r = project_iterate<P, Q>(cx, px, py, pz, sd);
       double rr;
-      if (r != kConverged || !finish64<P, Q>(cx, px, py, pz, sd.u, sd.v, sd.hu, sd.hv, rr)) return false;
+      if (!project_polish64<P, Q>(cx, px, py, pz, sd.u, sd.v, rr)) {
+        sd.u = u0;
+        sd.v = v0;
+        int r = kContinue;
+        while (r == kContinue) r = project_iterate<P, Q>(cx, px, py, pz, sd);
+        if (r != kConverged || !finish64<P, Q>(cx, px, py, pz, sd.u, sd.v, sd.hu, sd.hv, rr)) return false;
+      }
       if (ns == 1 && fabs(sd.u - us[0]) <= kDistinct && fabs(sd.v - vs[0]) <= kDistinct) {
         if (rr < rs[0]) { us[0] = sd.u; vs[0] = sd.v; rs[0] = rr; }
         return true;
