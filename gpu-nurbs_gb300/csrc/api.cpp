@@ -100,13 +100,15 @@ struct nurbs_surface_s {
   std::mutex mu;
 };
 
-// Enqueues one inversion on `st`: waits for the previous user of the counter slot, zeroes the
-// counter, launches, marks the slot.  Inside a stream capture the slot is used without the
-// event handshake (capture cannot wait on work recorded outside it).
-// precision: NURBS_PREC_FP64 / MIXED for the inversion, -1 / -3 for the projection (FP64 / mixed),
-// -2 / -4 for the adaptive quadtree inversion (FP64 / mixed, max_edge)
+// The persistent query kernels that take their work from a launch counter.
+enum class QueryOp { kInvert, kProject, kQuadtree };
+
+// Enqueues one launch of a query kernel on `st`: waits for the previous user of the counter
+// slot, zeroes the counter, launches, marks the slot.  Inside a stream capture the slot is used
+// without the event handshake (capture cannot wait on work recorded outside it).  precision:
+// NURBS_PREC_FP64 or NURBS_PREC_MIXED; max_edge: the quadtree inversion's.
 static cudaError_t invert_on(nurbs_surface_s* s, const double* P, int64_t n, double* uv, int* status, double* res,
-                             int precision, cudaStream_t st, double max_edge = 0) {
+                             int precision, cudaStream_t st, QueryOp op = QueryOp::kInvert, double max_edge = 0) {
   std::lock_guard<std::mutex> lk(s->mu);
   const int slot = (int)(s->next_slot++ % kCounterRing);
   cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
@@ -124,12 +126,10 @@ static cudaError_t invert_on(nurbs_surface_s* s, const double* P, int64_t n, dou
   }
   e = cudaMemsetAsync(s->counters + slot, 0, sizeof(unsigned), st);
   if (e == cudaSuccess) {
-    if (precision == -2 || precision == -4)
-      e = launch_invert_quadtree(s->dev, P, n, max_edge, uv, status, res,
-                                 precision == -4 ? NURBS_PREC_MIXED : NURBS_PREC_FP64, s->counters + slot, st);
-    else if (precision == -1 || precision == -3)
-      e = launch_project(s->dev, P, n, uv, status, res, precision == -3 ? NURBS_PREC_MIXED : NURBS_PREC_FP64,
-                         s->counters + slot, st);
+    if (op == QueryOp::kQuadtree)
+      e = launch_invert_quadtree(s->dev, P, n, max_edge, uv, status, res, precision, s->counters + slot, st);
+    else if (op == QueryOp::kProject)
+      e = launch_project(s->dev, P, n, uv, status, res, precision, s->counters + slot, st);
     else
       e = launch_invert(s->dev, P, n, uv, status, res, precision, s->counters + slot, st);
   }
@@ -218,6 +218,7 @@ int nurbs_surface_create(int p, int q, int nu, int nv, const double* knots_u, co
   if (e == cudaSuccess) e = launch_tree(d, st);
   if (e == cudaSuccess) e = launch_centre_ders(d, st);
   if (e == cudaSuccess) e = launch_cones(d, st);
+  if (e == cudaSuccess) e = launch_quadtree_boxes(d, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // img must outlive the copy
   if (e != cudaSuccess) {
     cudaFree(s->arena);
@@ -365,6 +366,7 @@ int nurbs_build_tree(nurbs_surface_t s, int levels, void* stream) {
   CUDA_TRY(launch_tree(s->dev, st), "tree launch");
   CUDA_TRY(launch_centre_ders(s->dev, st), "seed-centre derivatives");
   CUDA_TRY(launch_cones(s->dev, st), "normal cones");
+  CUDA_TRY(launch_quadtree_boxes(s->dev, st), "quadtree boxes");
   CUDA_TRY(cudaStreamSynchronize(st), "tree sync");
   s->tree_built = true;
   return NURBS_OK;
@@ -398,8 +400,8 @@ int nurbs_project(nurbs_surface_t s, const double* P_dev, int64_t n, double* uv_
     return fail(NURBS_E_INVALID, "precision %d is not FP64 or MIXED", precision);
   if (n == 0) return NURBS_OK;
   if (!P_dev || !uv_dev || !status_dev || !residual_dev) return fail(NURBS_E_INVALID, "NULL buffer");
-  CUDA_TRY(invert_on(s, P_dev, n, uv_dev, status_dev, residual_dev, precision == NURBS_PREC_MIXED ? -3 : -1,
-                     (cudaStream_t)stream),
+  CUDA_TRY(invert_on(s, P_dev, n, uv_dev, status_dev, residual_dev, precision, (cudaStream_t)stream,
+                     QueryOp::kProject),
            "project launch");
   return NURBS_OK;
 }
@@ -414,8 +416,8 @@ int nurbs_invert_quadtree(nurbs_surface_t s, const double* P_dev, int64_t n, dou
   if (n > 0xffffffffLL) return fail(NURBS_E_INVALID, "more than 2^32 - 1 queries");
   if (n == 0) return NURBS_OK;
   if (!P_dev || !uv_dev || !status_dev || !residual_dev) return fail(NURBS_E_INVALID, "NULL buffer");
-  CUDA_TRY(invert_on(s, P_dev, n, uv_dev, status_dev, residual_dev, precision == NURBS_PREC_MIXED ? -4 : -2,
-                     (cudaStream_t)stream, max_edge),
+  CUDA_TRY(invert_on(s, P_dev, n, uv_dev, status_dev, residual_dev, precision, (cudaStream_t)stream,
+                     QueryOp::kQuadtree, max_edge),
            "quadtree inversion launch");
   return NURBS_OK;
 }

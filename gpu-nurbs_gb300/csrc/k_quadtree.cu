@@ -76,8 +76,8 @@ __device__ __forceinline__ void put_node(double* o, double a, double b, double c
 }
 
 // Precomputed boxes of the top kQtDepth levels of square children (depth d, u index a, v index b:
-// code = base(d) + a * 2^d + b; base = 0, 1, 5).  Deeper nodes, and the halves of U / V splits,
-// scan their control points.
+// code = base(d) + a * 2^d + b; base = 0, 1, 5), written when the surface is converted.  Deeper
+// nodes, and the halves of U / V splits, scan their control points.
 constexpr int kQtDepth = 3;
 constexpr int kQtBoxes = 1 + 4 + 16;
 __device__ __forceinline__ int code_depth(int c) { return c == 0 ? 0 : (c < 5 ? 1 : 2); }
@@ -417,7 +417,6 @@ cudaError_t launch_quadtree_mode(const SurfDev& s, const double* P_, int64_t n, 
   }
   int64_t blocks = ((n + 31) / 32 + kWarps - 1) / kWarps;
   if (blocks > cached[dev]) blocks = cached[dev];
-  k_quadtree_boxes<<<kQtBoxes, 256, 0, st>>>(s, s.qtbox);
   k_invert_quadtree<P, Q, MODE><<<(unsigned)blocks, kThreads, 0, st>>>(s, s.qtbox, P_, n, max_edge, uv, st_, res,
                                                                        counter);
   return cudaGetLastError();
@@ -432,6 +431,11 @@ cudaError_t launch_quadtree_pq(const SurfDev& s, const double* P_, int64_t n, do
 }
 
 }  // namespace
+
+cudaError_t launch_quadtree_boxes(const SurfDev& s, cudaStream_t st) {
+  k_quadtree_boxes<<<kQtBoxes, 256, 0, st>>>(s, s.qtbox);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_invert_quadtree(const SurfDev& s, const double* P, int64_t n, double max_edge, double* uv,
                                    int* status, double* residual, int precision, unsigned* counter, cudaStream_t st) {

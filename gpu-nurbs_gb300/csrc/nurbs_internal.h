@@ -43,7 +43,7 @@ constexpr int kConeStride = 20;   // floats per normal-cone record
 //   lattice[65][81][3]               surface points of each node's 9x9 lattice (index 9 tx + ty),
 //                                    FP32 relative to org: distance bounds and projection seeds
 //   qtbox[21][6]                     control-point boxes of the quadtree inversion's square nodes of
-//                                    depth 0..2, written by each quadtree launch
+//                                    depth 0..2, written with the tree
 struct SurfDev {
   int p, q, nu, nv;
   int ns_u, ns_v;
@@ -154,7 +154,9 @@ cudaError_t launch_cones(const SurfDev& s, cudaStream_t st);
 // the projection: closest point over the closed domain (k_project.cu)
 cudaError_t launch_project(const SurfDev& s, const double* P, int64_t n, double* uv, int* status,
                            double* residual, int precision, unsigned* counter, cudaStream_t st);
-// adaptive quadtree inversion (k_quadtree.cu)
+// adaptive quadtree inversion (k_quadtree.cu); its top levels' control-point boxes (qtbox), written
+// with the tree
+cudaError_t launch_quadtree_boxes(const SurfDev& s, cudaStream_t st);
 cudaError_t launch_invert_quadtree(const SurfDev& s, const double* P, int64_t n, double max_edge, double* uv,
                                    int* status, double* residual, int precision, unsigned* counter, cudaStream_t st);
 // S, Su, Sv at the built nodes' uv-centres (cd32/cd64), after the tree is built

@@ -69,9 +69,8 @@ def test_quadtree_arguments(nurbs):
 
 
 def test_quadtree_and_projection_on_concurrent_streams(nurbs):
-    """The same surface on two streams at once (each launch rewrites the surface's top-level box
-    table with the same values; each call takes its own launch counter): the results equal those
-    of the calls one after the other."""
+    """The same surface on two streams at once (each call takes its own launch counter): the
+    results equal those of the calls one after the other."""
     from gpu_nurbs_gb300 import synth
     sf = synth.surface_large()
     s, o = nurbs.Surface(sf), O.OracleSurface(sf)
