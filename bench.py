@@ -15,7 +15,8 @@ FP64, oracle parity sample), "quintic" (degree 5, 256x256 net, 2^24 queries, per
 error against the oracle), "eval_large" (2^26 evaluations of S..Svv, FP64 and FP32, with their
 rooflines), "project" (nurbs_project of 2^20 points near and far from the 64x64 surface, mixed and
 FP64, oracle parity sample), "quadtree" (nurbs_invert_quadtree of 2^20 points on that surface, no
-tree build) and "serving" (continuous batching over a pool of 10^4 surfaces: peak
+tree build), "pcurve" (nurbs_pcurve of 2^20 samples of closed curves on that surface) and
+"serving" (continuous batching over a pool of 10^4 surfaces: peak
 throughput, p50/p99 at half of peak, FP64 server at the top rate).  --headline-only leaves them
 out.
 
@@ -352,7 +353,8 @@ def run_ours(a):
         line["cpu_baseline"], line["parity_sample"] = cpu_baseline(surf, P, a.cpu_sample, g_uv, g_st, res_mixed)
     if world == 1 and not a.headline_only and a.workload == "large":
         for name, fn in (("batched", batched_record), ("quintic", quintic_record), ("eval_large", eval_record),
-                         ("project", project_record), ("quadtree", quadtree_record), ("serving", serving_record)):
+                         ("project", project_record), ("quadtree", quadtree_record), ("pcurve", pcurve_record),
+                         ("serving", serving_record)):
             t0 = time.perf_counter()
             try:
                 line[name] = fn(a, compact=True)
@@ -688,6 +690,70 @@ def quadtree_record(a, compact=False):
     return rec
 
 
+def pcurve_record(a, compact=False):
+    """p-curves (nurbs_pcurve, mixed and FP64): 2^20 ordered samples of closed curves on the 64x64
+    bicubic surface (256 loops of 4096 samples, radii and centres seeded), each sample 1e-3 off the
+    surface along its normal.  Samples/s, parity with the oracle's p-curve on a bounded sample
+    (status, flags, parameters to 1e-9) and its CPU time."""
+    import torch
+    gn = load_pkg()
+    from gpu_nurbs_gb300 import synth
+    n_loops, per = (256, 4096) if compact or not a.queries else (max(1, a.queries // 4096), 4096)
+    n = n_loops * per
+    steps = 5 if compact else a.steps
+    surf = synth.surface_large()
+    s = gn.Surface(surf)
+    r = np.random.default_rng(77)
+    t = np.linspace(0.0, 1.0, per)
+    cu, cv = 0.25 + 0.5 * r.random(n_loops), 0.25 + 0.5 * r.random(n_loops)
+    ru, rv = 0.05 + 0.15 * r.random(n_loops), 0.05 + 0.15 * r.random(n_loops)
+    uv = np.stack([(cu[:, None] + ru[:, None] * np.cos(2 * np.pi * t)).ravel(),
+                   (cv[:, None] + rv[:, None] * np.sin(2 * np.pi * t)).ravel()], 1)
+    E = s.eval(torch.as_tensor(uv, device="cuda"), gn.S | gn.SU | gn.SV).cpu().numpy()
+    N = np.cross(E[3:6].T, E[6:9].T)
+    N /= np.linalg.norm(N, axis=1)[:, None]
+    C = np.ascontiguousarray(E[0:3].T + 1e-3 * N)
+    Cd = torch.as_tensor(C, device="cuda")
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    timed = event_timer(torch, flush)
+    run = lambda: s.pcurve(Cd, gn.PREC_MIXED)
+    run64 = lambda: s.pcurve(Cd, gn.PREC_FP64)
+    for _ in range(3):
+        run()
+    run64()
+    torch.cuda.synchronize()
+    clocks = Clocks(0)
+    tm = timed(run, steps)
+    t64 = timed(run64, max(2, steps // 2))
+    clk = clocks.stop()
+    g_uv, g_st, g_res, g_fl = (x.cpu().numpy() for x in run())
+    ms, ms64 = sum(tm) / len(tm), sum(t64) / len(t64)
+    rec = {"value": n / (ms / 1e3), "unit": "samples/s", "ms_per_step": ms, "steps": steps, "dtype": "f32+f64",
+           "fp64_value": n / (ms64 / 1e3), "fp64_ms_per_step": ms64, "mixed_vs_fp64": ms64 / ms,
+           "config": {"workload": f"pcurve-64x64-bicubic: {n_loops} closed loops x {per} samples, 1e-3 off the surface",
+                      "l2": "flushed (512 MB write) before each step"},
+           "found_frac": float(np.mean(g_st <= 1)), "flagged_frac": float(np.mean(g_fl != 0)),
+           "max_uv_err_vs_curve": float(np.abs(g_uv - uv)[g_st == 0].max()), "clocks": clk}
+    if not a.no_cpu:
+        import oracle as O
+        m = min(a.cpu_sample // per, n_loops) * per
+        o = O.OracleSurface(surf)
+        t0 = time.perf_counter()
+        ouv, ost, ores, ofl = o.pcurve(C[:m], threads=host_cores())
+        dt = time.perf_counter() - t0
+        f = (ost <= 1) & (g_st[:m] <= 1)
+        rec["parity_sample"] = {"n": m, "status_equal": int(np.sum(g_st[:m] == ost)),
+                                "flags_equal": int(np.sum(g_fl[:m] == ofl)),
+                                "max_uv_diff": float(np.abs(g_uv[:m][f] - ouv[f]).max()) if f.any() else 0.0}
+        rec["cpu_baseline"] = {"value": m / dt, "unit": "samples/s", "cores": host_cores(), "kind": "port",
+                               "sample": f"the first {m // per} loops of the workload, the oracle's p-curve"}
+    return rec
+
+
+def run_pcurve(a):
+    print(json.dumps(pcurve_record(a)))
+
+
 def run_quadtree(a):
     print(json.dumps(quadtree_record(a)))
 
@@ -743,6 +809,16 @@ def eval_record(a, compact=False, which="eval-large"):
     def ev32g():
         gn.check(L.nurbs_eval_f32(s.h, uvg.data_ptr(), ng, mask, out32.data_ptr(), gn._stream()), "eval")
 
+    # third order (Suuu..Svvv) and the normal with its second derivatives, FP64, on a quarter of
+    # the points (their outputs share the FP64 output buffer)
+    n3 = n // 4
+
+    def ev3():
+        gn.check(L.nurbs_eval(s.h, uv.data_ptr(), n3, 0x3C0, out.data_ptr(), gn.PREC_FP64, gn._stream()), "eval")
+
+    def evn():
+        gn.check(L.nurbs_eval_normal(s.h, uv.data_ptr(), n3, 0x39, out.data_ptr(), gn._stream()), "eval")
+
     for _ in range(3):
         ev64()
         ev32()
@@ -752,6 +828,8 @@ def eval_record(a, compact=False, which="eval-large"):
     t64 = timed(ev64, steps)
     t32 = timed(ev32, steps)
     t32g = timed(ev32g, steps)
+    t3 = timed(ev3, steps) if nb >= 4 else [float("nan")]
+    tn = timed(evn, steps) if nb >= 4 else [float("nan")]
     clk = clocks.stop()
     ms64, ms32 = sum(t64) / len(t64), sum(t32) / len(t32)
     ms32g = sum(t32g) / len(t32g)
@@ -779,12 +857,16 @@ def eval_record(a, compact=False, which="eval-large"):
                      "fp32": {"bound": "hbm", "achieved": gbs32, "peak": hbm, "unit": "GB/s",
                               "frac": gbs32 / hbm if hbm else None, "peak_source": hbm_src,
                               "note": "random (u,v): bound by the L1 wavefronts of per-lane span gathers"},
+                     "fp64_third_order": {"points_per_step": n3, "value": n3 / (sum(t3) / len(t3) / 1e3),
+                                          "outputs": "Suuu, Suuv, Suvv, Svvv"},
+                     "fp64_normals": {"points_per_step": n3, "value": n3 / (sum(tn) / len(tn) / 1e3),
+                                      "outputs": "N, Nuu, Nuv, Nvv"},
                      "fp32_grid": {"points_per_step": ng, "value": ng / (ms32g / 1e3), "ms_per_step": ms32g,
                                    "bound": "hbm", "achieved": bytes32 * ng / (ms32g / 1e3) / 1e9, "peak": hbm,
                                    "unit": "GB/s", "frac": bytes32 * ng / (ms32g / 1e3) / 1e9 / hbm if hbm else None,
                                    "uv": "row-major parameter grid (tessellation order)"},
                      "fp32_achieved_tflops": flop * n / (ms32 / 1e3) / 1e12, "fp32_peak": peak32},
-        "clocks": clk, "gpu_launches": 3 * steps,
+        "clocks": clk, "gpu_launches": 5 * steps,
     }
 
 
@@ -971,7 +1053,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="large",
-                    choices=["large", "small", "quintic", "batched", "eval-small", "eval-large", "serving", "project", "quadtree"])
+                    choices=["large", "small", "quintic", "batched", "eval-small", "eval-large", "serving", "project", "quadtree", "pcurve"])
     ap.add_argument("--rates", default="1000,10000,30000,100000,300000,1000000")
     ap.add_argument("--serve-seconds", type=float, default=1.0)
     ap.add_argument("--max-requests", type=int, default=40000)
@@ -999,6 +1081,8 @@ def main():
         run_project(a)
     elif a.workload == "quadtree":
         run_quadtree(a)
+    elif a.workload == "pcurve":
+        run_pcurve(a)
     else:
         run_ours(a)
 
