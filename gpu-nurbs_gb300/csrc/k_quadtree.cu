@@ -5,14 +5,14 @@
 //
 // A persistent grid whose warps take chunks of 32 queries from a counter.  The first layer (the
 // root: its precomputed box and one trajectory from the domain's centre) runs lane per query and
-// answers most queries; with MODE mixed that trajectory runs in FP32 and its end takes FP64
-// Newton steps (the mixed inversion's final steps).  A query it leaves open is then searched by
-// the whole warp, in FP64:
+// answers most queries.  A query it leaves open is then searched by the whole warp.  With MODE
+// mixed every node's trajectory runs in FP32 and its end takes FP64 Newton steps (the mixed
+// inversion's final steps); the box checks and split decisions stay exact FP64:
 //   * a layer's nodes live in shared memory; each node's control-point box is reduced by the
 //     whole warp (lanes stride over the node's control-point rows and columns, min/max by
 //     shuffles: exact, so the pass/fail decisions equal the oracle's);
-//   * the passing nodes' trajectories run one per lane (the inversion's FP64 iteration from the
-//     node centre); a result counts when it converged inside the domain within max_edge of P;
+//   * the passing nodes' trajectories run one per lane (from the node centre); a result counts
+//     when it converged inside the domain within max_edge of P;
 //   * the first layer with a result answers (its closest result; AMBIGUOUS as in the inversion);
 //     otherwise each passing node is split by the reference's getSplitType, evaluated with the
 //     reference-order FP64 functions (this translation unit is compiled with --fmad=false, so
@@ -143,10 +143,56 @@ __global__ void __launch_bounds__(256) k_quadtree_boxes(SurfDev s, double* __res
   }
 }
 
+// One node's trajectory from (u, v): FP64 (the inversion's FP64 iteration), or MIXED (the mixed
+// inversion's FP32 iteration, the point relative to the control net's centre, then its FP64
+// final steps).  True when it converged inside the domain within max_edge of P; (u, v, rr) the
+// result.
+template <int P, int Q, int MODE>
+__device__ bool node_trajectory(const SurfDev& s, const Ctx& cx, double px, double py, double pz, double max_edge,
+                                double& u, double& v, double& rr) {
+  if constexpr (MODE == kModeMixed) {
+    Seed<float> sd;
+    sd.u = (float)u;
+    sd.v = (float)v;
+    sd.prev = INFINITY;
+    sd.it = 0;
+    sd.hu = 0;
+    sd.hv = 0;
+    sd.newton = false;
+    const float tx = (float)(px - s.org[0]), ty = (float)(py - s.org[1]), tz = (float)(pz - s.org[2]);
+    const float eu = 2.0f * (float)(s.dom_u1 - s.dom_u0), ev = 2.0f * (float)(s.dom_v1 - s.dom_v0);
+    const float far[4] = {(float)s.dom_u0 - eu, (float)s.dom_u1 + eu, (float)s.dom_v0 - ev, (float)s.dom_v1 + ev};
+    float dist;
+    int r = kContinue;
+    while (r == kContinue) {
+      r = iterate32<P, Q>(cx, tx, ty, tz, sd, dist);
+      if (r == kContinue && !(sd.u >= far[0] && sd.u <= far[1] && sd.v >= far[2] && sd.v <= far[3])) r = kFailed;
+    }
+    if (r != kConverged) return false;
+    u = sd.u;
+    v = sd.v;
+    return final64<P, Q>(cx, px, py, pz, u, v, rr) && rr < max_edge;
+  } else {
+    Seed<double> sd;
+    sd.u = u;
+    sd.v = v;
+    sd.prev = INFINITY;
+    sd.it = 0;
+    sd.hu = 0;
+    sd.hv = 0;
+    sd.newton = false;
+    int r = kContinue;
+    while (r == kContinue) r = iterate64<P, Q>(cx, px, py, pz, sd);
+    u = sd.u;
+    v = sd.v;
+    return r == kConverged && finish64<P, Q>(cx, px, py, pz, u, v, sd.hu, sd.hv, rr) && rr < max_edge;
+  }
+}
+
 // The whole warp searches one query's tree.  root_failed: the root passed and its trajectory had
 // no result (the chunk's lane-per-query first layer found that), so layer 0 goes straight to the
 // split.
-template <int P, int Q>
+template <int P, int Q, int MODE>
 __device__ void quadtree_query(const SurfDev& s, const Ctx& cx, QtWarp& w, const double* __restrict__ qtbox,
                                const double* __restrict__ Pq, int64_t qi, double max_edge, bool root_failed,
                                double* __restrict__ uv_out, int* __restrict__ st_out, double* __restrict__ res_out) {
@@ -199,21 +245,11 @@ __device__ void quadtree_query(const SurfDev& s, const Ctx& cx, QtWarp& w, const
       w.ok[i] = 0;
       if (!w.pass[i]) continue;
       const double* nd = w.node[cur][i];
-      Seed<double> sd;
-      sd.u = (nd[0] + nd[2]) / 2;
-      sd.v = (nd[1] + nd[3]) / 2;
-      sd.prev = INFINITY;
-      sd.it = 0;
-      sd.hu = 0;
-      sd.hv = 0;
-      sd.newton = false;
-      int r = kContinue;
-      while (r == kContinue) r = iterate64<P, Q>(cx, px, py, pz, sd);
-      double rr;
-      if (r == kConverged && finish64<P, Q>(cx, px, py, pz, sd.u, sd.v, sd.hu, sd.hv, rr) && rr < max_edge) {
+      double u = (nd[0] + nd[2]) / 2, v = (nd[1] + nd[3]) / 2, rr;
+      if (node_trajectory<P, Q, MODE>(s, cx, px, py, pz, max_edge, u, v, rr)) {
         w.ok[i] = 1;
-        w.su[i] = sd.u;
-        w.sv[i] = sd.v;
+        w.su[i] = u;
+        w.sv[i] = v;
         w.sr[i] = rr;
       }
     }
@@ -334,48 +370,8 @@ __global__ void __launch_bounds__(kThreads)
       int status = 2;  // the root alone does not pass: no node ever passes
       double ou = __longlong_as_double(0x7ff8000000000000ll), ov = ou, orr = ou;
       if (pass) {
-        bool ok = false;
         double u = (s.dom_u0 + s.dom_u1) / 2, v = (s.dom_v0 + s.dom_v1) / 2, rr = 0;
-        if constexpr (MODE == kModeMixed) {
-          // the root's trajectory in FP32 (the mixed inversion's iteration, the point relative to
-          // the control net's centre), then its FP64 Newton steps and residual
-          Seed<float> sd;
-          sd.u = (float)u;
-          sd.v = (float)v;
-          sd.prev = INFINITY;
-          sd.it = 0;
-          sd.hu = 0;
-          sd.hv = 0;
-          sd.newton = false;
-          const float tx = (float)(px - s.org[0]), ty = (float)(py - s.org[1]), tz = (float)(pz - s.org[2]);
-          const float eu = 2.0f * (float)(s.dom_u1 - s.dom_u0), ev = 2.0f * (float)(s.dom_v1 - s.dom_v0);
-          const float far[4] = {(float)s.dom_u0 - eu, (float)s.dom_u1 + eu, (float)s.dom_v0 - ev, (float)s.dom_v1 + ev};
-          float dist;
-          int r = kContinue;
-          while (r == kContinue) {
-            r = iterate32<P, Q>(cx, tx, ty, tz, sd, dist);
-            if (r == kContinue && !(sd.u >= far[0] && sd.u <= far[1] && sd.v >= far[2] && sd.v <= far[3])) r = kFailed;
-          }
-          if (r == kConverged) {
-            u = sd.u;
-            v = sd.v;
-            ok = final64<P, Q>(cx, px, py, pz, u, v, rr) && rr < max_edge;
-          }
-        } else {
-          Seed<double> sd;
-          sd.u = u;
-          sd.v = v;
-          sd.prev = INFINITY;
-          sd.it = 0;
-          sd.hu = 0;
-          sd.hv = 0;
-          sd.newton = false;
-          int r = kContinue;
-          while (r == kContinue) r = iterate64<P, Q>(cx, px, py, pz, sd);
-          u = sd.u;
-          v = sd.v;
-          ok = r == kConverged && finish64<P, Q>(cx, px, py, pz, u, v, sd.hu, sd.hv, rr) && rr < max_edge;
-        }
+        const bool ok = node_trajectory<P, Q, MODE>(s, cx, px, py, pz, max_edge, u, v, rr);
         if (ok) {
           status = 0;
           ou = u;
@@ -396,7 +392,8 @@ __global__ void __launch_bounds__(kThreads)
     while (m) {
       const int j = __ffs(m) - 1;
       m &= m - 1;
-      quadtree_query<P, Q>(s, cx, w, qtbox, Pq, (int64_t)ch * 32 + j, max_edge, true, uv_out, st_out, res_out);
+      quadtree_query<P, Q, MODE>(s, cx, w, qtbox, Pq, (int64_t)ch * 32 + j, max_edge, true, uv_out, st_out,
+                                 res_out);
     }
   }
 }
