@@ -14,11 +14,12 @@
 //   * the passing nodes' trajectories run one per lane (from the node centre); a result counts
 //     when it converged inside the domain within max_edge of P;
 //   * the first layer with a result answers (its closest result; AMBIGUOUS as in the inversion);
-//     otherwise each passing node is split by the reference's getSplitType, evaluated with the
-//     reference-order FP64 functions (this translation unit is compiled with --fmad=false, so
-//     the split decisions, and with them the tree, are the oracle's bit for bit; the v-length
-//     uses the v-derivative, which the reference takes with MatrixSurfaceDerivativeU), and the
-//     children are compacted into the next layer in the reference's order by a warp prefix sum.
+//     otherwise each passing node is split by the reference's getSplitType, decided in FP32 where
+//     its lengths are clearly off max_edge and else evaluated with the reference-order FP64
+//     functions (this translation unit is compiled with --fmad=false, so the split decisions,
+//     and with them the tree, are the oracle's; the v-length uses the v-derivative, which the
+//     reference takes with MatrixSurfaceDerivativeU), and the children are compacted into the
+//     next layer in the reference's order by a warp prefix sum.
 // Culled nodes are not split (their control-point box does not hold P, so neither does their
 // surface); a layer of more than 64 nodes or 60 layers ends the query unanswered.
 #include "invert_core.cuh"
@@ -65,6 +66,38 @@ __device__ int split_type(const SurfDev& s, const double* nd, double max_edge) {
   if (nd[2] - nd[0] > 0.25 || nd[3] - nd[1] > 0.25) return 3;
   if (ul < max_edge) return 1;
   if (vl < max_edge) return 2;
+  return 3;
+}
+
+// getSplitType decided in FP32 where that is safe: the lengths from the FP32 tables' derivatives
+// (errors below 1e-4 of their size), used when each is more than 1 % away from max_edge and every
+// sample falls in the same span as in FP64; otherwise the reference-order FP64 evaluation above.
+// Both give the same decision, the FP32 one at a fraction of the FP64 work.
+template <int P, int Q>
+__device__ int split_type_fast(const SurfDev& s, const Ctx& cx, const double* nd, double max_edge) {
+  const double iu = (nd[2] - nd[0]) / 4, iv = (nd[3] - nd[1]) / 4;
+  float ul = 0, vl = 0;
+  bool exact = false;
+  for (int i = 0; i < 4; ++i) {
+    const double x = nd[0] + i * iu, y = nd[1] + i * iv;
+    const int su = exact::find_seg(s.bu, s.ns_u, x), sv = exact::find_seg(s.bv, s.ns_v, y);
+    int hu = su, hv = sv;
+    const fast::SDer<float> d = fast::eval_at<float, P, Q, 1, true>(cx.L32, cx.m32, cx.p, cx.q, (float)x, (float)y,
+                                                                  hu, hv);
+    exact = exact || hu != su || hv != sv;
+    ul += sqrtf(dot3(d.Su, d.Su));
+    vl += sqrtf(dot3(d.Sv, d.Sv));
+  }
+  ul *= (float)((nd[2] - nd[0]) * 0.25);
+  vl *= (float)((nd[3] - nd[1]) * 0.25);
+  const float me = (float)max_edge;
+  exact = exact || !(fabsf(ul - me) > 0.01f * me) || !(fabsf(vl - me) > 0.01f * me);
+  if (exact) return split_type(s, nd, max_edge);
+  const bool us = ul < me, vs = vl < me;
+  if (us && vs) return 0;
+  if (nd[2] - nd[0] > 0.25 || nd[3] - nd[1] > 0.25) return 3;
+  if (us) return 1;
+  if (vs) return 2;
   return 3;
 }
 
@@ -274,7 +307,7 @@ __device__ void quadtree_query(const SurfDev& s, const Ctx& cx, QtWarp& w, const
     for (int r = 0; r < 2; ++r) {
       const int i = lane + 32 * r;
       if (i < size && w.pass[i]) {
-        typ[r] = split_type(s, w.node[cur][i], max_edge);
+        typ[r] = split_type_fast<P, Q>(s, cx, w.node[cur][i], max_edge);
         nch[r] = typ[r] == 3 ? 4 : (typ[r] == 0 ? 0 : 2);
       }
     }
