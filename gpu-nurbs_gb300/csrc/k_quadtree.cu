@@ -69,10 +69,13 @@ __device__ int split_type(const SurfDev& s, const double* nd, double max_edge) {
   return 3;
 }
 
-// getSplitType decided in FP32 where that is safe: the lengths from the FP32 tables' derivatives
-// (errors below 1e-4 of their size), used when each is more than 1 % away from max_edge and every
+// getSplitType decided in FP32 where that is safe: the lengths from the FP32 tables' derivatives,
+// used when each differs from max_edge by more than 1 % of max_edge plus 0.1 % of itself and every
 // sample falls in the same span as in FP64; otherwise the reference-order FP64 evaluation above.
-// Both give the same decision, the FP32 one at a fraction of the FP64 work.
+// Measured against the FP64 lengths over 20,000 nodes (depths 0-8) of six surfaces up to degree 5
+// and 256x256 nets, the FP32 lengths err by at most 1.4e-4 of themselves, so both give the same
+// decision; the FP32 one costs a fraction of the FP64 work (the FP64 split types took most of a
+// launch).
 template <int P, int Q>
 __device__ int split_type_fast(const SurfDev& s, const Ctx& cx, const double* nd, double max_edge) {
   const double iu = (nd[2] - nd[0]) / 4, iv = (nd[3] - nd[1]) / 4;
@@ -91,7 +94,7 @@ __device__ int split_type_fast(const SurfDev& s, const Ctx& cx, const double* nd
   ul *= (float)((nd[2] - nd[0]) * 0.25);
   vl *= (float)((nd[3] - nd[1]) * 0.25);
   const float me = (float)max_edge;
-  exact = exact || !(fabsf(ul - me) > 0.01f * me) || !(fabsf(vl - me) > 0.01f * me);
+  exact = exact || !(fabsf(ul - me) > 0.01f * me + 1e-3f * ul) || !(fabsf(vl - me) > 0.01f * me + 1e-3f * vl);
   if (exact) return split_type(s, nd, max_edge);
   const bool us = ul < me, vs = vl < me;
   if (us && vs) return 0;
