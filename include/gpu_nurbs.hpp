@@ -110,9 +110,15 @@ class Surface {
   void matrix_n(double* matrix_n_dev, void* stream = nullptr) const {
     check(nurbs_get_matrix_n(h_, matrix_n_dev, stream), "nurbs_get_matrix_n");
   }
-  // S / Su / Sv / Suu / Suv / Svv (mask bits) at n device (u,v) pairs, SoA output
-  void eval(const double* uv_dev, int64_t n, unsigned mask, double* out_dev, void* stream = nullptr) const {
-    check(nurbs_eval(h_, uv_dev, n, mask, out_dev, NURBS_PREC_FP64, stream), "nurbs_eval");
+  // S / Su / Sv / Suu / Suv / Svv / Suuu..Svvv (mask bits) at n device (u,v) pairs, SoA output;
+  // precision NURBS_PREC_EXACT: the reference's expressions term by term (mask <= 63)
+  void eval(const double* uv_dev, int64_t n, unsigned mask, double* out_dev, void* stream = nullptr,
+            int precision = NURBS_PREC_FP64) const {
+    check(nurbs_eval(h_, uv_dev, n, mask, out_dev, precision, stream), "nurbs_eval");
+  }
+  // N = Su x Sv and its derivatives (NURBS_N..NURBS_NVV bits), SoA output
+  void eval_normal(const double* uv_dev, int64_t n, unsigned mask, double* out_dev, void* stream = nullptr) const {
+    check(nurbs_eval_normal(h_, uv_dev, n, mask, out_dev, stream), "nurbs_eval_normal");
   }
   void eval_f32(const float* uv_dev, int64_t n, unsigned mask, float* out_dev, void* stream = nullptr) const {
     check(nurbs_eval_f32(h_, uv_dev, n, mask, out_dev, stream), "nurbs_eval_f32");
@@ -127,6 +133,22 @@ class Surface {
   void invert_host(const double* P, int64_t n, double* uv, int* status, double* residual,
                    int precision = NURBS_PREC_MIXED, void* stream = nullptr) const {
     check(nurbs_invert_host(h_, P, n, uv, status, residual, precision, stream), "nurbs_invert_host");
+  }
+  // closest points over the closed domain (nurbs_project)
+  void project(const double* P_dev, int64_t n, double* uv_dev, int* status_dev, double* residual_dev,
+               int precision = NURBS_PREC_MIXED, void* stream = nullptr) const {
+    check(nurbs_project(h_, P_dev, n, uv_dev, status_dev, residual_dev, precision, stream), "nurbs_project");
+  }
+  // the tree-free adaptive quadtree inversion (nurbs_invert_quadtree)
+  void invert_quadtree(const double* P_dev, int64_t n, double max_edge, double* uv_dev, int* status_dev,
+                       double* residual_dev, int precision = NURBS_PREC_MIXED, void* stream = nullptr) const {
+    check(nurbs_invert_quadtree(h_, P_dev, n, max_edge, uv_dev, status_dev, residual_dev, precision, stream),
+          "nurbs_invert_quadtree");
+  }
+  // p-curve of ordered curve samples (nurbs_pcurve)
+  void pcurve(const double* C_dev, int64_t n, double* uv_dev, int* status_dev, double* residual_dev, int* flags_dev,
+              int precision = NURBS_PREC_MIXED, void* stream = nullptr) const {
+    check(nurbs_pcurve(h_, C_dev, n, uv_dev, status_dev, residual_dev, flags_dev, precision, stream), "nurbs_pcurve");
   }
 
  private:

@@ -61,6 +61,21 @@ int main() {
     };
     std::vector<double> got(2 * n);
 
+    // the surface calls beyond the inversion: projection, quadtree inversion, p-curve (points on
+    // the surface: each returns the generating parameters)
+    int* d_fl;
+    CK(cudaMalloc(&d_fl, sizeof(int) * n));
+    surf.project(d_P, n, d_out_uv, d_st, d_res);
+    CK(cudaMemcpy(got.data(), d_out_uv, sizeof(double) * 2 * n, cudaMemcpyDeviceToHost));
+    check_uv(got);
+    surf.invert_quadtree(d_P, n, 1e-4, d_out_uv, d_st, d_res);
+    CK(cudaMemcpy(got.data(), d_out_uv, sizeof(double) * 2 * n, cudaMemcpyDeviceToHost));
+    check_uv(got);
+    surf.pcurve(d_P, n, d_out_uv, d_st, d_res, d_fl);
+    CK(cudaMemcpy(got.data(), d_out_uv, sizeof(double) * 2 * n, cudaMemcpyDeviceToHost));
+    check_uv(got);
+    CK(cudaFree(d_fl));
+
     nurbs::Pool pool(int64_t(64) << 20, 16);
     std::vector<int> ids = pool.add({desc, desc});
     nurbs::Batch batch{{ids[0], ids[1]}, {0, n / 2, n}};
