@@ -5,8 +5,9 @@
 // Three passes over the samples, all on the caller's stream:
 //   1. every sample is inverted as nurbs_invert does (tree candidates, GN then Newton, FP64 or
 //      mixed precision);
-//   2. continuation: each sample also takes FP64 Newton steps from its two neighbours' pass-1
-//      parameters, and keeps such a minimum when it is strictly closer than its own (a curve
+//   2. continuation: each sample also takes Newton steps (FP64, with the FP32 curvature term
+//      first) from its two neighbours' pass-1 parameters, and keeps such a minimum when it is
+//      strictly closer than its own (a curve
 //      sample's closest point is usually next to its neighbour's, even where the tree seeds miss
 //      it); a sample without an answer takes the closer of the two;
 //   3. flags per sample: NURBS_PCURVE_JUMP when the parameter step from the previous sample is
@@ -38,10 +39,21 @@ __device__ __forceinline__ Ctx global_ctx(const SurfDev& s) {
   return cx;
 }
 
-// FP64 Newton steps (GN where the Hessian is not positive definite) from (u, v) toward the
-// minimum of |S - P|; true when they converge inside the domain, with the residual.
+// Newton steps (GN where the Hessian is not positive definite) from (u, v) toward the minimum of
+// |S - P|; true when they converge inside the domain, with the residual.  First the mixed
+// inversion's final steps (S, Su, Sv in FP64, the curvature term from FP32 second derivatives:
+// a neighbour's answer is next to the sample's minimum, where those converge as the FP64 steps
+// do at a fraction of the FP64 work), then, where they do not converge, FP64 Newton steps.
 template <int P, int Q>
 __device__ bool continue_from(const Ctx& cx, double px, double py, double pz, double& u, double& v, double& res) {
+  {
+    double uu = u, vv = v;
+    if (final64<P, Q>(cx, px, py, pz, uu, vv, res)) {
+      u = uu;
+      v = vv;
+      return true;
+    }
+  }
   Seed<double> sd;
   sd.u = u;
   sd.v = v;
