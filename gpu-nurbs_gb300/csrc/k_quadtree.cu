@@ -256,7 +256,7 @@ __device__ void quadtree_query(const SurfDev& s, const Ctx& cx, QtWarp& w, const
     for (int i = 0; i < (known ? 0 : size); ++i) {
       const double* nd = w.node[cur][i];
       double mn[3], mx[3];
-      if (w.code[cur][i] >= 0) {  // the top levels' boxes, computed once per launch
+      if (w.code[cur][i] >= 0) {  // the top levels' boxes, written with the surface
         const double* b = qtbox + 6 * w.code[cur][i];
         for (int c = 0; c < 3; ++c) {
           mn[c] = b[c];
