@@ -6,6 +6,7 @@
 
 #include <cmath>
 #include <cstdarg>
+#include <cstdint>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -48,6 +49,44 @@ namespace {
     cudaError_t e_ = (expr);                         \
     if (e_ != cudaSuccess) return cuda_fail(e_, what); \
   } while (0)
+
+// Temporary device buffers of a call (host-buffer inversion, p-curve scratch, ...) come from
+// a stream-ordered pool of the library's own, one per device, that keeps up to kTmpKeepBytes
+// of freed memory between calls.  The device's default pool keeps none: it returns freed
+// memory to the system at every synchronisation, and mapping it again on the next call costs
+// more than the host<->device copies of a 2^20-query call.  The pools live as long as the
+// process's contexts: like every handle of this library, they do not survive cudaDeviceReset.
+constexpr int kTmpDevices = 64;
+constexpr uint64_t kTmpKeepBytes = 512ull << 20;
+
+cudaError_t tmp_alloc(void** p, size_t bytes, cudaStream_t st) {
+  static std::mutex mu;
+  static cudaMemPool_t pools[kTmpDevices] = {};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= kTmpDevices) return cudaMallocAsync(p, bytes, st);
+  cudaMemPool_t pool;
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    if (!pools[dev]) {
+      cudaMemPoolProps props{};
+      props.allocType = cudaMemAllocationTypePinned;
+      props.location.type = cudaMemLocationTypeDevice;
+      props.location.id = dev;
+      cudaMemPool_t created;
+      if ((e = cudaMemPoolCreate(&created, &props)) != cudaSuccess) return e;
+      uint64_t keep = kTmpKeepBytes;
+      if ((e = cudaMemPoolSetAttribute(created, cudaMemPoolAttrReleaseThreshold, &keep)) != cudaSuccess) {
+        cudaMemPoolDestroy(created);
+        return e;
+      }
+      pools[dev] = created;
+    }
+    pool = pools[dev];
+  }
+  return cudaMallocFromPoolAsync(p, bytes, pool, st);
+}
 
 int validate_dims(int p, int q, int nu, int nv) {
   if (p < 1 || q < 1 || p > NURBS_MAX_DEGREE || q > NURBS_MAX_DEGREE)
@@ -287,7 +326,7 @@ int nurbs_get_matrix_n_raw(double* matrix_n_dev, int p, int q, int nu, int nv, c
   size_t o_bv = o_bu + align256((size_t)nsu * k1 * k1 * 8);
   size_t total = o_bv + align256((size_t)nsv * k2 * k2 * 8);
   char* tmp = nullptr;
-  CUDA_TRY(cudaMallocAsync((void**)&tmp, total, st), "temporary allocation");
+  CUDA_TRY(tmp_alloc((void**)&tmp, total, st), "temporary allocation");
   SurfDev d{};
   d.p = p; d.q = q; d.nu = nu; d.nv = nv; d.ns_u = nsu; d.ns_v = nsv;
   d.knot_u = (const int*)(tmp + o_iu);
@@ -456,7 +495,7 @@ int nurbs_pcurve(nurbs_surface_t s, const double* C_dev, int64_t n, double* uv_d
   // pass-1 answers in scratch: uv (16 n), status (4 n), residual (8 n)
   const size_t oS = align256((size_t)n * 16), oR = oS + align256((size_t)n * 4), total = oR + align256((size_t)n * 8);
   char* buf = nullptr;
-  CUDA_TRY(cudaMallocAsync((void**)&buf, total, st), "p-curve scratch");
+  CUDA_TRY(tmp_alloc((void**)&buf, total, st), "p-curve scratch");
   double* uv0 = (double*)buf;
   int* st0 = (int*)(buf + oS);
   double* res0 = (double*)(buf + oR);
@@ -482,7 +521,7 @@ int nurbs_invert_count(nurbs_surface_t s, const double* P_dev, int64_t n, int pr
   const size_t oUV = 256, oS = oUV + align256((size_t)n * 16), oR = oS + align256((size_t)n * 4),
                total = oR + align256((size_t)n * 8);
   char* buf = nullptr;
-  CUDA_TRY(cudaMallocAsync((void**)&buf, total, st), "device buffers");
+  CUDA_TRY(tmp_alloc((void**)&buf, total, st), "device buffers");
   unsigned* counter = (unsigned*)buf;
   unsigned long long* counts = (unsigned long long*)(buf + 64);
   cudaError_t e = cudaMemsetAsync(buf, 0, 256, st);
@@ -509,7 +548,7 @@ int nurbs_invert_host(nurbs_surface_t s, const double* P_host, int64_t n, double
   size_t bP = (size_t)n * 24, bUV = (size_t)n * 16, bS = (size_t)n * 4, bR = (size_t)n * 8;
   size_t oUV = align256(bP), oS = oUV + align256(bUV), oR = oS + align256(bS), total = oR + align256(bR);
   char* buf = nullptr;
-  CUDA_TRY(cudaMallocAsync((void**)&buf, total, st), "device buffers");
+  CUDA_TRY(tmp_alloc((void**)&buf, total, st), "device buffers");
   cudaError_t e = cudaMemcpyAsync(buf, P_host, bP, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess)
     e = invert_on(s, (const double*)buf, n, (double*)(buf + oUV), (int*)(buf + oS), (double*)(buf + oR),

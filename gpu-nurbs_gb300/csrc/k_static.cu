@@ -1,7 +1,7 @@
 // GetMatrixN into a caller buffer without any device allocation.
 //
 // nurbs_get_matrix_n_raw needs scratch memory for the per-span basis-to-power matrices and
-// the span index tables, which it takes from cudaMallocAsync.  Some callers cannot allocate
+// the span index tables, which it takes from a stream-ordered pool.  Some callers cannot allocate
 // device memory at the point where they convert a surface: code that runs under a device
 // allocator it does not own (a host application whose caching allocator claims all free
 // memory, or a memory-budget admitter that forbids allocations outside its pool), and
