@@ -313,6 +313,19 @@ template <typename T>
 GN_HD v4<T> vmad(const v4<T>& a, T s, const v4<T>& c) {
   return {mad(a.x, s, c.x), mad(a.y, s, c.y), mad(a.z, s, c.z), mad(a.w, s, c.w)};
 }
+// FP32 on the device: two packed two-wide FMAs (sm_100 and later) instead of four, each
+// component the same round-to-nearest fused multiply-add as fmaf, so no result changes.
+template <>
+GN_HD v4<float> vmad<float>(const v4<float>& a, float s, const v4<float>& c) {
+#ifdef __CUDA_ARCH__
+  const float2 ss = make_float2(s, s);
+  const float2 lo = __ffma2_rn(make_float2(a.x, a.y), ss, make_float2(c.x, c.y));
+  const float2 hi = __ffma2_rn(make_float2(a.z, a.w), ss, make_float2(c.z, c.w));
+  return {lo.x, lo.y, hi.x, hi.y};
+#else
+  return {mad(a.x, s, c.x), mad(a.y, s, c.y), mad(a.z, s, c.z), mad(a.w, s, c.w)};
+#endif
+}
 
 // Coefficient loads through the read-only path.  An FP64 coefficient (32 bytes, 32-byte
 // aligned) is one 256-bit load; two adjacent FP32 coefficients starting at an even index of a
