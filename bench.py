@@ -1002,11 +1002,21 @@ def run_serving(a):
 
 def cpu_baseline(surf, P, sample, g_uv, g_st, g_res):
     """The oracle (C restatement of the reference FP64 path) on all host cores, bounded sample;
-    its results on that sample also check this run's mixed-precision results."""
+    its results on that sample also check this run's mixed-precision results.  `one_core`: the
+    same inversion on one host thread over the first eighth of the sample."""
+    import oracle as O
     Ps = P[:sample]
     par, dt = oracle_parity_sample(surf, Ps, g_uv[:sample], g_st[:sample], g_res[:sample])
+    o1 = O.OracleSurface(surf)
+    o1.tree()
+    P1 = Ps[:max(1, len(Ps) // 8)]
+    t0 = time.perf_counter()
+    o1.invert(P1, threads=1)
+    dt1 = time.perf_counter() - t0
     return ({"value": len(Ps) / dt, "unit": "inversions/s", "cores": host_cores(), "kind": "port",
-             "sample": f"{len(Ps)} queries of the same workload, the oracle's inversion, {dt:.2f} s wall"}, par)
+             "sample": f"{len(Ps)} queries of the same workload, the oracle's inversion, {dt:.2f} s wall",
+             "one_core": {"value": len(P1) / dt1, "unit": "inversions/s", "sample": f"{len(P1)} queries, 1 thread"}},
+            par)
 
 
 def run_reference(a):
