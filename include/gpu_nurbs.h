@@ -188,7 +188,8 @@ int nurbs_evaluate_random(const double* uv_dev, double* xyz_dev, int64_t n, cons
 int nurbs_build_tree(nurbs_surface_t s, int levels, void* stream);
 /* Copies the tree to host memory in the reference TreeNode order (kernel.cuh:30-39):
  * per node 10 doubles {uv.lb.x, uv.lb.y, uv.rt.x, uv.rt.y, lb.x, lb.y, lb.z, rt.x, rt.y, rt.z},
- * plus Divided[] and built[] (1 where the node was computed).  Synchronous. */
+ * plus Divided[] and built[] (1 where the node was computed).  Synchronous, on the legacy default
+ * stream: a tree built on a non-blocking stream must be complete first (that stream synchronised). */
 int nurbs_tree_export(nurbs_surface_t s, double* nodes_host, unsigned char* divided_host,
                       unsigned char* built_host);
 /* Candidate lists (the NewInverse scan, src/kernel/kernel.cu:456-457, over built nodes):
@@ -234,7 +235,8 @@ int nurbs_invert_quadtree(nurbs_surface_t s, const double* P_dev, int64_t n, dou
  * cone[65*20] FP32 records relative to the control net's centre (bound-box ball centre and radius,
  * cone axis, cos and sin of its half-angle (0 and 1: every direction), bound box rounded outward,
  * zero padding), lattice[65*81*3] the nodes' 9x9 lattice surface points (FP32, relative to the
- * same centre).  Synchronous. */
+ * same centre).  Synchronous, on the legacy default stream: cones built on a non-blocking stream
+ * (nurbs_surface_create, nurbs_build_tree) must be complete first. */
 int nurbs_normal_cones_export(nurbs_surface_t s, double* nbox_host, float* cone_host, float* lattice_host);
 
 /* p-curve of a 3-D curve on the surface: the parameters of its n ordered samples C_dev[3n].
