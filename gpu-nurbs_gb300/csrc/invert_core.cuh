@@ -34,6 +34,12 @@ constexpr float kDistinct32 = 1e-4f;    // FP32 minima: the same
 // the batch.
 constexpr int kSols = 4;                // FP64 mode: distinct minima kept per query
 constexpr int kSmemSpans = 256;         // breakpoint tables staged in shared memory up to this
+// MIXED: lanes whose seed has ended wait until this many are free (or no lane still iterates)
+// and then start their next seeds together, so that the divergent start (task decode, the first
+// step from the node centre) runs once for several lanes instead of every iteration for ~3.
+// Which lane runs which seed, and when, does not change any seed's arithmetic, and the
+// records are independent of arrival order, so results are the same for every value.
+constexpr int kStartBatch = 8;
 
 // Arithmetic below writes every product that feeds a sum as an explicit FMA (the translation
 // units are compiled with --fmad=false), so a seed's trajectory is the same bit for bit in
@@ -622,7 +628,8 @@ __device__ __forceinline__ void invert_chunk(Staged<KS, MODE>& sm, WarpWork<MODE
         first_step<float>(sm.cd32 + 9 * node, tx, ty, tz, sm.far32, sd);
       };
       if (active) start();
-      while (__any_sync(FULL, active)) {
+      bool waiting = false;  // finished, waiting for the next batch of starts
+      while (__any_sync(FULL, active || waiting)) {
         int res = kContinue;
         if (active) {
           res = iterate32<P, Q>(cx, tx, ty, tz, sd, dist);
@@ -664,13 +671,20 @@ __device__ __forceinline__ void invert_chunk(Staged<KS, MODE>& sm, WarpWork<MODE
           __syncwarp();
           fm &= fm - 1;
         }
-        unsigned dm = __ballot_sync(FULL, done);
         if (done) {
-          task = next + __popc(dm & lt_mask);
-          active = task < total;
-          if (active) start();
+          active = false;
+          waiting = true;
         }
-        next += __popc(dm);
+        const unsigned wm = __ballot_sync(FULL, waiting);
+        if (wm && (__popc(wm) >= kStartBatch || !__any_sync(FULL, active))) {
+          if (waiting) {
+            task = next + __popc(wm & lt_mask);
+            active = task < total;
+            waiting = false;
+            if (active) start();
+          }
+          next += __popc(wm);
+        }
       }
     } else {
       Seed<double> sd;
