@@ -383,7 +383,8 @@ __device__ __forceinline__ void project_chunk(const Staged<kSmemSpans, MODE>& sm
       sd.hv = 0;
     };
     if (active) start();
-    while (__any_sync(FULL, active)) {
+    bool waiting = false;  // finished, waiting for the next batch of starts (as the inversion's)
+    while (__any_sync(FULL, active || waiting)) {
       int res = kContinue;
       if (active) res = project_iterate32<P, Q>(cx, dom32, tx, ty, tz, sd, dist);
       const bool done = active && res != kContinue;
@@ -405,13 +406,20 @@ __device__ __forceinline__ void project_chunk(const Staged<kSmemSpans, MODE>& sm
         __syncwarp();
         fm &= fm - 1;
       }
-      const unsigned dm = __ballot_sync(FULL, done);
       if (done) {
-        task = next + __popc(dm & lt_mask);
-        active = task < total;
-        if (active) start();
+        active = false;
+        waiting = true;
       }
-      next += __popc(dm);
+      const unsigned wm = __ballot_sync(FULL, waiting);
+      if (wm && (__popc(wm) >= kStartBatch || !__any_sync(FULL, active))) {
+        if (waiting) {
+          task = next + __popc(wm & lt_mask);
+          active = task < total;
+          waiting = false;
+          if (active) start();
+        }
+        next += __popc(wm);
+      }
     }
   } else {
     PSeed sd;
