@@ -18,8 +18,11 @@
 // last warps finish while the others idle.  A query has anywhere from 0 to 65 candidate seeds
 // and a seed needs from 2 to 24 iterations, so one thread per query leaves most lanes of a warp
 // idle.  Each warp flattens its chunk's (query, seed) pairs into a task list (warp prefix sum
-// over the candidate counts) and every lane pulls the next task as soon as its seed converges
-// or fails, so all 32 lanes iterate until the warp's list is exhausted.  Finished seeds are merged
+// over the candidate counts) and lanes pull the next tasks as their seeds converge or fail, so
+// all 32 lanes iterate until the warp's list is exhausted: at once in the FP64 schedule, in
+// batches of eight free lanes in the mixed one (the start is divergent work, cheaper done once
+// for several lanes than every iteration for the two or three that just finished).  Finished
+// seeds are merged
 // into per-query records in shared memory (only results that can change a record, one lane at
 // a time).  Every seed runs to its own end (convergence, failure, the iteration cap, or an FP32
 // iterate two domain extents outside the domain), decided by the seed alone, so a query's result
@@ -29,13 +32,14 @@
 // Precision schedules (template MODE):
 //   FP64  — every evaluation, solve and update in FP64.
 //   MIXED — the seed exploration in FP32 (FP32 span matrices, FP32 breakpoints); the best
-//           minimum (plus a runner-up within 0.1 %) then takes the final two Newton steps in
-//           FP64: S, Su, Sv and the gradient J^T r in FP64, the Hessian's curvature term from
-//           FP32 second derivatives (it only sets the convergence rate), the 2x2 solve and the
-//           residual |S - P| at the returned point in FP64 (from the last step's S, Su, Sv and
-//           the step, a first-order update whose error is far below FP64 rounding).  Extra FP64
-//           steps (at most 4) run only when the second step is not yet below tolerance
-//           (near-singular or boundary cases).
+//           minimum (plus a distinct runner-up within 5 % of its distance, and the closest
+//           minimum just outside the domain when as close) then takes the final Newton steps in
+//           FP64: S, Su, Sv and the gradient J^T r in FP64, for the first three steps the
+//           Hessian's curvature term from FP32 second derivatives (it only sets the convergence
+//           rate; two steps normally reach the tolerance), the 2x2 solve and the residual
+//           |S - P| at the returned point in FP64 (from the last step's S, Su, Sv and the step, a
+//           first-order update whose error is far below FP64 rounding).  Later steps (at most 24
+//           in all) take the curvature in FP64 too, for nearly degenerate minima.
 #include "invert_core.cuh"
 
 namespace gnurbs {
