@@ -247,7 +247,8 @@ int nurbs_normal_cones_export(nurbs_surface_t s, double* nbox_host, float* cone_
  * step from the previous sample exceeds 4 |chord| / sigma_min(J): a seam, a fold, another
  * sheet), NURBS_PCURVE_AMBIGUOUS and NURBS_PCURVE_NOT_FOUND.  uv_dev[2n], status_dev[n],
  * residual_dev[n] as nurbs_invert.  Allocates and frees 48 n bytes of device scratch on
- * `stream`. */
+ * `stream`, from the library's stream-ordered pool (it keeps up to 512 MB of freed temporaries
+ * per device between calls). */
 #define NURBS_PCURVE_JUMP      1
 #define NURBS_PCURVE_AMBIGUOUS 2
 #define NURBS_PCURVE_NOT_FOUND 4
@@ -261,7 +262,8 @@ int nurbs_pcurve(nurbs_surface_t s, const double* C_dev, int64_t n, double* uv_d
 int nurbs_invert_count(nurbs_surface_t s, const double* P_dev, int64_t n, int precision,
                        unsigned long long* counts_host, void* stream);
 /* Same with host buffers: copies P in, runs, copies results out, waits.  Pinned host memory
- * gives the fastest copies. */
+ * gives the fastest copies; the 52 n bytes of device buffers come from the library's pool (as
+ * nurbs_pcurve's scratch). */
 int nurbs_invert_host(nurbs_surface_t s, const double* P_host, int64_t n, double* uv_host, int* status_host,
                       double* residual_host, int precision, void* stream);
 
