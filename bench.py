@@ -927,7 +927,8 @@ def serving_record(a, compact=False):
 
     def serve(rate, nreq, precision):
         arrival, kind, req_ids, qoff, P, uidx, sizes = trace(rate, nreq)
-        srv = gn.Server(pool, slots=a.slots, max_batch_queries=1 << 16, max_batch_requests=4096, precision=precision)
+        srv = gn.Server(pool, slots=a.slots, max_batch_queries=a.max_batch_queries, max_batch_requests=4096,
+                        precision=precision)
         clocks = Clocks(0)
         uv, st, res, lat, results, uids = srv.replay(arrival, kind, req_ids, qoff, P, upload_bank, uidx,
                                                      timeout_ms=600000)
@@ -975,7 +976,7 @@ def serving_record(a, compact=False):
         "scaling": "weak", "vs_baseline": None, "dtype": "fp32+fp64 (mixed)", "data": "synthetic (seeded)",
         "config": {"workload": f"serving: pool of {npool} surfaces (batched-workload distribution), 20 GB budget, "
                                "Poisson arrivals, Zipf(1.1) surfaces, 1..4096 queries/request log-uniform, "
-                               "10% uploads", "slots": a.slots, "max_batch_queries": 1 << 16,
+                               "10% uploads", "slots": a.slots, "max_batch_queries": a.max_batch_queries,
                    "queries_per_warp_chunk": a.serve_chunk, "rates_req_s": rates, "seconds_per_rate": serve_seconds},
         "peak": {"req_s": peak["achieved_req_s"], "queries_s": peak["achieved_queries_s"]},
         "half_peak": half, "sweep": sweep,
@@ -1068,6 +1069,7 @@ def main():
     ap.add_argument("--serve-seconds", type=float, default=1.0)
     ap.add_argument("--max-requests", type=int, default=40000)
     ap.add_argument("--slots", type=int, default=4)
+    ap.add_argument("--max-batch-queries", type=int, default=1 << 16, help="serving: queries per batch at most")
     ap.add_argument("--upload-frac", type=float, default=0.10)
     ap.add_argument("--serve-chunk", type=int, default=16, help="queries per warp chunk when serving")
     ap.add_argument("--surfaces", type=int, default=4096)
